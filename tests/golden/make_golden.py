@@ -1,0 +1,256 @@
+"""Generate the golden fixtures in this directory by running the exptool
+reference (imported from its source tree through ``refshim``) on small,
+seeded inputs.
+
+Run from the repository root:  python tests/golden/make_golden.py
+
+Outputs (all small):
+  sl_c{0,1,2}.cache / .model  SL basis tables (reference file formats)
+  eof_c1.cache, eof_c0.cache  EOF tables (old-style header; with / without density)
+  sl_c{0,1,2}.npz             particles, SL accumulate / evaluate outputs
+  eof_c1.npz, eof_c0.npz      particles, EOF accumulate / evaluate outputs
+  fields.npz                  Fields.return_forces_cart, leapfrog_integrate,
+                              compute_timestep outputs
+The table files are built by this project's generators; every output array is
+produced by the reference code.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+import refshim  # noqa: E402
+from exptool_gb300.tables.models import TruncatedHernquist  # noqa: E402
+from exptool_gb300.tables.sl_solver import SLBasis, write_sl_cache, write_model_file  # noqa: E402
+from exptool_gb300.tables.eof_builder import EOFTables  # noqa: E402
+from exptool_gb300.tables.samplers import hernquist_sample, disc_sample  # noqa: E402
+
+
+def P(name):
+    return os.path.join(HERE, name)
+
+
+class Data:
+    """Container with the ``.data`` dict of ``particle.Input`` plus the holder
+    attributes (``eof.accumulated_eval_particles`` reads ``.zpos`` too)."""
+
+    def __init__(self, x, y, z, m):
+        self.data = {"x": x, "y": y, "z": z, "m": m}
+        self.xpos, self.ypos, self.zpos, self.mass = x, y, z, m
+        self.time = 0.0
+        self.filename = "synthetic"
+        self.comp = "dark"
+
+
+def holder(ref, x, y, z, m):
+    h = ref.particle.holder()
+    h.xpos, h.ypos, h.zpos, h.mass = x, y, z, m
+    return h
+
+
+SL_EDGE = np.array([
+    [0.0, 0.0, 0.0, 1e-3],        # origin
+    [0.0, 0.0, 0.7, 1e-3],        # +z axis
+    [0.0, 0.0, -2.5, 1e-3],       # -z axis
+    [150.0, 20.0, -30.0, 1e-3],   # beyond rmax
+    [5e-5, -3e-5, 2e-5, 1e-3],    # inside rmin
+    [-2.0, -0.0, 0.5, 1e-3],      # phi = -pi branch
+    [-0.3, 0.4, 0.0, 2e-3],       # midplane
+])
+
+
+def sl_case(ref, cmap):
+    lmax, nmax, numr = 4, 6, 200
+    rmin, rmax, scale = 1e-3, 100.0, 1.0
+    model = TruncatedHernquist(a=1.0, rtrunc=100.0)
+    basis = SLBasis(model, lmax, nmax, rmin, rmax, nfine=8001)
+    cache, modelf = P(f"sl_c{cmap}.cache"), P(f"sl_c{cmap}.model")
+    write_sl_cache(cache, basis, numr, cmap, scale)
+    write_model_file(modelf, model, rmin * 0.5, rmax, npts=300, title="truncated Hernquist a=1 rt=100")
+    refshim.set_log_bounds(ref, rmin, rmax)
+    x, y, z, m = hernquist_sample(200, 100 + cmap)
+    x = np.concatenate([x, SL_EDGE[:, 0]])
+    y = np.concatenate([y, SL_EDGE[:, 1]])
+    z = np.concatenate([z, SL_EDGE[:, 2]])
+    m = np.concatenate([m, SL_EDGE[:, 3]])
+    sl = ref.spheresl
+    out = dict(x=x, y=y, z=z, m=m)
+    out["expcoef"] = sl.compute_coefficients_solitary(holder(ref, x, y, z, m), cache, modelf, 0, False)
+    out["expcoef_noodd"] = sl.compute_coefficients_solitary(holder(ref, x, y, z, m), cache, modelf, 0, True)
+    ec = out["expcoef"]
+    for tag, (L1, L2, NO) in {"aep": (-1000, 1000, False), "aep_l02": (0, 2, False),
+                               "aep_l13_noodd": (1, 3, True)}.items():
+        res = sl.all_eval_particles(Data(x, y, z, m), ec, cache, modelf, 0, L1=L1, L2=L2, NO_ODD=NO)
+        out[tag] = np.array(res)
+    # point-wise evaluators with the tables loaded the way Fields.prep_tables does
+    (lm, nm, nr, cm, r0, r1, sc, lt, evt, eft) = ref.halo_methods.read_cached_table(cache)
+    xi, rarr, p0, d0 = ref.halo_methods.init_table(modelf, nr, r0, r1, cmap=cm, scale=sc)
+    out.update(xi=xi, p0=p0, d0=d0)
+    rng = np.random.default_rng(300 + cmap)
+    npt = 24
+    pr = np.concatenate([10 ** rng.uniform(-3.5, 2.3, npt - 3), [1e-10, 1e-3, 100.0]])
+    pc = np.concatenate([rng.uniform(-1, 1, npt - 3), [1.0, -1.0, 0.0]])
+    pp = rng.uniform(-np.pi, np.pi, npt)
+    out.update(pt_r=pr, pt_costh=pc, pt_phi=pp)
+    ae = []
+    for i in range(npt):
+        ae.append(sl.all_eval(pr[i], pc[i], pp[i], ec, xi, p0, d0, cm, sc, lm, nm, evt, eft, no_odd=False))
+    out["all_eval"] = np.array(ae)
+    ae = []
+    for i in range(npt):
+        ae.append(sl.all_eval(pr[i], pc[i], pp[i], ec, xi, p0, d0, cm, sc, lm, nm, evt, eft, no_odd=True))
+    out["all_eval_noodd"] = np.array(ae)
+    for tag, (lu, nu, no) in {"force_eval": (lm, nm, False), "force_eval_l2n4": (2, 4, False),
+                               "force_eval_noodd": (lm, nm, True)}.items():
+        fe = []
+        for i in range(npt):
+            fe.append(sl.force_eval(pr[i], pc[i], pp[i], ec, xi, p0, d0, cm, sc, lu, nu, evt, eft, no_odd=no))
+        out[tag] = np.array(fe)
+    # radial function matrices and Legendre tables
+    dpf = [np.array(sl.get_halo_dens_pot_force(r, lm, nm, evt, eft, xi, d0, p0, cm, sc)) for r in pr]
+    out["dens_force_pot"] = np.array(dpf)
+    out["pot_matrix"] = np.array([sl.get_halo_pot_matrix(r, lm, nm, evt, eft, xi, p0, cm, sc) for r in pr])
+    lx = np.array([-1.0, -0.999999999, -0.5, 0.0, 0.3, 0.99999999, 1.0])
+    out["leg_x"] = lx
+    out["legendre"] = np.array([sl.legendre_R(6, v) for v in lx])
+    out["dlegendre"] = np.array([np.array(sl.dlegendre_R(6, v)) for v in lx])
+    out["factorial6"] = sl.factorial_return(6)
+    np.savez_compressed(P(f"sl_c{cmap}.npz"), **out)
+    print("sl", cmap, "done")
+    return cache, modelf, ec
+
+
+EOF_EDGE = np.array([
+    [0.0, 0.0, 0.0, 1e-3],        # origin (R = 1e-5 from the 1e-10 softening)
+    [40.0, 0.0, 0.1, 1e-3],       # beyond the radial table: extrapolation
+    [3.0, 4.0, 30.0, 1e-3],       # beyond the vertical table: extrapolation
+    [1.0, 1.0, -30.0, 1e-3],      # below the vertical table: clamp
+    [-2.0, -0.0, 0.5, 1e-3],      # phi = -pi branch
+    [1e-4, 1e-4, 0.0, 1e-3],      # inside rmin: clamp
+    [0.5, -0.5, 0.0, 2e-3],       # midplane
+])
+
+
+def eof_case(ref, tag, cmap, dens, mmax, norder, numx, seed):
+    tables = EOFTables(mmax=mmax, norder=norder, numx=numx, numy=numx, rmin=0.001, rmax=30.0,
+                       ascale=1.0, hscale=0.1, cmap=cmap, lmax_sph=12, nmax_sph=8,
+                       nsample=20000, seed=seed)
+    path = P(f"eof_{tag}.cache")
+    tables.write(path, dens=dens)
+    e = ref.eof
+    potC, rforceC, zforceC, densC, potS, rforceS, zforceS, densS = e.parse_eof(path)
+    rmin, rmax, nx, ny, mm, no, asc, hsc, cm, dn = e.eof_params(path)
+    XMIN, XMAX, dX, YMIN, YMAX, dY = e.set_table_params(RMAX=rmax, RMIN=rmin, ASCALE=asc, HSCALE=hsc,
+                                                        NUMX=nx, NUMY=ny, CMAP=cm)
+    x, y, z, m = disc_sample(200, seed + 1)
+    x = np.concatenate([x, EOF_EDGE[:, 0]])
+    y = np.concatenate([y, EOF_EDGE[:, 1]])
+    z = np.concatenate([z, EOF_EDGE[:, 2]])
+    m = np.concatenate([m, EOF_EDGE[:, 3]])
+    out = dict(x=x, y=y, z=z, m=m, table_params=np.array([XMIN, XMAX, dX, YMIN, YMAX, dY]))
+    a_cos, a_sin = e.accumulate(holder(ref, x, y, z, m), potC, potS, mm, no, XMIN, dX, YMIN, dY,
+                                nx, ny, asc, hsc, cm)
+    out.update(cos=a_cos, sin=a_sin)
+    c2, s2 = e.accumulate(Data(x, y, z, m), potC, potS, mm, no, XMIN, dX, YMIN, dY, nx, ny, asc, hsc, cm)
+    out.update(cos_data=c2, sin_data=s2)
+    mc = e.make_coefficients_multi(Data(x, y, z, m), 3, potC, potS, mm, no, XMIN, dX, YMIN, dY,
+                                   nx, ny, asc, hsc, cm)
+    out.update(cos_multi=mc[0], sin_multi=mc[1])
+    kw = dict(rmin=XMIN, dR=dX, zmin=YMIN, dZ=dY, numx=nx, numy=ny, MMAX=mm, NMAX=no,
+              ASCALE=asc, HSCALE=hsc, CMAP=cm, verbose=0)
+    out["aep"] = np.array(e.accumulated_eval_particles(Data(x, y, z, m), a_cos, a_sin, potC, rforceC, zforceC,
+                                                       potS, rforceS, zforceS, m1=0, m2=1000, **kw))
+    out["aep_m12"] = np.array(e.accumulated_eval_particles(Data(x, y, z, m), a_cos, a_sin, potC, rforceC,
+                                                           zforceC, potS, rforceS, zforceS, m1=1, m2=2, **kw))
+    if dens:
+        # the density branch is reachable only through eof_file (eof.py:1027-1035)
+        out["aep_dens"] = np.array(e.accumulated_eval_particles(Data(x, y, z, m), a_cos, a_sin, density=True,
+                                                                verbose=0, eof_file=path))
+    rng = np.random.default_rng(seed + 7)
+    npt = 20
+    pR = np.concatenate([rng.uniform(0.01, 12, npt - 4), [1e-5, 40.0, 2.0, 0.5]])
+    pz = np.concatenate([rng.normal(0, 0.3, npt - 4), [0.0, 0.1, 30.0, -30.0]])
+    pp = rng.uniform(-np.pi, np.pi, npt)
+    out.update(pt_R=pR, pt_z=pz, pt_phi=pp)
+    fk = dict(rmin=XMIN, dR=dX, zmin=YMIN, dZ=dY, numx=nx, numy=ny, ASCALE=asc, HSCALE=hsc, CMAP=cm)
+    for tg, (MM, NN, NO, PT) in {"force_eval": (mm, no, False, False), "force_eval_noodd": (mm, no, True, False),
+                                  "force_eval_m2n2": (min(2, mm), 2, False, False),
+                                  "force_eval_perturb": (mm, no, False, True)}.items():
+        res = []
+        for i in range(npt):
+            res.append(e.force_eval(pR[i], pz[i], pp[i], a_cos, a_sin, potC, rforceC, zforceC,
+                                    potS, rforceS, zforceS, MMAX=MM, NMAX=NN, no_odd=NO, perturb=PT, **fk))
+        out[tg] = np.array(res)
+    for tg, NO in {"acc_eval": False, "acc_eval_noodd": True}.items():
+        res = []
+        for i in range(npt):
+            res.append(e.accumulated_eval(pR[i], pz[i], pp[i], a_cos, a_sin, potC, rforceC, zforceC, densC,
+                                          potS, rforceS, zforceS, densS, MMAX=mm, NMAX=no, no_odd=NO, **fk))
+        out[tg] = np.array(res)
+    out["bins"] = np.array(e.return_bins(pR, pz, **fk))
+    np.savez_compressed(P(f"eof_{tag}.npz"), **out)
+    print("eof", tag, "done")
+    return path, a_cos, a_sin
+
+
+def fields_case(ref, sph_cache, sph_model, expcoef, eof_path, a_cos, a_sin):
+    refshim.set_log_bounds(ref, 1e-3, 100.0)
+    F = ref.potential.Fields("none", eof_path, sph_cache, sph_model, verbose=0)
+    F.EOF = ref.eof.EOF_Object()
+    F.EOF.eof_file, F.EOF.cos, F.EOF.sin = eof_path, a_cos, a_sin
+    F.SL = ref.spheresl.SL_Object()
+    F.SL.sph_file, F.SL.model_file, F.SL.expcoef = sph_cache, sph_model, expcoef
+    F.halofac = 0.8
+    F.prep_tables()
+    rng = np.random.default_rng(900)
+    npt = 16
+    px = rng.normal(0, 3, npt)
+    py = rng.normal(0, 3, npt)
+    pz = rng.normal(0, 0.5, npt)
+    rot = rng.uniform(0, 2 * np.pi, npt)
+    out = dict(px=px, py=py, pz=pz, rot=rot, halofac=0.8)
+    res = [F.return_forces_cart(px[i], py[i], pz[i], rotpos=rot[i]) for i in range(npt)]
+    out["forces_cart"] = np.array(res)
+    F.set_field_parameters(no_odd=True, halo_l=2, halo_n=4, disk_m=2, disk_n=2)
+    out["forces_cart_trunc"] = np.array([F.return_forces_cart(px[i], py[i], pz[i], rotpos=rot[i])
+                                         for i in range(npt)])
+    F.reset_field_parameters()
+    orbits = [([1.0, 0.0, 0.05], [0.0, 0.55, 0.02], 0.0, False, 1000, False),
+              ([0.3, -1.2, 0.0], [0.4, 0.1, 0.0], 0.2, True, 1000, False),
+              ([2.5, 0.5, -0.1], [-0.1, -0.4, 0.05], -0.15, False, 1, True)]
+    for k, (ip, iv, rf, force, apmax, apse) in enumerate(orbits):
+        O = ref.integrate.leapfrog_integrate(F, 60, 0.02, ip, iv, rotfreq=rf, force=force,
+                                             ap_max=apmax, apse=apse)
+        for key, val in O.items():
+            out[f"orbit{k}_{key}"] = np.asarray(val)
+    O = ref.integrate.leapfrog_integrate(F, 40, 0.02, [0.8, 0.2, 0.0], [0.1, 0.6, 0.0], no_odd=True,
+                                         halo_l=2, disk_m=2, disk_n=2)
+    for key, val in O.items():
+        out[f"orbit3_{key}"] = np.asarray(val)
+    F.reset_field_parameters()
+    out["timestep"] = np.array([ref.integrate.compute_timestep(F, [1.0, 0.2, 0.1], [0.1, 0.5, 0.0]),
+                                ref.integrate.compute_timestep(F, [4.0, -1.0, 0.3], [0.2, 0.3, 0.05], dyn_res=50.)])
+    np.savez_compressed(P("fields.npz"), **out)
+    print("fields done")
+
+
+def main():
+    ref = refshim.load()
+    sl_out = {}
+    for cmap in (0, 1, 2):
+        sl_out[cmap] = sl_case(ref, cmap)
+    eof_path, a_cos, a_sin = eof_case(ref, "c1", 1, True, 3, 3, 12, 500)
+    eof_case(ref, "c0", 0, False, 2, 3, 8, 600)
+    cache, modelf, ec = sl_out[2]
+    fields_case(ref, cache, modelf, ec, eof_path, a_cos, a_sin)
+
+
+if __name__ == "__main__":
+    main()
