@@ -1,0 +1,400 @@
+"""Benchmark of the basis-function-expansion hot path on GB300.
+
+Headline workload: the exponential-disc cylindrical EOF expansion (mmax=6,
+norder=18, 256x256 mapped (R, z) table, cmap=1; N = 1e6 equal-mass particles,
+exponential disc of scale length 1, sech^2 height 0.1, R < 20, |z| < 2,
+seed 1).  One step = coefficient accumulation over all N particles followed
+by potential/force evaluation at all N particles, the plain FP64 drop-in path.
+``value`` is particles per second through that step with the particles
+resident in HBM; ``e2e`` is the same through the public API
+(``eof.compute_coefficients`` + ``eof.compute_forces``) from pinned host
+arrays, host<->device copies included.  The same step on the mixed path
+(FP32 per-particle arithmetic, FP64 reductions) and the spherical workload
+(Hernquist halo, lmax=4, nmax=10, 2000-point log-r table, N=1e5) are reported
+beside it.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle; exptool itself is pure Python and cannot run on the GPU machine) on all
+host cores over a bounded sample of the same workload.
+
+Run:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG1 = dict(mmax=6, norder=18, numx=256, numy=256, rmin=0.001, rmax=30.0, ascale=1.0, hscale=0.1, cmap=1,
+            lmax_sph=32, nmax_sph=14, nsample=100000, seed=12345)
+N1 = 1_000_000
+CFG0 = dict(lmax=4, nmax=10, numr=2000, rmin=1e-3, rmax=100.0, cmap=2, scale=1.0)
+N0 = 100_000
+L2_BYTES = 129 * 1024 * 1024
+
+
+def cache_dir():
+    d = os.environ.get("XT_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "xt_bench_tables"))
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
+def eof_table_path():
+    """Build (once per machine) the disc EOF cache file."""
+    path = os.path.join(cache_dir(), "eof.disc.m6n18.256.cache")
+    if not os.path.exists(path):
+        from exptool_gb300.tables.eof_builder import make_disc_eof
+        tmp = path + f".tmp{os.getpid()}"
+        make_disc_eof(tmp, dens=True, **CFG1)
+        os.replace(tmp, path)
+    return path
+
+
+def sl_table_paths():
+    d = cache_dir()
+    cache = os.path.join(d, "SLGridSph.cache.hernquist_l4n10")
+    model = os.path.join(d, "SLGridSph.model.hernquist_l4n10")
+    if not (os.path.exists(cache) and os.path.exists(model)):
+        from exptool_gb300.tables.sl_solver import make_hernquist_sl
+        make_hernquist_sl(d, lmax=CFG0["lmax"], nmax=CFG0["nmax"], numr=CFG0["numr"], rmin=CFG0["rmin"],
+                          rmax=CFG0["rmax"], cmap=CFG0["cmap"], scale=CFG0["scale"], tag="hernquist_l4n10")
+    return cache, model
+
+
+def disc_particles(n=N1, seed=1):
+    from exptool_gb300.tables.samplers import disc_sample
+    return disc_sample(n, seed)
+
+
+def halo_particles(n=N0, seed=0):
+    from exptool_gb300.tables.samplers import hernquist_sample
+    return hernquist_sample(n, seed)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Sample nvidia-smi clocks and throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.out = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.out is None:
+            return None
+        self.out.seek(0)
+        rows = [r.split(",") for r in self.out.read().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    from exptool_gb300 import _lib, device as dev
+    from exptool_gb300.basis import eof, spheresl
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    path = eof_table_path()
+    x, y, z, m = disc_particles()
+    table = eof.table_from_file(path)
+    xd, yd, zd, md = (dev.to_dev(a) for a in (x, y, z, m))
+    ws = torch.empty(_lib.load().xt_cyl_accumulate_workspace(table.handle), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    want = [1, 1, 1, 1, 1, 1, 0, 0]
+
+    def step(prec):
+        c, s = table.accumulate(xd, yd, zd, md, precision=prec, workspace=ws)
+        f = table.prepare(c, s, precision=prec)
+        outs = table.eval_points(f, xd, yd, zd, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, want=want)
+        return c, s, outs
+
+    def timed(prec, steps, warmup, phases=False):
+        for _ in range(warmup):
+            step(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        tot = 0.0
+        ph = np.zeros(3)
+        for _ in range(steps):
+            flush.fill_(1.0)            # L2 flush outside the timed events
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record()
+            c, s = table.accumulate(xd, yd, zd, md, precision=prec, workspace=ws)
+            ev[1].record()
+            f = table.prepare(c, s, precision=prec)
+            ev[2].record()
+            table.eval_points(f, xd, yd, zd, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, want=want)
+            ev[3].record()
+            torch.cuda.synchronize()
+            t = [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+            ph += t
+            tot += sum(t)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            tot = float(tt.item())
+        return tot, ph / steps
+
+    K, W = args.steps, args.warmup
+    with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        tot64, ph64 = timed("f64", K, W)
+    clocks = clk.summary()
+    tot32, ph32 = timed("f32", K, W)
+    ms64 = tot64 / K
+    value = world * N1 / (ms64 * 1e-3)
+
+    # mixed-precision error against the FP64 path on the same particles
+    c64, s64, o64 = step("f64")
+    c32, s32, o32 = step("f32")
+    torch.cuda.synchronize()
+    coef_err = max(float((c32 - c64).abs().max() / c64.abs().max()), float((s32[1:] - s64[1:]).abs().max() /
+                                                                             s64[1:].abs().max()))
+    fr64, fz64, fr32, fz32 = o64[2], o64[4], o32[2], o32[4]
+    fmag = torch.sqrt(fr64 * fr64 + fz64 * fz64)
+    ferr = torch.sqrt((fr32 - fr64) ** 2 + (fz32 - fz64) ** 2) / fmag
+    force_err_med = float(ferr.median())
+
+    # e2e through the public API from pinned host memory
+    from exptool_gb300.io.particle import ParticleData
+    pinned = [torch.from_numpy(a).pin_memory() for a in (x, y, z, m)]
+    P = ParticleData(*(t.numpy() for t in pinned))
+    E = eof.compute_coefficients(P, path, verbose=0)
+    eof.compute_forces(P, E, verbose=0)
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(max(3, min(K, 10))):
+        t0 = time.perf_counter()
+        E = eof.compute_coefficients(P, path, verbose=0)
+        out = eof.compute_forces(P, E, verbose=0)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_times))
+    h2d = 2 * 4 * N1 * 8            # x y z m for accumulation, x y z (+z) for evaluation
+    d2h = 6 * N1 * 8 + 2 * 7 * 18 * 8
+
+    # spherical workload (halo, lmax 4)
+    cache, model = sl_table_paths()
+    hx, hy, hz, hm = halo_particles()
+    st = spheresl.table_from_files(cache, model)
+    hxd, hyd, hzd, hmd = (dev.to_dev(a) for a in (hx, hy, hz, hm))
+    sws = torch.empty(_lib.load().xt_sph_accumulate_workspace(st.handle), dtype=torch.uint8, device="cuda")
+
+    def sstep(prec):
+        ec = st.accumulate(hxd, hyd, hzd, hmd, precision=prec, workspace=sws)
+        f = st.prepare(ec, precision=prec)
+        st.eval_points(f, hxd, hyd, hzd, _lib.XT_SPH_ALL_EVAL_PARTICLES, _lib.XT_COORD_CART)
+    for _ in range(W):
+        sstep("f64")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        sstep("f64")
+    e1.record()
+    torch.cuda.synchronize()
+    sl_ms = e0.elapsed_time(e1) / K
+
+    peak, peak_kind = measured_peaks()
+    nnode = 257 * 257
+    field_bytes = nnode * 7 * 6 * 8
+    alg = {"accumulate": 32 * N1 + (7 + 6) * 18 * nnode * 8 + 13 * nnode * 8,
+           "prepare": (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * 8 + field_bytes,
+           "eval": 72 * N1 + field_bytes}
+    names = ["accumulate", "prepare", "eval"]
+    dom = int(np.argmax(ph64))
+    kname = {"accumulate": "k_cyl_deposit+k_cyl_contract", "prepare": "k_cyl_field", "eval": "k_cyl_eval"}
+    phases = {n: {"ms": round(float(ph64[i]), 4), "alg_bytes": alg[n],
+                  "gbs": round(alg[n] / (ph64[i] * 1e-3) / 1e9, 1)} for i, n in enumerate(names)}
+    ach = alg[names[dom]] / (ph64[dom] * 1e-3) / 1e9
+    line = {
+        "metric": "particle-force evals/s & coef-accum particles/s, learned/mixed vs plain FP64",
+        "value": value,
+        "unit": "particles/s (accumulate + force eval, EOF disc)",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": ms64,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded exponential disc, seed 1; tables from the project's EOF builder)",
+        "config": {"workload": "cylindrical EOF disc: accumulate + force eval", "particles_per_gpu": N1,
+                   "mmax": 6, "norder": 18, "numx": 256, "numy": 256, "cmap": 1,
+                   "l2": "flushed between timed steps (512 MB write outside the timed events)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * N1 / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients + eof.compute_forces, pinned numpy"},
+        "gpu_launches": 5 * K,
+        "roofline": {"bound": "hbm", "kernel": kname[names[dom]], "achieved": round(ach, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": None,
+                     "peak_source": peak_kind},
+        "phases_f64": phases,
+        "mixed_f32": {"value": world * N1 / (tot32 / K * 1e-3), "ms_per_step": tot32 / K,
+                      "phases_ms": [round(float(v), 4) for v in ph32], "coef_rel_err_vs_f64": coef_err,
+                      "force_rel_err_median_vs_f64": force_err_med},
+        "spherical_halo": {"workload": "Hernquist SL lmax=4 nmax=10 numr=2000 cmap=2, N=1e5, accumulate+eval",
+                           "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
+        "clocks": clocks,
+    }
+    return line
+
+
+# ------------------------------------------------------------------ CPU (oracle) arm
+def cpu_rate(n_sample, threads, table, x, y, z, m):
+    """Oracle accumulate + evaluate over n_sample particles on `threads` threads;
+    returns particles/s."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import eof as oeof
+    t = table
+    idx = np.arange(n_sample)
+    parts = np.array_split(idx, threads)
+    kw = dict(MMAX=t["mmax"], NMAX=t["norder"], XMIN=t["XMIN"], dX=t["dX"], YMIN=t["YMIN"], dY=t["dY"],
+              NUMX=t["numx"], NUMY=t["numy"], ASCALE=t["ascale"], HSCALE=t["hscale"], CMAP=t["cmap"])
+    tabs = [t[k] for k in ("potC", "rforceC", "zforceC", "potS", "rforceS", "zforceS")]
+
+    def acc(ix):
+        return oeof.accumulate(x[ix], y[ix], z[ix], m[ix], t["potC"], t["potS"], chunk=4096, **kw)
+
+    def ev(ix, c, s):
+        return oeof.accumulated_eval_particles(x[ix], y[ix], z[ix], c, s, *tabs, t["XMIN"], t["dX"], t["YMIN"],
+                                               t["dY"], t["numx"], t["numy"], t["mmax"], t["norder"], t["ascale"],
+                                               t["hscale"], t["cmap"], chunk=2048)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(acc, parts))
+        c = sum(r[0] for r in res)
+        s = sum(r[1] for r in res)
+        list(ex.map(lambda ix: ev(ix, c, s), parts))
+    return n_sample / (time.perf_counter() - t0)
+
+
+def cpu_baseline(target_s=12.0):
+    from oracle import eof as oeof
+    t = oeof.load_table(eof_table_path())
+    x, y, z, m = disc_particles()
+    threads = os.cpu_count() or 1
+    cal = cpu_rate(2000, threads, t, x, y, z, m)
+    n = int(min(N1, max(2000, cal * target_s)))
+    rate = cpu_rate(n, threads, t, x, y, z, m)
+    return {"value": rate, "unit": "particles/s", "cores": threads, "kind": "port",
+            "sample": f"{n} of {N1} disc particles, one accumulate + eval pass, oracle (vectorised NumPy "
+                      f"restatement of eof.accumulate / accumulated_eval_particles) on {threads} threads"}
+
+
+def reference_arm(args, rank, world):
+    from oracle import eof as oeof
+    t = oeof.load_table(eof_table_path())
+    x, y, z, m = disc_particles()
+    threads = os.cpu_count() or 1
+    cal = cpu_rate(2000, threads, t, x, y, z, m)
+    per_step = int(min(N1, max(2000, cal * 150.0 / max(1, args.steps + args.warmup))))
+    for _ in range(args.warmup):
+        cpu_rate(per_step, threads, t, x, y, z, m)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_rate(per_step, threads, t, x, y, z, m)
+    el = time.perf_counter() - t0
+    value = per_step * args.steps / el
+    sample = (f"{per_step} of {N1} disc particles per step, oracle (vectorised NumPy restatement of "
+              f"eof.accumulate / accumulated_eval_particles) on {threads} threads")
+    return {"impl": "reference", "metric": "particle-force evals/s & coef-accum particles/s, learned/mixed vs plain "
+                                           "FP64",
+            "value": value, "unit": "particles/s (accumulate + force eval, EOF disc)", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded exponential disc, seed 1)",
+            "config": {"workload": "cylindrical EOF disc: accumulate + force eval", "particles_per_gpu": N1,
+                       "mmax": 6, "norder": 18, "numx": 256, "numy": 256, "cmap": 1},
+            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(reference_arm(args, rank, world)))
+        return 0
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    line = gpu_arm(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,302 @@
+"""Cylindrical EOF expansion on the GPU, with the call signatures of
+``exptool/basis/eof.py``.
+
+Cache parsing is host-side I/O; accumulation and evaluation run in the CUDA
+library.  ``precision='f32'`` selects the mixed path.
+
+Behaviour that differs from the reference where the reference cannot run:
+* ``compute_coefficients`` moves particles with NaN positions to the origin
+  (the reference intends this but fails at ``if nanvals > 0`` on numpy >= 2,
+  eof.py:1194, and would edit ``.xpos`` while accumulating ``.data``);
+* ``compute_forces`` / ``find_forces_multi`` honour m1/m2 and work for any
+  ``nprocs`` (the reference's multi-process branch crashes, eof.py:1523).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .. import device as dev
+from ..io.particle import positions
+from .compatibility import r_to_xi, z_to_y
+
+
+class EOF_Object(object):
+    """Coefficient container (eof.py:1627-1636)."""
+    time = None
+    dump = None
+    comp = None
+    nbodies = None
+    mmax = None
+    nmax = None
+    eof_file = None
+    cos = None
+    sin = None
+    filename = None
+
+
+# ---------------------------------------------------------------- cache files
+HMAGIC = 0xC0A57A1
+
+
+def eof_params(file, verbose=0):
+    """Cache header (eof.py:98-200): returns rmin, rmax, numx, numy, mmax,
+    norder, ascale, hscale, cmap, dens.  New-style (YAML) headers need PyYAML."""
+    with open(file, "rb") as f:
+        tmagic = np.fromfile(f, dtype="<i4", count=1)
+        if tmagic.size == 1 and int(tmagic[0]) == HMAGIC:
+            ssize = int(np.fromfile(f, dtype="<i4", count=1)[0])
+            buf = f.read(ssize)
+            try:
+                import yaml
+            except ImportError as e:
+                raise RuntimeError("new-style EOF cache headers need PyYAML") from e
+            data = yaml.safe_load(buf)
+            cmap = data.get("cmap", data.get("cmapr"))
+            vals = (data["rmin"], data["rmax"], data["numx"], data["numy"], data["mmax"], data["norder"],
+                    data["ascl"], data["hscl"], cmap, data["dens"])
+        else:
+            f.seek(0)
+            a = np.fromfile(f, dtype="<u4", count=7)
+            b = np.fromfile(f, dtype="<f8", count=6)
+            if a.size != 7 or b.size != 6:
+                raise ValueError(f"{file}: truncated EOF cache header")
+            mmax, numx, numy, nmax, norder, dens, cmap = (int(v) for v in a)
+            rmin, rmax, ascale, hscale, cylmass, tnow = (float(v) for v in b)
+            vals = (rmin, rmax, numx, numy, mmax, norder, ascale, hscale, cmap, dens)
+    if verbose:
+        print("eof.eof_params: RMIN={0},RMAX={1},NUMX={2},NUMY={3},MMAX={4},NORDER={5},ASCALE={6},HSCALE={7},"
+              "CMAP={8},DENS={9}".format(*vals))
+    return vals
+
+
+def _data_offset(file):
+    with open(file, "rb") as f:
+        tmagic = np.fromfile(f, dtype="<i4", count=1)
+        if tmagic.size == 1 and int(tmagic[0]) == HMAGIC:
+            ssize = int(np.fromfile(f, dtype="<i4", count=1)[0])
+            return 8 + ssize
+    return 76
+
+
+def parse_eof(file, verbose=0):
+    """Cache tables (eof.py:224-313): potC, rforceC, zforceC, densC, potS,
+    rforceS, zforceS, densS, each (mmax+1, norder, numx+1, numy+1)."""
+    rmin, rmax, numx, numy, mmax, norder, ascale, hscale, cmap, dens = eof_params(file, verbose=verbose)
+    nb = (numx + 1) * (numy + 1)
+    nblk = 4 if dens == 1 else 3
+    raw = np.fromfile(file, dtype="<f8", offset=_data_offset(file))
+    need = ((mmax + 1) + mmax) * norder * nblk * nb
+    if raw.size < need:
+        raise ValueError(f"{file}: truncated EOF cache ({raw.size} of {need} values)")
+    shape = (mmax + 1, norder, numx + 1, numy + 1)
+    out = [np.zeros(shape) for _ in range(8)]
+    cosb = raw[:(mmax + 1) * norder * nblk * nb].reshape(mmax + 1, norder, nblk, numx + 1, numy + 1)
+    sinb = raw[(mmax + 1) * norder * nblk * nb:need].reshape(mmax, norder, nblk, numx + 1, numy + 1)
+    for k in range(3):
+        out[k][:] = cosb[:, :, k]
+        out[4 + k][1:] = sinb[:, :, k]
+    if dens == 1:
+        out[3][:] = cosb[:, :, 3]
+        out[7][1:] = sinb[:, :, 3]
+    return tuple(out)
+
+
+def set_table_params(RMAX=20.0, RMIN=0.001, ASCALE=0.01, HSCALE=0.001, NUMX=128, NUMY=64, CMAP=0):
+    """Scaled table bounds (eof.py:316-347): XMIN, XMAX, dX, YMIN, YMAX, dY."""
+    Rtable = np.sqrt(0.5) * RMAX
+    XMIN = float(r_to_xi(RMIN * ASCALE, CMAP, ASCALE))
+    XMAX = float(r_to_xi(Rtable * ASCALE, CMAP, ASCALE))
+    dX = (XMAX - XMIN) / NUMX
+    YMIN = float(z_to_y(-Rtable * ASCALE, HSCALE))
+    YMAX = float(z_to_y(Rtable * ASCALE, HSCALE))
+    dY = (YMAX - YMIN) / NUMY
+    return XMIN, XMAX, dX, YMIN, YMAX, dY
+
+
+# ---------------------------------------------------------------- table caches
+def table_from_file(eof_file) -> dev.CylTable:
+    key = ("cyl-file", dev.file_key(eof_file))
+
+    def make():
+        tabs = parse_eof(eof_file)
+        rmin, rmax, numx, numy, mmax, norder, ascale, hscale, cmap, dens = eof_params(eof_file)
+        XMIN, XMAX, dX, YMIN, YMAX, dY = set_table_params(RMAX=rmax, RMIN=rmin, ASCALE=ascale, HSCALE=hscale,
+                                                          NUMX=numx, NUMY=numy, CMAP=cmap)
+        return dev.CylTable(mmax, norder, numx, numy, cmap, dens, XMIN, dX, YMIN, dY, ascale, hscale, *tabs)
+
+    return dev.TABLES.get(key, make)
+
+
+def table_from_arrays(MMAX, NMAX, numx, numy, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, potC, rforceC=None,
+                      zforceC=None, potS=None, rforceS=None, zforceS=None, densC=None, densS=None) -> dev.CylTable:
+    arrs = [potC, rforceC, zforceC, potS, rforceS, zforceS, densC, densS]
+    present = tuple(a is not None for a in arrs)
+    fp = dev.fingerprint(*[a for a in arrs if a is not None])
+    key = ("cyl-arrays", fp, present, int(MMAX), int(NMAX), int(numx), int(numy), int(CMAP), float(XMIN), float(dX),
+           float(YMIN), float(dY), float(ASCALE), float(HSCALE))
+
+    def make():
+        dens = densC is not None and densS is not None
+        return dev.CylTable(MMAX, NMAX, numx, numy, CMAP, dens, XMIN, dX, YMIN, dY, ASCALE, HSCALE, potC, rforceC,
+                            zforceC, densC if dens else None, potS, rforceS, zforceS, densS if dens else None)
+
+    return dev.TABLES.get(key, make)
+
+
+def field_for(table, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64") -> dev.CylField:
+    if isinstance(cos, torch.Tensor):
+        return table.prepare(cos, sin, mmax_use, nmax_use, density, precision)
+    c = np.asarray(cos, dtype=np.float64)
+    s = np.asarray(sin, dtype=np.float64)
+    key = (dev.fingerprint(c, s), int(mmax_use), int(nmax_use), bool(density), precision)
+    return table.field_cache.get(key, lambda: table.prepare(c, s, mmax_use, nmax_use, density, precision))
+
+
+# ---------------------------------------------------------------- accumulation
+def accumulate(ParticleInstance, potC, potS, MMAX, NMAX, XMIN, dX, YMIN, dY, NUMX, NUMY, ASCALE, HSCALE, CMAP,
+               verbose=0, no_odd=False, VAR=0, precision="f64"):
+    """eof.accumulate (eof.py:492-640): returns (accum_cos, accum_sin), each
+    (MMAX+1, NMAX).  ``no_odd`` is accepted and, as in the reference, not
+    applied (its mask is never used, eof.py:544-549).  ``VAR`` sub-sampling
+    (unseeded jackknife draws) is not supported."""
+    if VAR:
+        raise NotImplementedError("VAR jackknife partitions are not part of the GPU path")
+    pC = np.asarray(potC)[:MMAX + 1, :NMAX]
+    pS = np.asarray(potS)[:MMAX + 1, :NMAX]
+    table = table_from_arrays(MMAX, NMAX, NUMX, NUMY, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, pC, potS=pS)
+    x, y, z, m = (dev.to_dev(a) for a in positions(ParticleInstance))
+    c, s = table.accumulate(x, y, z, m, precision=precision)
+    return c.cpu().numpy(), s.cpu().numpy()
+
+
+def make_coefficients_multi(ParticleInstance, nprocs, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy,
+                            ascale, hscale, cmap, verbose=0, no_odd=False, VAR=False, precision="f64"):
+    """eof.make_coefficients_multi (eof.py:1415-1455): one GPU pass (nprocs is
+    accepted for signature compatibility)."""
+    return accumulate(ParticleInstance, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy, ascale, hscale,
+                      cmap, verbose=verbose, no_odd=no_odd, VAR=VAR, precision=precision)
+
+
+def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max=-1, VAR=False, nanblock=False,
+                         precision="f64"):
+    """eof.compute_coefficients (eof.py:1158-1260): returns an EOF_Object with
+    .cos/.sin of shape (mmax+1, norder)."""
+    if VAR:
+        raise NotImplementedError("VAR jackknife partitions are not part of the GPU path")
+    x, y, z, m = positions(PSPInput)
+    bad = np.isnan(x) | np.isnan(y) | np.isnan(z)
+    if np.any(bad):
+        if verbose:
+            print("eof.compute_coefficients: NaN values found in output file {}.".format(
+                getattr(PSPInput, "filename", "")))
+        if not nanblock:
+            x, y, z = (np.where(bad, 0.0, a) for a in (x, y, z))
+    table = table_from_file(eof_file)
+    out = EOF_Object()
+    out.time = getattr(PSPInput, "time", None)
+    out.filename = getattr(PSPInput, "filename", None)
+    out.comp = getattr(PSPInput, "comp", None)
+    out.nbodies = m.size
+    out.eof_file = eof_file
+    out.mmax = table.mmax
+    out.nmax = table.norder
+    c, s = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision)
+    out.cos = c.cpu().numpy()
+    out.sin = s.cpu().numpy()
+    return out
+
+
+# ---------------------------------------------------------------- evaluation
+def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=0, zforceC=0, potS=0, rforceS=0,
+                               zforceS=0, rmin=0, dR=0, zmin=0, dZ=0, numx=0, numy=0, MMAX=6, NMAX=18, ASCALE=0.0,
+                               HSCALE=0.0, CMAP=0, m1=0, m2=1000, verbose=1, density=False, eof_file="",
+                               precision="f64"):
+    """eof.accumulated_eval_particles (eof.py:989-1144): returns
+    p0, p, fr, fp, fz, R (density: p0, p, d0, d, fr, fp, fz, R)."""
+    if eof_file != "":
+        table = table_from_file(eof_file)
+    else:
+        # the reference loops m <= MMAX over full coefficient rows (NMAX unused, eof.py:1093-1126)
+        sl = (slice(0, int(MMAX) + 1),)
+        nfull = np.asarray(potC).shape[1]
+        table = table_from_arrays(MMAX, nfull, numx, numy, CMAP, rmin, dR, zmin, dZ, ASCALE, HSCALE,
+                                  np.asarray(potC)[sl], np.asarray(rforceC)[sl], np.asarray(zforceC)[sl],
+                                  np.asarray(potS)[sl], np.asarray(rforceS)[sl], np.asarray(zforceS)[sl])
+        accum_cos = np.asarray(accum_cos)[sl]
+        accum_sin = np.asarray(accum_sin)[sl]
+    if density and not table.dens:
+        if verbose > 0:
+            print("eof.accumulated_eval_particles: cannot compute density (functions not specified). moving on "
+                  "without...")
+        density = False
+    field = field_for(table, accum_cos, accum_sin, density=density, precision=precision)
+    d = Particles.data
+    x = dev.to_dev(d["x"])
+    y = dev.to_dev(d["y"])
+    z = dev.to_dev(Particles.zpos if hasattr(Particles, "zpos") and Particles.zpos is not None else d["z"])
+    outs = table.eval_points(field, x, y, z, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, m1=m1, m2=m2,
+                             want=[1, 1, 1, 1, 1, 1, int(density), int(density)])
+    p0, p, fr, fp, fz, R, d0, dd = (t.cpu().numpy() if t is not None else None for t in outs)
+    if density:
+        return p0, p, d0, dd, fr, fp, fz, R
+    return p0, p, fr, fp, fz, R
+
+
+def compute_forces(PSPInput, EOF_Object, verbose=1, nprocs=-1, m1=0, m2=1000, density=False, precision="f64"):
+    """eof.compute_forces (eof.py:1263-1317)."""
+    return accumulated_eval_particles(PSPInput, EOF_Object.cos, EOF_Object.sin, m1=m1, m2=m2, verbose=verbose,
+                                      density=density, eof_file=EOF_Object.eof_file, precision=precision)
+
+
+def _pts(*vals):
+    arrs = [np.atleast_1d(np.asarray(v, dtype=np.float64)) for v in vals]
+    n = max(a.size for a in arrs)
+    arrs = [np.broadcast_to(a, (n,)).copy() if a.size != n else a for a in arrs]
+    return arrs, all(np.ndim(v) == 0 for v in vals)
+
+
+def force_eval(r, z, phi, accum_cos, accum_sin, potC, rforceC, zforceC, potS, rforceS, zforceS, rmin=0, dR=0, zmin=0,
+               dZ=0, numx=0, numy=0, fac=1.0, MMAX=6, NMAX=18, ASCALE=0.0, HSCALE=0.0, CMAP=0, no_odd=False,
+               perturb=False, precision="f64"):
+    """eof.force_eval (eof.py:756-870): returns (fr+fr0, fp, fz+fz0, p+p0, p0)
+    or with perturb (fr, fp, fz, p, p0, fr0, fz0).  r, z, phi may be arrays."""
+    MM = int(MMAX)
+    NN = int(NMAX)
+    full_m = np.asarray(potC).shape[0] - 1
+    full_n = np.asarray(potC).shape[1]
+    table = table_from_arrays(full_m, full_n, numx, numy, CMAP, rmin, dR, zmin, dZ, ASCALE, HSCALE, potC, rforceC,
+                              zforceC, potS, rforceS, zforceS)
+    field = field_for(table, accum_cos, accum_sin, mmax_use=min(MM, full_m), nmax_use=min(NN, full_n),
+                      precision=precision)
+    (ra, za, pa), scalar = _pts(r, z, phi)
+    outs = table.eval_points(field, dev.to_dev(ra), dev.to_dev(za), dev.to_dev(pa), _lib.XT_CYL_FORCE_EVAL,
+                             _lib.XT_COORD_CYL, mmax_use=min(MM, full_m), no_odd=no_odd, perturb=perturb)
+    k = 7 if perturb else 5
+    res = [t.cpu().numpy() for t in outs[:k]]
+    return tuple(float(v[0]) for v in res) if scalar else tuple(res)
+
+
+def accumulated_eval(r, z, phi, accum_cos, accum_sin, potC, rforceC, zforceC, densC, potS, rforceS, zforceS, densS,
+                     rmin=0, dR=0, zmin=0, dZ=0, numx=0, numy=0, fac=1.0, MMAX=6, NMAX=18, ASCALE=0.0, HSCALE=0.0,
+                     CMAP=0, no_odd=False, precision="f64"):
+    """eof.accumulated_eval (eof.py:874-929): returns p0, p, fr, fp, fz, d0, d
+    (p and d summed over all m, p0 and d0 their m = 0 parts)."""
+    # m <= MMAX over full coefficient rows, as eof.py:900-927 (NMAX unused)
+    MM = int(MMAX)
+    sl = (slice(0, MM + 1),)
+    NN = np.asarray(potC).shape[1]
+    table = table_from_arrays(MM, NN, numx, numy, CMAP, rmin, dR, zmin, dZ, ASCALE, HSCALE,
+                              np.asarray(potC)[sl], np.asarray(rforceC)[sl], np.asarray(zforceC)[sl],
+                              np.asarray(potS)[sl], np.asarray(rforceS)[sl], np.asarray(zforceS)[sl],
+                              np.asarray(densC)[sl], np.asarray(densS)[sl])
+    field = field_for(table, np.asarray(accum_cos)[sl], np.asarray(accum_sin)[sl], density=True,
+                      precision=precision)
+    (ra, za, pa), scalar = _pts(r, z, phi)
+    outs = table.eval_points(field, dev.to_dev(ra), dev.to_dev(za), dev.to_dev(pa), _lib.XT_CYL_ACCUMULATED_EVAL,
+                             _lib.XT_COORD_CYL, no_odd=no_odd)
+    res = [t.cpu().numpy() for t in outs[:7]]
+    return tuple(float(v[0]) for v in res) if scalar else tuple(res)

@@ -1,0 +1,179 @@
+"""Halo (SL) + disc (EOF) field composition on the GPU, with the interface of
+``exptool/basis/potential.py`` ``Fields``.
+
+``prep_tables`` uploads both bases once; the coefficient-contracted fields are
+prepared on first use and cached for the current coefficients, halofac and
+truncation settings, so repeated force calls (orbit integration) only run the
+per-point kernel.  Snapshot reading is outside this package:
+``total_coefficients`` takes in-memory particle containers instead of a file.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .. import device as dev
+from ..utils import halo_methods
+from . import eof, spheresl
+
+
+class Fields:
+    """Field of a halo + disc system (potential.py:49-963)."""
+
+    def __init__(self, infile, eof_file, sph_file, model_file, nhalo=1000000, transform=False, no_odd=False,
+                 centering=False, mutual_center=False, verbose=1, precision="f64", halo_correct_m=False):
+        self.filename = infile
+        self.eof_file = eof_file
+        self.sph_file = sph_file
+        self.model_file = model_file
+        self.nhalo = nhalo
+        self.transform = transform
+        self.no_odd = no_odd
+        self.centering = centering
+        self.mutual_center = mutual_center
+        self.verbose = verbose
+        self.halofac = 1.0
+        self.precision = precision
+        # The reference halo force (spheresl.force_eval) uses cos(l phi) for row
+        # (l, m) (spheresl.py:1173); halo_correct_m=True uses cos(m phi).
+        self.halo_correct_m = halo_correct_m
+        self._fcache = {}
+
+    # ------------------------------------------------------------ coefficients
+    def total_coefficients(self, disk_particles=None, halo_particles=None, halo_total=None):
+        """Accumulate disc (EOF) and halo (SL) coefficients from in-memory
+        particle containers (``.data`` dicts or holders); cf. potential.py:98-252.
+        halofac = len(halo_particles) / halo_total when halo_total is given."""
+        if disk_particles is None or halo_particles is None:
+            raise ValueError("total_coefficients needs disk_particles and halo_particles (no snapshot reader here)")
+        self.time = getattr(disk_particles, "time", None)
+        nh = np.asarray(halo_particles.data["m"] if hasattr(halo_particles, "data") else halo_particles.mass).size
+        self.halofac = float(nh) / float(halo_total) if halo_total else 1.0
+        self.xcen_disk = self.ycen_disk = self.zcen_disk = 0.0
+        self.xcen_halo = self.ycen_halo = self.zcen_halo = 0.0
+        self.EOF = eof.compute_coefficients(disk_particles, self.eof_file, verbose=self.verbose, no_odd=self.no_odd)
+        self.SL = spheresl.compute_coefficients(halo_particles, self.sph_file, self.model_file, verbose=self.verbose,
+                                                no_odd=self.no_odd)
+
+    # ------------------------------------------------------------ tables
+    def prep_tables(self):
+        """Read and upload both bases (potential.py:257-294)."""
+        try:
+            eof_file = self.EOF.eof_file
+        except AttributeError:
+            raise RuntimeError("potential.Fields.prep_tables: must first call total_coefficients.") from None
+        self.potC, self.rforceC, self.zforceC, self.densC, self.potS, self.rforceS, self.zforceS, self.densS = \
+            eof.parse_eof(eof_file)
+        (self.rmindisk, self.rmaxdisk, self.numx, self.numy, self.mmax, self.norder, self.ascale, self.hscale,
+         self.cmapdisk, self.densdisk) = eof.eof_params(eof_file)
+        self.XMIN, self.XMAX, self.dX, self.YMIN, self.YMAX, self.dY = eof.set_table_params(
+            RMAX=self.rmaxdisk, RMIN=self.rmindisk, ASCALE=self.ascale, HSCALE=self.hscale, NUMX=self.numx,
+            NUMY=self.numy, CMAP=self.cmapdisk)
+        self.disk_use_m = self.mmax
+        self.disk_use_n = self.norder
+        (self.lmaxhalo, self.nmaxhalo, self.numrhalo, self.cmaphalo, self.rminhalo, self.rmaxhalo, self.scalehalo,
+         self.ltablehalo, self.evtablehalo, self.eftablehalo) = halo_methods.read_cached_table(self.SL.sph_file)
+        self.xihalo, self.rarrhalo, self.p0halo, self.d0halo = halo_methods.init_table(
+            self.SL.model_file, self.numrhalo, self.rminhalo, self.rmaxhalo, cmap=self.cmaphalo, scale=self.scalehalo)
+        self.halo_use_l = self.lmaxhalo
+        self.halo_use_n = self.nmaxhalo
+        self._cyl = eof.table_from_file(eof_file)
+        self._sph = dev.SphTable(self.lmaxhalo, self.nmaxhalo, self.numrhalo, self.cmaphalo, self.rminhalo,
+                                 self.rmaxhalo, self.scalehalo, self.xihalo, self.p0halo, self.d0halo,
+                                 self.evtablehalo, self.eftablehalo)
+        self._fcache = {}
+
+    def set_field_parameters(self, no_odd=False, halo_l=-1, halo_n=-1, disk_m=-1, disk_n=-1):
+        """potential.py:365-377."""
+        self.no_odd = no_odd
+        if halo_l > -1:
+            self.halo_use_l = halo_l
+        if halo_n > -1:
+            self.halo_use_n = halo_n
+        if disk_m > -1:
+            self.disk_use_m = disk_m
+        if disk_n > -1:
+            self.disk_use_n = disk_n
+
+    def reset_field_parameters(self):
+        """potential.py:380-386."""
+        self.no_odd = False
+        self.halo_use_l = self.lmaxhalo
+        self.halo_use_n = self.nmaxhalo
+        self.disk_use_m = self.mmax
+        self.disk_use_n = self.norder
+
+    # ------------------------------------------------------------ device fields
+    def device_fields(self, precision=None):
+        """(SphField, CylField) for the current coefficients and settings."""
+        if not hasattr(self, "_sph"):
+            self.prep_tables()
+        precision = self.precision if precision is None else precision
+        ec = np.asarray(self.SL.expcoef, dtype=np.float64)
+        key = (dev.fingerprint(ec, self.EOF.cos, self.EOF.sin), float(self.halofac), int(self.halo_use_l),
+               int(self.halo_use_n), int(self.disk_use_m), int(self.disk_use_n), precision)
+        if key not in self._fcache:
+            lmax_use = min(int(self.halo_use_l), self.lmaxhalo)
+            nmax_use = min(int(self.halo_use_n), self.nmaxhalo)
+            sf = self._sph.prepare(ec, self.halofac, lmax_use, nmax_use, precision)
+            cf = self._cyl.prepare(np.asarray(self.EOF.cos), np.asarray(self.EOF.sin), min(int(self.disk_use_m),
+                                                                                          self.mmax),
+                                   min(int(self.disk_use_n), self.norder), False, precision)
+            self._fcache = {key: (sf, cf)}
+        return self._fcache[key]
+
+    def _halo_l(self):
+        return min(int(self.halo_use_l), self.lmaxhalo)
+
+    def _disk_m(self):
+        return min(int(self.disk_use_m), self.mmax)
+
+    def return_forces_cart(self, xval, yval, zval, rotpos=0.0):
+        """potential.py:445-497: fxdisk, fxhalo, fydisk, fyhalo, fzdisk, fzhalo,
+        diskp, halop+halop0.  Scalars or arrays (rotpos scalar or per point)."""
+        sf, cf = self.device_fields()
+        scalar = all(np.ndim(v) == 0 for v in (xval, yval, zval))
+        x = np.atleast_1d(np.asarray(xval, dtype=np.float64))
+        y = np.atleast_1d(np.asarray(yval, dtype=np.float64))
+        z = np.atleast_1d(np.asarray(zval, dtype=np.float64))
+        rot = None
+        rs = 0.0
+        if np.ndim(rotpos) == 0:
+            rs = float(rotpos)
+        else:
+            rot = dev.to_dev(np.asarray(rotpos, dtype=np.float64))
+        outs = dev.fields_forces(sf, cf, dev.to_dev(x), dev.to_dev(y), dev.to_dev(z), rotpos=rot, rotpos_scalar=rs,
+                                 halo_l=self._halo_l(), disk_m=self._disk_m(), no_odd=self.no_odd,
+                                 trig_l=not self.halo_correct_m)
+        res = [t.cpu().numpy() for t in outs]
+        return tuple(float(v[0]) for v in res) if scalar else tuple(res)
+
+    def return_forces_cyl(self, xval, yval, zval, rotpos=0.0):
+        """potential.py:389-442: diskfr, frhalo, diskfp, -halofp, diskfz, fzhalo,
+        -diskp, halop+halop0, with R = sqrt(x^2+y^2)+1e-10, r = sqrt(R^2+z^2)+1e-10."""
+        if not hasattr(self, "_sph"):
+            self.prep_tables()
+        scalar = all(np.ndim(v) == 0 for v in (xval, yval, zval))
+        x = np.atleast_1d(np.asarray(xval, dtype=np.float64))
+        y = np.atleast_1d(np.asarray(yval, dtype=np.float64))
+        z = np.atleast_1d(np.asarray(zval, dtype=np.float64))
+        r2 = np.sqrt(x * x + y * y) + 1.0e-10
+        r3 = np.sqrt(r2 * r2 + z * z) + 1.0e-10
+        costh = z / r3
+        phi = np.arctan2(y, x) + rotpos
+        sf, cf = self.device_fields()
+        from .. import _lib
+        dfr, dfp, dfz, dp, dp0 = self._cyl.eval_points(cf, dev.to_dev(r2), dev.to_dev(z), dev.to_dev(phi),
+                                                       _lib.XT_CYL_FORCE_EVAL, _lib.XT_COORD_CYL,
+                                                       mmax_use=self._disk_m(), no_odd=self.no_odd)[:5]
+        hfr, hft, hfp, hp, hp0 = self._sph.eval_points(sf, dev.to_dev(r3), dev.to_dev(costh), dev.to_dev(phi),
+                                                       _lib.XT_SPH_FORCE_EVAL, _lib.XT_COORD_SPH, no_odd=self.no_odd,
+                                                       lmax_use=self._halo_l(), trig_l=not self.halo_correct_m)[:5]
+        dfr, dfp, dfz, dp, hfr, hft, hfp, hp, hp0 = (t.cpu().numpy() for t in (dfr, dfp, dfz, dp, hfr, hft, hfp, hp,
+                                                                             hp0))
+        inner = r3 < np.min(self.xihalo)
+        hfp = np.where(inner, 0.0, hfp)
+        dfp = np.where(inner, 0.0, dfp)
+        frhalo = -1.0 * (r2 * hfr + z * hft) / r3
+        fzhalo = -1.0 * (z * hfr - r2 * hft) / r3
+        res = (dfr, frhalo, dfp, -1.0 * hfp, dfz, fzhalo, -1.0 * dp, hp + hp0)
+        return tuple(float(v[0]) for v in res) if scalar else res

@@ -1,0 +1,196 @@
+"""Spherical Sturm-Liouville expansion on the GPU, with the call signatures of
+``exptool/basis/spheresl.py``.
+
+Every function here marshals NumPy inputs to the device and calls the CUDA
+library (``include/exptool_gb300.h``); outputs come back as NumPy arrays owned
+by the caller.  Tables are uploaded once per (file, size, mtime) or per array
+content and reused.  ``precision='f32'`` selects the mixed path (FP32
+per-particle arithmetic, FP64 reductions); the default ``'f64'`` is the drop-in.
+
+Behaviour that differs from the reference where the reference cannot run:
+* cmap = 2 clamps use log(rmin), log(rmax) (the reference reads undefined
+  globals ``xmin``/``xmax``, spheresl.py:128-130);
+* ``eval_particles`` honours l1/l2 for any ``nprocs`` (the reference's
+  multi-process branch crashes, spheresl.py:507);
+* ``all_eval`` truncated to lmax keeps (lmax+1)^2 coefficient rows (the
+  reference keeps lmax+1 rows and then indexes past them, spheresl.py:1019).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .. import device as dev
+from ..io.particle import positions
+from ..utils import halo_methods
+
+
+class SL_Object(object):
+    """Coefficient container (spheresl.py:1377-1386)."""
+    time = None
+    dump = None
+    comp = None
+    nbodies = None
+    lmax = None
+    nmax = None
+    sph_file = None
+    model_file = None
+    expcoef = None
+    filename = None
+
+
+# ---------------------------------------------------------------- table caches
+def table_from_files(sph_file, mod_file) -> dev.SphTable:
+    key = ("sph-files", dev.file_key(sph_file), dev.file_key(mod_file))
+
+    def make():
+        lmax, nmax, numr, cmap, rmin, rmax, scale, lt, ev, ef = halo_methods.read_cached_table(sph_file)
+        xi, r, p0, d0 = halo_methods.init_table(mod_file, numr, rmin, rmax, cmap, scale)
+        return dev.SphTable(lmax, nmax, numr, cmap, rmin, rmax, scale, xi, p0, d0, ev, ef)
+
+    return dev.TABLES.get(key, make)
+
+
+def table_from_arrays(xi, p0, d0, cmap, scale, evtable, eftable) -> dev.SphTable:
+    xi = np.asarray(xi, dtype=np.float64)
+    ev = np.asarray(evtable, dtype=np.float64)
+    ef = np.asarray(eftable, dtype=np.float64)
+    key = ("sph-arrays", dev.fingerprint(xi, p0, d0, ev, ef), int(cmap), float(scale))
+
+    def make():
+        lmax = ev.shape[0] - 1
+        nmax = ev.shape[1]
+        if int(cmap) == 2:
+            rmin, rmax = float(np.exp(xi[0])), float(np.exp(xi[-1]))
+        else:
+            rmin, rmax = float(xi[0]), float(xi[-1])
+        return dev.SphTable(lmax, nmax, xi.size, int(cmap), rmin, rmax, float(scale), xi, p0, d0, ev, ef)
+
+    return dev.TABLES.get(key, make)
+
+
+def field_for(table, expcoef, coef_scale=1.0, lmax_use=-1, nmax_use=-1, precision="f64") -> dev.SphField:
+    ec = np.asarray(expcoef, dtype=np.float64) if not isinstance(expcoef, torch.Tensor) else expcoef
+    if isinstance(ec, torch.Tensor):
+        return table.prepare(ec, coef_scale, lmax_use, nmax_use, precision)
+    key = (dev.fingerprint(ec), float(coef_scale), int(lmax_use), int(nmax_use), precision)
+    return table.field_cache.get(key, lambda: table.prepare(ec, coef_scale, lmax_use, nmax_use, precision))
+
+
+def _full_coef(expcoef, table, lmax_use, nmax_use):
+    """Pad a truncated coefficient matrix to the table's full (rows, nmax)."""
+    ec = np.asarray(expcoef, dtype=np.float64)
+    full = np.zeros((table.nrow, table.nmax))
+    rows = min(ec.shape[0], table.nrow)
+    cols = min(ec.shape[1], table.nmax)
+    full[:rows, :cols] = ec[:rows, :cols]
+    return full
+
+
+# ---------------------------------------------------------------- accumulation
+def compute_coefficients_solitary(ParticleInstance, sph_file, model_file, verbose=0, no_odd=False, precision="f64"):
+    """spheresl.compute_coefficients_solitary (spheresl.py:567-656): returns
+    expcoef ((lmax+1)^2, nmax)."""
+    table = table_from_files(sph_file, model_file)
+    x, y, z, m = (dev.to_dev(a) for a in positions(ParticleInstance))
+    ec = table.accumulate(x, y, z, m, no_odd=no_odd, precision=precision)
+    return ec.cpu().numpy()
+
+
+def compute_coefficients(PSPInput, sph_file, mod_file, verbose=1, no_odd=False, precision="f64"):
+    """spheresl.compute_coefficients (spheresl.py:439-475): one GPU pass over
+    all particles (the reference's process pool and object-array sum are not
+    needed).  Returns an SL_Object."""
+    out = SL_Object()
+    out.time = getattr(PSPInput, "time", None)
+    out.filename = getattr(PSPInput, "filename", None)
+    out.comp = getattr(PSPInput, "comp", None)
+    x, y, z, m = positions(PSPInput)
+    out.nbodies = m.size
+    out.sph_file = sph_file
+    out.model_file = mod_file
+    table = table_from_files(sph_file, mod_file)
+    out.lmax = table.lmax
+    out.nmax = table.nmax
+    xd, yd, zd, md = (dev.to_dev(a) for a in (x, y, z, m))
+    out.expcoef = table.accumulate(xd, yd, zd, md, no_odd=no_odd, precision=precision).cpu().numpy()
+    return out
+
+
+# ---------------------------------------------------------------- evaluation
+def all_eval_particles(Particles, expcoef, sph_file, mod_file, verbose=0, L1=-1000, L2=1000, NO_ODD=False,
+                       precision="f64"):
+    """spheresl.all_eval_particles (spheresl.py:1240-1362): returns
+    den0, den1, pot0, pot1, potr, pott, potp, rr."""
+    table = table_from_files(sph_file, mod_file)
+    field = field_for(table, expcoef, precision=precision)
+    d = Particles.data
+    a, b, c = (dev.to_dev(d[k]) for k in ("x", "y", "z"))
+    outs = table.eval_points(field, a, b, c, _lib.XT_SPH_ALL_EVAL_PARTICLES, _lib.XT_COORD_CART, L1=L1, L2=L2,
+                             no_odd=NO_ODD)
+    return tuple(t.cpu().numpy() for t in outs)
+
+
+def eval_particles(ParticleInstance, expcoef, sph_file, mod_file, nprocs=-1, verbose=1, l1=0, l2=1000,
+                   precision="f64"):
+    """spheresl.eval_particles (spheresl.py:502-528)."""
+    return all_eval_particles(ParticleInstance, expcoef, sph_file, mod_file, verbose, L1=l1, L2=l2,
+                              precision=precision)
+
+
+def _points(*vals):
+    arrs = [np.atleast_1d(np.asarray(v, dtype=np.float64)) for v in vals]
+    n = max(a.size for a in arrs)
+    arrs = [np.broadcast_to(a, (n,)) if a.size != n else a for a in arrs]
+    scalar = all(np.ndim(v) == 0 for v in vals)
+    return arrs, scalar
+
+
+def _point_eval(mode, r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax, evtable, eftable, no_odd,
+                trig_l, precision):
+    table = table_from_arrays(xi, p0, d0, cmap, scale, evtable, eftable)
+    lmax = table.lmax if lmax is None else int(lmax)
+    nmax = table.nmax if nmax is None else int(nmax)
+    lmax_use = lmax if lmax < table.lmax else table.lmax
+    nmax_use = nmax if nmax < table.nmax else table.nmax
+    coef = _full_coef(expcoef, table, lmax_use, nmax_use)
+    field = field_for(table, coef, 1.0, lmax_use, nmax_use, precision)
+    (ra, ca, pa), scalar = _points(r, costh, phi)
+    outs = table.eval_points(field, dev.to_dev(ra), dev.to_dev(ca), dev.to_dev(pa), mode, _lib.XT_COORD_SPH,
+                             no_odd=no_odd, lmax_use=lmax_use, trig_l=trig_l)
+    return outs, scalar
+
+
+def all_eval(r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax, evtable, eftable, no_odd=False, verbose=0,
+             precision="f64"):
+    """spheresl.all_eval (spheresl.py:987-1102); r, costh, phi may be arrays.
+    Returns den0, den1, pot0, pot1, potr, pott, potp."""
+    outs, scalar = _point_eval(_lib.XT_SPH_ALL_EVAL, r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax,
+                               evtable, eftable, no_odd, False, precision)
+    res = [t.cpu().numpy() for t in outs[:7]]
+    return tuple(float(v[0]) for v in res) if scalar else tuple(res)
+
+
+def force_eval(r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax, evtable, eftable, no_odd=False,
+               verbose=0, correct_m=False, precision="f64"):
+    """spheresl.force_eval (spheresl.py:1107-1234): returns potr, pott, potp,
+    pot1, pot0.  By default the azimuthal factor of row (l, m) is cos(l phi) /
+    sin(l phi) exactly as the reference computes it (spheresl.py:1173);
+    ``correct_m=True`` uses cos(m phi) / sin(m phi) as ``all_eval`` does."""
+    outs, scalar = _point_eval(_lib.XT_SPH_FORCE_EVAL, r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax,
+                               evtable, eftable, no_odd, not correct_m, precision)
+    res = [t.cpu().numpy() for t in outs[:5]]
+    return tuple(float(v[0]) for v in res) if scalar else tuple(res)
+
+
+def factorial_return(lmax):
+    """spheresl.factorial_return (spheresl.py:823-863), host-side constants."""
+    from scipy.special import gammaln
+    f = np.zeros((lmax + 1, lmax + 1))
+    for l in range(lmax + 1):
+        for m in range(l + 1):
+            f[l, m] = np.sqrt((0.5 * l + 0.25) / np.pi * np.exp(gammaln(1.0 + l - m) - gammaln(1.0 + l + m)))
+            if m != 0:
+                f[l, m] *= np.sqrt(2.0)
+    return f

@@ -1,0 +1,106 @@
+// Shared host/device helpers of the exptool_gb300 CUDA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+#include "../../include/exptool_gb300.h"
+
+namespace xt {
+
+// Loops over l, m are fully unrolled (register-resident Legendre tables) for
+// lmax <= 8; the lmax <= 32 fallback keeps them rolled to bound code size.
+template <int L>
+constexpr int unr_v = (L <= 8) ? 64 : 1;
+
+// ------------------------------------------------------------------ errors
+void set_error(const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define XT_CUDA(call)                                              \
+  do {                                                             \
+    cudaError_t _e = (call);                                       \
+    if (_e != cudaSuccess) return ::xt::cuda_fail(_e, #call);      \
+  } while (0)
+
+#define XT_CHECK_LAUNCH(what)                                      \
+  do {                                                             \
+    cudaError_t _e = cudaGetLastError();                           \
+    if (_e != cudaSuccess) return ::xt::cuda_fail(_e, what);       \
+  } while (0)
+
+#define XT_REQUIRE(cond, ...)                                      \
+  do {                                                             \
+    if (!(cond)) {                                                 \
+      ::xt::set_error(__VA_ARGS__);                                \
+      return XT_ERR_ARG;                                           \
+    }                                                              \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Grid size for a grid-stride loop over n items: a multiple of the SM count
+// (152 on GB300) times the resident blocks per SM, capped by the work.
+int grid_for(long long n, int block, int blocks_per_sm = 8);
+
+// ------------------------------------------------------------------ device math
+constexpr double PI = 3.14159265358979323846;
+
+template <typename R>
+__device__ __forceinline__ bool finite(R v) { return isfinite(v); }
+
+// compatibility.r_to_xi (exptool/basis/compatibility.py:16-49): r < 0 maps to 0.
+template <typename R>
+__device__ __forceinline__ R r_to_xi(R r, int cmap, R scale) {
+  R out;
+  if (cmap == 1) {
+    out = (r / scale - R(1)) / (r / scale + R(1));
+  } else if (cmap == 2) {
+    out = log(r);
+  } else {
+    out = r;
+  }
+  return (r < R(0)) ? R(0) : out;
+}
+
+// compatibility.d_xi_to_r (compatibility.py:65-80)
+template <typename R>
+__device__ __forceinline__ R d_xi_to_r(R xi, int cmap, R scale) {
+  if (cmap == 1) return R(0.5) * (R(1) - xi) * (R(1) - xi) / scale;
+  if (cmap == 2) return exp(-xi);
+  return R(1);
+}
+
+// compatibility.z_to_y (compatibility.py:83-91): z/(|z|+1e-8) * asinh(|z/h|)
+template <typename R>
+__device__ __forceinline__ R z_to_y(R z, R hscale) {
+  return (z / (fabs(z) + R(1.0e-8))) * asinh(fabs(z / hscale));
+}
+
+// cos(phi), sin(phi) of phi = atan2(y, x) without the arctangent:
+// x/rho, y/rho; rho == 0 keeps atan2's signed-zero conventions.
+template <typename R>
+__device__ __forceinline__ void unit_phi(R x, R y, R& c, R& s) {
+  R rho = sqrt(x * x + y * y);
+  if (rho > R(0)) {
+    R inv = R(1) / rho;
+    c = x * inv;
+    s = y * inv;
+  } else {
+    R p = atan2(y, x);
+    c = cos(p);
+    s = sin(p);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void sincos_r(R a, R* s, R* c);
+template <>
+__device__ __forceinline__ void sincos_r<double>(double a, double* s, double* c) { sincos(a, s, c); }
+template <>
+__device__ __forceinline__ void sincos_r<float>(float a, float* s, float* c) { sincosf(a, s, c); }
+
+}  // namespace xt

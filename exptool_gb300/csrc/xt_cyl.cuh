@@ -1,0 +1,124 @@
+// Cylindrical EOF basis: device tables and per-point kernels.
+//
+// Reference: exptool/basis/eof.py (return_bins :354-427, get_pot :430-457,
+// accumulate :492-640, force_eval :756-870, accumulated_eval :874-929,
+// accumulated_eval_particles :989-1144).
+#pragma once
+
+#include "xt_common.cuh"
+
+namespace xt {
+
+template <typename R>
+struct CylTab {
+  int mmax, norder, numx, numy, cmap;
+  R XMIN, dX, YMIN, dY, ascale, hscale;
+};
+
+// eof.return_bins + bilinear weights (eof.py:354-427, 436-449).  The lower
+// clamps zero both index and coordinate; the upper clamps change only the
+// index (the coordinate clamp that follows tests the clamped index and never
+// fires), so points beyond the last cell are linearly extrapolated.
+template <typename R>
+struct CylBins {
+  int node;       // ix*(numy+1) + iy
+  R c00, c10, c01, c11;
+};
+
+template <typename R>
+__device__ __forceinline__ CylBins<R> cyl_bins(const CylTab<R>& T, R Rcyl, R z) {
+  R X = (r_to_xi(Rcyl, T.cmap, T.ascale) - T.XMIN) / T.dX;
+  R Y = (z_to_y(z, T.hscale) - T.YMIN) / T.dY;
+  R fx = trunc(X), fy = trunc(Y);
+  if (!(fx >= R(0))) fx = R(0);       // negative or NaN
+  if (!(fy >= R(0))) fy = R(0);
+  if (X < R(0)) X = R(0);
+  if (Y < R(0)) Y = R(0);
+  if (fx >= R(T.numx)) fx = R(T.numx - 1);
+  if (fy >= R(T.numy)) fy = R(T.numy - 1);
+  const int ix = (int)fx, iy = (int)fy;
+  const R delx0 = fx + R(1) - X, dely0 = fy + R(1) - Y;
+  const R delx1 = X - fx, dely1 = Y - fy;
+  CylBins<R> B;
+  B.node = ix * (T.numy + 1) + iy;
+  B.c00 = delx0 * dely0;
+  B.c10 = delx1 * dely0;
+  B.c01 = delx0 * dely1;
+  B.c11 = delx1 * dely1;
+  return B;
+}
+
+struct CylEvalOpts {
+  int mode;       // XT_CYL_*
+  int m1, m2;     // accumulated_eval_particles m range
+  int mmax_use;
+  int no_odd;
+  int perturb;
+  int density;
+  int nf;         // fields per (node, m): 6 or 8
+};
+
+// Field F: per node, per m, nf values
+//   [PC RC ZC PS RS ZS (DC DS)] = sum_n {cos,sin}[m,n] * {pot,rforce,zforce,dens}{C,S}[m,n,node]
+// One point: out = p0 p fr fp fz d0 d fr0 fz0 (mode-specific meaning).
+template <typename R, int MCAP>
+__device__ __forceinline__ void cyl_eval_point(const CylTab<R>& T, const R* __restrict__ F, R Rcyl, R z, R c1,
+                                               R s1, const CylEvalOpts& o, R out[9]) {
+  const CylBins<R> B = cyl_bins(T, Rcyl, z);
+  const int ny1 = T.numy + 1;
+  const int stride = (T.mmax + 1) * o.nf;
+  const R* f00 = F + (size_t)B.node * stride;
+  const R* f01 = f00 + stride;                 // iy+1
+  const R* f10 = f00 + (size_t)ny1 * stride;   // ix+1
+  const R* f11 = f10 + stride;
+  R p0 = 0, p = 0, fr = 0, fp = 0, fz = 0, d0 = 0, d = 0, fr0 = 0, fz0 = 0;
+  R cprev = R(1), sprev = R(0), ccur = c1, scur = s1;   // cos/sin of m phi by recurrence
+  const int mtop = o.mmax_use;
+#pragma unroll 1
+  for (int m = 0; m <= mtop; ++m) {
+    R c, s;
+    if (m == 0) { c = R(1); s = R(0); }
+    else if (m == 1) { c = c1; s = s1; }
+    else {
+      c = R(2) * c1 * ccur - cprev;
+      s = R(2) * c1 * scur - sprev;
+      cprev = ccur; sprev = scur; ccur = c; scur = s;
+    }
+    bool use = true;
+    if (o.mode == XT_CYL_ACCUMULATED_EVAL_PARTICLES) use = (m >= o.m1 && m <= o.m2);
+    if (o.mode == XT_CYL_ACCUMULATED_EVAL) use = !(o.no_odd && (m & 1));
+    if (!use) continue;
+    const int b = m * o.nf;
+    R v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k >= o.nf) break;
+      v[k] = f00[b + k] * B.c00 + f10[b + k] * B.c10 + f01[b + k] * B.c01 + f11[b + k] * B.c11;
+    }
+    const R pm = c * v[0] + s * v[3];
+    const R frm = c * v[1] + s * v[4];
+    const R fzm = c * v[2] + s * v[5];
+    const R fpm = R(m) * (s * v[0] - c * v[3]);
+    const R dm = (o.nf == 8) ? (c * v[6] + s * v[7]) : R(0);
+    if (o.mode == XT_CYL_FORCE_EVAL) {
+      if (m == 0) {
+        p0 = pm; fr0 = frm; fz0 = fzm;
+      } else {
+        // odd-m mask |cos(pi/2 m)| of eof.force_eval (eof.py:822-826)
+        const R mask = o.no_odd ? R(fabs(cos((PI / 2.0) * (double)m))) : R(1);
+        p += mask * pm; fr += mask * frm; fz += mask * fzm; fp += mask * fpm;
+      }
+    } else if (o.mode == XT_CYL_ACCUMULATED_EVAL_PARTICLES) {
+      if (m == 0) { p0 = pm; d0 = dm; }
+      else { p += pm; d += dm; }
+      fr += frm; fz += fzm; fp += fpm;
+    } else {  // ACCUMULATED_EVAL: totals, with p0/d0 the m = 0 parts
+      p += pm; d += dm; fr += frm; fz += fzm; fp += fpm;
+      if (m == 0) { p0 = p; d0 = d; }
+    }
+  }
+  out[0] = p0; out[1] = p; out[2] = fr; out[3] = fp; out[4] = fz;
+  out[5] = d0; out[6] = d; out[7] = fr0; out[8] = fz0;
+}
+
+}  // namespace xt

@@ -1,0 +1,292 @@
+"""Device-side objects: uploaded SL / EOF tables and the calls on them.
+
+``SphTable`` and ``CylTable`` own a C-ABI table handle; their methods take and
+return torch CUDA tensors and launch on the current torch stream.  Table
+handles are cached by file identity (path, size, mtime) or by the identity
+and a content fingerprint of the NumPy arrays they were built from, so the
+reference-style APIs that pass tables on every call upload them once.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_F = {"f64": _lib.XT_F64, "f32": _lib.XT_F32, _lib.XT_F64: _lib.XT_F64, _lib.XT_F32: _lib.XT_F32}
+
+
+def precision_code(p) -> int:
+    try:
+        return _F[p]
+    except KeyError:
+        raise ValueError(f"precision must be 'f64' or 'f32', got {p!r}") from None
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("exptool_gb300 needs a CUDA device (GB300, sm_103a); none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def to_dev(a, dtype=torch.float64) -> torch.Tensor:
+    """numpy / tensor -> contiguous CUDA tensor of ``dtype``."""
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device(), dtype=dtype)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64))).to(device(), dtype=dtype)
+    return t.contiguous()
+
+
+def dptr(t) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def fingerprint(*arrays) -> str:
+    """Cheap content fingerprint of numpy arrays (shape, dtype and a hash of a
+    bounded strided sample plus the full bytes of small arrays)."""
+    h = hashlib.blake2b(digest_size=16)
+    for a in arrays:
+        a = np.asarray(a)
+        h.update(str((a.shape, a.dtype.str)).encode())
+        flat = a.reshape(-1)
+        if flat.size <= 1 << 17:
+            h.update(np.ascontiguousarray(flat).tobytes())
+        else:
+            step = max(1, flat.size // (1 << 16))
+            h.update(np.ascontiguousarray(flat[::step]).tobytes())
+            h.update(np.ascontiguousarray(flat[-64:]).tobytes())
+    return h.hexdigest()
+
+
+def file_key(path: str):
+    st = os.stat(path)
+    return (os.path.abspath(path), st.st_size, st.st_mtime_ns)
+
+
+class _Cache:
+    def __init__(self, limit=8):
+        self._d = {}
+        self._lock = threading.Lock()
+        self._limit = limit
+
+    def get(self, key, make):
+        with self._lock:
+            if key in self._d:
+                v = self._d.pop(key)
+                self._d[key] = v
+                return v
+        v = make()
+        with self._lock:
+            self._d[key] = v
+            while len(self._d) > self._limit:
+                self._d.pop(next(iter(self._d)))
+        return v
+
+
+TABLES = _Cache()
+
+
+class SphTable:
+    """Uploaded spherical SL basis (halo_methods.read_cached_table + init_table)."""
+
+    def __init__(self, lmax, nmax, numr, cmap, rmin, rmax, scale, xi, p0, d0, ev, ef):
+        device()
+        lib = _lib.load()
+        self.lmax, self.nmax, self.numr, self.cmap = int(lmax), int(nmax), int(numr), int(cmap)
+        self.rmin, self.rmax, self.scale = float(rmin), float(rmax), float(scale)
+        self.xi = np.ascontiguousarray(xi, dtype=np.float64)
+        self.xi_min = float(np.min(self.xi))
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xi, p0, d0, ev, ef)]
+        if arrs[0].size != self.numr or arrs[3].shape != (self.lmax + 1, self.nmax) or \
+                arrs[4].shape != (self.lmax + 1, self.nmax, self.numr):
+            raise ValueError("SL table arrays do not match lmax/nmax/numr")
+        h = _lib.c_vp()
+        _lib.check(lib.xt_sph_table_create(self.lmax, self.nmax, self.numr, self.cmap, self.rmin, self.rmax,
+                                           self.scale, *[a.ctypes.data for a in arrs], _lib.ctypes.byref(h)),
+                   "xt_sph_table_create")
+        self.handle = h.value
+        self._lib = lib
+        self.field_cache = _Cache(limit=8)
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self._lib.xt_sph_table_destroy(self.handle)
+        except Exception:
+            pass
+
+    @property
+    def nrow(self):
+        return (self.lmax + 1) ** 2
+
+    def accumulate(self, x, y, z, m, no_odd=False, precision="f64", workspace=None):
+        n = int(x.numel())
+        out = torch.empty((self.nrow, self.nmax), dtype=torch.float64, device=x.device)
+        need = self._lib.xt_sph_accumulate_workspace(self.handle)
+        ws = workspace if workspace is not None else torch.empty(need, dtype=torch.uint8, device=x.device)
+        _lib.check(self._lib.xt_sph_accumulate(self.handle, dptr(x), dptr(y), dptr(z), dptr(m), n, int(bool(no_odd)),
+                                               precision_code(precision), dptr(out), dptr(ws), ws.numel(),
+                                               stream_ptr()), "xt_sph_accumulate")
+        return out
+
+    def prepare(self, expcoef, coef_scale=1.0, lmax_use=-1, nmax_use=-1, precision="f64"):
+        pc = precision_code(precision)
+        nbytes = self._lib.xt_sph_field_bytes(self.handle, pc)
+        field = torch.empty(nbytes, dtype=torch.uint8, device=device())
+        ec = to_dev(expcoef)
+        if ec.shape != (self.nrow, self.nmax):
+            raise ValueError(f"expcoef shape {tuple(ec.shape)} != {(self.nrow, self.nmax)}")
+        _lib.check(self._lib.xt_sph_prepare(self.handle, dptr(ec), float(coef_scale), int(lmax_use), int(nmax_use), pc,
+                                            dptr(field), nbytes, stream_ptr()), "xt_sph_prepare")
+        return SphField(self, field, pc, lmax_use if 0 <= lmax_use <= self.lmax else self.lmax)
+
+    def eval_points(self, field, a, b, c, mode, coord_mode, L1=-1000, L2=1000, no_odd=False, lmax_use=-1,
+                    trig_l=False, want=None):
+        n = int(a.numel())
+        outs = [torch.empty(n, dtype=torch.float64, device=a.device) if (want is None or want[k]) else None
+                for k in range(8)]
+        pp, keep = _lib.ptr_array([dptr(t) for t in outs])
+        _lib.check(self._lib.xt_sph_eval_points(self.handle, dptr(field.buf), field.precision, coord_mode, dptr(a),
+                                                dptr(b), dptr(c), n, mode, int(L1), int(L2), int(bool(no_odd)),
+                                                int(lmax_use), int(bool(trig_l)), pp, stream_ptr()),
+                   "xt_sph_eval_points")
+        return outs
+
+
+class SphField:
+    """Coefficient-contracted radial field of a SphTable."""
+
+    def __init__(self, table, buf, precision, lmax_use):
+        self.table, self.buf, self.precision, self.lmax_use = table, buf, precision, lmax_use
+
+
+class CylTable:
+    """Uploaded EOF basis (eof.parse_eof + eof_params + set_table_params)."""
+
+    def __init__(self, mmax, norder, numx, numy, cmap, dens, XMIN, dX, YMIN, dY, ascale, hscale, potC, rforceC,
+                 zforceC, densC, potS, rforceS, zforceS, densS):
+        device()
+        lib = _lib.load()
+        self.mmax, self.norder, self.numx, self.numy = int(mmax), int(norder), int(numx), int(numy)
+        self.cmap, self.dens = int(cmap), int(bool(dens))
+        self.XMIN, self.dX, self.YMIN, self.dY = float(XMIN), float(dX), float(YMIN), float(dY)
+        self.ascale, self.hscale = float(ascale), float(hscale)
+        shape = (self.mmax + 1, self.norder, self.numx + 1, self.numy + 1)
+        arrs = []
+        for a in (potC, rforceC, zforceC, densC if self.dens else None, potS, rforceS, zforceS,
+                  densS if self.dens else None):
+            if a is None:
+                arrs.append(None)
+                continue
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.float64)[:shape[0], :shape[1]])
+            if a.shape != shape:
+                raise ValueError(f"EOF table shape {a.shape} != {shape}")
+            arrs.append(a)
+        ptrs = [a.ctypes.data if a is not None else None for a in arrs]
+        h = _lib.c_vp()
+        _lib.check(lib.xt_cyl_table_create(self.mmax, self.norder, self.numx, self.numy, self.cmap, self.dens,
+                                           self.XMIN, self.dX, self.YMIN, self.dY, self.ascale, self.hscale, *ptrs,
+                                           _lib.ctypes.byref(h)), "xt_cyl_table_create")
+        self.handle = h.value
+        self._lib = lib
+        self.field_cache = _Cache(limit=8)
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self._lib.xt_cyl_table_destroy(self.handle)
+        except Exception:
+            pass
+
+    def accumulate(self, x, y, z, m, precision="f64", workspace=None):
+        n = int(x.numel())
+        cos = torch.empty((self.mmax + 1, self.norder), dtype=torch.float64, device=x.device)
+        sin = torch.empty_like(cos)
+        need = self._lib.xt_cyl_accumulate_workspace(self.handle)
+        ws = workspace if workspace is not None else torch.empty(need, dtype=torch.uint8, device=x.device)
+        _lib.check(self._lib.xt_cyl_accumulate(self.handle, dptr(x), dptr(y), dptr(z), dptr(m), n,
+                                               precision_code(precision), dptr(cos), dptr(sin), dptr(ws), ws.numel(),
+                                               stream_ptr()), "xt_cyl_accumulate")
+        return cos, sin
+
+    def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):
+        pc = precision_code(precision)
+        nbytes = self._lib.xt_cyl_field_bytes(self.handle, int(bool(density)), pc)
+        field = torch.empty(nbytes, dtype=torch.uint8, device=device())
+        c = to_dev(np.asarray(cos, dtype=np.float64) if not isinstance(cos, torch.Tensor) else cos)
+        s = to_dev(np.asarray(sin, dtype=np.float64) if not isinstance(sin, torch.Tensor) else sin)
+        c = _pad2(c, self.mmax + 1, self.norder)
+        s = _pad2(s, self.mmax + 1, self.norder)
+        _lib.check(self._lib.xt_cyl_prepare(self.handle, dptr(c), dptr(s), int(mmax_use), int(nmax_use),
+                                            int(bool(density)), pc, dptr(field), nbytes, stream_ptr()),
+                   "xt_cyl_prepare")
+        return CylField(self, field, pc, bool(density))
+
+    def eval_points(self, field, a, b, c, mode, coord_mode, m1=0, m2=1000, mmax_use=-1, no_odd=False,
+                    perturb=False, want=None):
+        n = int(a.numel())
+        outs = [torch.empty(n, dtype=torch.float64, device=a.device) if (want is None or want[k]) else None
+                for k in range(8)]
+        pp, keep = _lib.ptr_array([dptr(t) for t in outs])
+        _lib.check(self._lib.xt_cyl_eval_points(self.handle, dptr(field.buf), field.precision, int(field.density),
+                                                coord_mode, dptr(a), dptr(b), dptr(c), n, mode, int(m1), int(m2),
+                                                int(mmax_use), int(bool(no_odd)), int(bool(perturb)), pp,
+                                                stream_ptr()), "xt_cyl_eval_points")
+        return outs
+
+
+def _pad2(t, rows, cols):
+    """Zero-pad / crop a (r, c) coefficient tensor to (rows, cols)."""
+    if t.shape == (rows, cols):
+        return t.contiguous()
+    out = torch.zeros((rows, cols), dtype=t.dtype, device=t.device)
+    r, c = min(rows, t.shape[0]), min(cols, t.shape[1])
+    out[:r, :c] = t[:r, :c]
+    return out
+
+
+class CylField:
+    def __init__(self, table, buf, precision, density):
+        self.table, self.buf, self.precision, self.density = table, buf, precision, density
+
+
+def fields_forces(sph_field, cyl_field, x, y, z, rotpos=None, rotpos_scalar=0.0, halo_l=-1, disk_m=-1,
+                  no_odd=False, trig_l=True, precision=None):
+    """Fields.return_forces_cart at the points (x, y, z): 8 output tensors."""
+    lib = _lib.load()
+    pc = sph_field.precision if precision is None else precision_code(precision)
+    if sph_field.precision != pc or cyl_field.precision != pc:
+        raise ValueError("both fields must be prepared at the requested precision")
+    n = int(x.numel())
+    outs = [torch.empty(n, dtype=torch.float64, device=x.device) for _ in range(8)]
+    pp, keep = _lib.ptr_array([dptr(t) for t in outs])
+    _lib.check(lib.xt_fields_forces(sph_field.table.handle, dptr(sph_field.buf), cyl_field.table.handle,
+                                    dptr(cyl_field.buf), pc, int(halo_l), int(disk_m), int(bool(no_odd)),
+                                    int(bool(trig_l)), dptr(x), dptr(y), dptr(z), dptr(rotpos),
+                                    float(rotpos_scalar), n, pp, stream_ptr()), "xt_fields_forces")
+    return outs
+
+
+STATE_SLOTS = ("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz", "pot", "r2m1", "r2m2", "aps", "nstep", "e0",
+               "edev")
+
+
+def leapfrog(sph_field, cyl_field, state, step0, nsteps, nint, dt, rotc=0.0, apse=False, ap_max=1000, traj=None,
+             halo_l=-1, disk_m=-1, no_odd=False, trig_l=True):
+    """Advance orbit ensemble ``state`` (16 x n float64 tensor) in place."""
+    lib = _lib.load()
+    n = int(state.shape[1])
+    pp, keep = _lib.ptr_array([state[k].data_ptr() for k in range(len(STATE_SLOTS))])
+    _lib.check(lib.xt_leapfrog(sph_field.table.handle, dptr(sph_field.buf), cyl_field.table.handle,
+                               dptr(cyl_field.buf), sph_field.precision, int(halo_l), int(disk_m), int(bool(no_odd)),
+                               int(bool(trig_l)), pp, n, int(step0), int(nsteps), int(nint), float(dt), float(rotc),
+                               int(bool(apse)), int(ap_max), dptr(traj), stream_ptr()), "xt_leapfrog")

@@ -1,0 +1,151 @@
+/*
+ * exptool_gb300 — C ABI of the GB300 (sm_103a) basis-function-expansion path.
+ *
+ * Every entry point returns an int status (XT_OK = 0, negative on error) and
+ * never throws across the ABI; xt_last_error() returns the message of the
+ * last failure on the calling thread.  Particle arrays, coefficient arrays,
+ * outputs and workspaces are DEVICE pointers owned by the caller; table
+ * handles own their device copies of the basis tables.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Calls are asynchronous with
+ * respect to the host unless stated otherwise.
+ *
+ * The reference interfaces each entry point replaces are cited as
+ * exptool/<file>:<line> (exptool 0.4.0, pure Python/NumPy).
+ */
+#ifndef EXPTOOL_GB300_H
+#define EXPTOOL_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XT_OK 0
+#define XT_ERR_ARG (-1)     /* invalid argument / size mismatch          */
+#define XT_ERR_CUDA (-2)    /* CUDA runtime error                        */
+#define XT_ERR_OOM (-3)     /* device allocation failed                  */
+#define XT_ERR_WORKSPACE (-4) /* workspace too small                     */
+#define XT_ERR_DEVICE (-5)  /* a kernel reported an error flag           */
+
+/* precision of the per-particle arithmetic */
+#define XT_F64 0            /* plain FP64: the drop-in path              */
+#define XT_F32 1            /* FP32 per-particle work, FP64 reductions   */
+
+/* coordinate modes of evaluation inputs (a, b, c) */
+#define XT_COORD_CART 0     /* x, y, z                                   */
+#define XT_COORD_SPH 1      /* r, cos(theta), phi   (spherical basis)    */
+#define XT_COORD_CYL 1      /* R, z, phi            (cylindrical basis)  */
+
+/* spherical evaluation modes */
+#define XT_SPH_ALL_EVAL_PARTICLES 0 /* spheresl.all_eval_particles  (spheresl.py:1240) */
+#define XT_SPH_ALL_EVAL 1           /* spheresl.all_eval            (spheresl.py:987)  */
+#define XT_SPH_FORCE_EVAL 2         /* spheresl.force_eval          (spheresl.py:1107) */
+
+/* cylindrical evaluation modes */
+#define XT_CYL_ACCUMULATED_EVAL_PARTICLES 0 /* eof.accumulated_eval_particles (eof.py:989) */
+#define XT_CYL_FORCE_EVAL 1                 /* eof.force_eval                 (eof.py:756) */
+#define XT_CYL_ACCUMULATED_EVAL 2           /* eof.accumulated_eval           (eof.py:874) */
+
+/* --------------------------------------------------------------- misc */
+int xt_abi_version(void);
+const char *xt_last_error(void);
+
+/* --------------------------------------------------------------- spherical (SL) */
+/* Upload an SL basis: replaces the per-call table reads of
+ * halo_methods.read_cached_table + init_table (halo_methods.py:96,178) done by
+ * spheresl.compute_coefficients_solitary (spheresl.py:587-588).
+ * ev: (lmax+1) x nmax, ef: (lmax+1) x nmax x numr, xi/p0/d0: numr; host arrays. */
+int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, double rmax, double scale,
+                        const double *xi, const double *p0, const double *d0, const double *ev,
+                        const double *ef, void **handle);
+int xt_sph_table_destroy(void *handle);
+
+/* Coefficient accumulation, spheresl.compute_coefficients_solitary
+ * (spheresl.py:567-656): expcoef_out ((lmax+1)^2 x nmax, row-major) =
+ * sum over particles.  Particles x, y, z, m: n float64 each. */
+size_t xt_sph_accumulate_workspace(void *handle);
+int xt_sph_accumulate(void *handle, const double *x, const double *y, const double *z, const double *m,
+                      long long n, int no_odd, int precision, double *expcoef_out, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
+/* Contract coefficients (scaled by `coef_scale`, e.g. Fields.halofac) with
+ * the radial tables into an evaluation field (kept in `field`, caller-owned).
+ * lmax_use/nmax_use truncate the expansion (spheresl.py:1139-1151). */
+size_t xt_sph_field_bytes(void *handle, int precision);
+int xt_sph_prepare(void *handle, const double *expcoef, double coef_scale, int lmax_use, int nmax_use,
+                   int precision, void *field, size_t field_bytes, void *stream);
+
+/* Evaluate at n points (spheresl.all_eval_particles / all_eval / force_eval).
+ * outs: array of 8 device pointers (may be NULL to skip):
+ *   ALL_EVAL_PARTICLES: den0 den1 pot0 pot1 potr pott potp rr
+ *   ALL_EVAL:           den0 den1 pot0 pot1 potr pott potp -
+ *   FORCE_EVAL:         potr pott potp pot1 pot0 - - -
+ * L1/L2: l range (ALL_EVAL_PARTICLES); trig_l: 1 = the reference force_eval
+ * azimuthal factor cos(l phi) (spheresl.py:1173), 0 = cos(m phi). */
+int xt_sph_eval_points(void *handle, const void *field, int precision, int coord_mode, const double *a,
+                       const double *b, const double *c, long long n, int mode, int L1, int L2, int no_odd,
+                       int lmax_use, int trig_l, double *const *outs, void *stream);
+
+/* --------------------------------------------------------------- cylindrical (EOF) */
+/* Upload EOF tables parsed by eof.parse_eof (eof.py:224-313); each table is
+ * (mmax+1) x norder x (numx+1) x (numy+1) float64; force tables may be NULL
+ * (stored as zeros, for accumulation-only use) and dens tables may be NULL
+ * when dens == 0.  XMIN/dX/YMIN/dY from eof.set_table_params (eof.py:316). */
+int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int dens, double XMIN,
+                        double dX, double YMIN, double dY, double ascale, double hscale, const double *potC,
+                        const double *rforceC, const double *zforceC, const double *densC, const double *potS,
+                        const double *rforceS, const double *zforceS, const double *densS, void **handle);
+int xt_cyl_table_destroy(void *handle);
+
+/* Coefficient accumulation, eof.accumulate (eof.py:492-640): cos_out and
+ * sin_out are (mmax+1) x norder row-major. */
+size_t xt_cyl_accumulate_workspace(void *handle);
+int xt_cyl_accumulate(void *handle, const double *x, const double *y, const double *z, const double *m,
+                      long long n, int precision, double *cos_out, double *sin_out, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
+/* Contract cos/sin coefficients with the tables into an evaluation field.
+ * mmax_use/nmax_use truncate (eof.py:789-799); density != 0 also contracts
+ * the density tables. */
+size_t xt_cyl_field_bytes(void *handle, int density, int precision);
+int xt_cyl_prepare(void *handle, const double *cos_c, const double *sin_c, int mmax_use, int nmax_use,
+                   int density, int precision, void *field, size_t field_bytes, void *stream);
+
+/* Evaluate at n points.  outs (8 device pointers, NULL to skip):
+ *   ACCUMULATED_EVAL_PARTICLES: p0 p fr fp fz R d0 d   (m1 <= m <= m2)
+ *   FORCE_EVAL:                 fr fp fz p p0 fr0 fz0 -  (perturb != 0: fr,fz,p
+ *                               exclude m = 0, as eof.py:861-867)
+ *   ACCUMULATED_EVAL:           p0 p fr fp fz d0 d - */
+int xt_cyl_eval_points(void *handle, const void *field, int precision, int density, int coord_mode,
+                       const double *a, const double *b, const double *c, long long n, int mode, int m1, int m2,
+                       int mmax_use, int no_odd, int perturb, double *const *outs, void *stream);
+
+/* --------------------------------------------------------------- fields + orbits */
+/* potential.Fields.return_forces_cart (potential.py:445-497) at n points:
+ * outs = fxdisk fxhalo fydisk fyhalo fzdisk fzhalo diskp halop+halop0.
+ * Fields prepared with xt_sph_prepare(coef_scale = halofac, halo_use_l/n) and
+ * xt_cyl_prepare(disk_use_m/n).  rotpos: per-point array or NULL (then
+ * rotpos_scalar is used). */
+int xt_fields_forces(void *sph, const void *sph_field, void *cyl, const void *cyl_field, int precision,
+                     int halo_l, int disk_m, int no_odd, int trig_l, const double *x, const double *y,
+                     const double *z, const double *rotpos, double rotpos_scalar, long long n,
+                     double *const *outs, void *stream);
+
+/* Velocity-Verlet orbits (integrate.leapfrog_integrate, integrate.py:53-190)
+ * for n independent orbits.  state: 16 device arrays of n float64
+ * (x y z vx vy vz fx fy fz pot r2m1 r2m2 aps nstep e0 emaxdev) updated in
+ * place; steps [step0, step0+nsteps) of a run of nint steps with rotation
+ * angle rotc * (k*dt) at step k.  traj (optional, may be NULL): row-major
+ * (n, nint, 10) = x y z vx vy vz p fx fy fz of every step.  apse != 0 stops
+ * an orbit after ap_max planar apocentres.  The force precision follows
+ * `precision` (fields prepared at that precision); kick/drift are FP64. */
+int xt_leapfrog(void *sph, const void *sph_field, void *cyl, const void *cyl_field, int precision,
+                int halo_l, int disk_m, int no_odd, int trig_l, double *const *state, long long n,
+                int step0, int nsteps, int nint, double dt, double rotc, int apse, int ap_max, double *traj,
+                void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EXPTOOL_GB300_H */

@@ -1,0 +1,140 @@
+"""Full-size workloads on the GPU against the oracle and physical checks.
+
+* spherical halo (Hernquist, lmax 4, nmax 10, 2000-point log-r table, N = 1e5):
+  GPU accumulation vs oracle on all particles, evaluation vs oracle on a subset;
+* exponential disc (EOF mmax 6, norder 18, 257^2 nodes, N = 1e6): accumulation
+  vs oracle on all particles, evaluation on a subset;
+* mixed (FP32) path error bounds against the FP64 path;
+* physics: the monopole reproduces the truncated-Hernquist potential;
+* run-to-run reproducibility of the FP64 accumulation.
+Tolerance of the FP64 path: 1e-10 normwise relative (per l / m block)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def halo():
+    import bench
+    from oracle import sl as osl
+    cache, model = bench.sl_table_paths()
+    x, y, z, m = bench.halo_particles()
+    return cache, model, (x, y, z, m), osl.load_table(cache, model)
+
+
+@pytest.fixture(scope="module")
+def disc():
+    import bench
+    from oracle import eof as oeof
+    path = bench.eof_table_path()
+    return path, bench.disc_particles(), oeof.load_table(path)
+
+
+class PD:
+    def __init__(self, x, y, z, m):
+        self.xpos, self.ypos, self.zpos, self.mass = x, y, z, m
+        self.data = {"x": x, "y": y, "z": z, "m": m}
+
+
+def test_halo_full(halo):
+    from exptool_gb300.basis import spheresl
+    from oracle import sl as osl
+    cache, model, (x, y, z, m), t = halo
+    ec = spheresl.compute_coefficients_solitary(PD(x, y, z, m), cache, model)
+    ref = osl.compute_coefficients_solitary(x, y, z, m, t)
+    row = 0
+    for l in range(5):
+        blk = slice(row, row + 2 * l + 1)
+        assert rel(ec[blk], ref[blk]) <= 1e-10, l
+        row += 2 * l + 1
+    sub = slice(0, 20000)
+    P = PD(x[sub], y[sub], z[sub], m[sub])
+    got = spheresl.all_eval_particles(P, ec, cache, model, 0)
+    want = osl.all_eval_particles(x[sub], y[sub], z[sub], ec, t)
+    for k in range(8):
+        assert rel(got[k], want[k]) <= 1e-10, k
+    # per-particle total force vector |dF|/|F| (potr, pott, potp components)
+    fg = np.stack([got[4], got[5], got[6]])
+    fw = np.stack([want[4], want[5], want[6]])
+    assert np.max(np.linalg.norm(fg - fw, axis=0) / np.linalg.norm(fw, axis=0)) <= 1e-9
+
+
+def test_halo_monopole_physics(halo):
+    """l = 0 field of the sample reproduces the truncated Hernquist potential."""
+    from exptool_gb300.basis import spheresl
+    from exptool_gb300.tables.models import TruncatedHernquist
+    cache, model, (x, y, z, m), t = halo
+    ec = spheresl.compute_coefficients_solitary(PD(x, y, z, m), cache, model)
+    r = np.geomspace(0.05, 50.0, 25)
+    den0, den1, pot0, pot1, potr, pott, potp = spheresl.all_eval(r, np.zeros_like(r), np.zeros_like(r), ec,
+                                                                t["xi"], t["p0"], t["d0"], 2, 1.0, 4, 10,
+                                                                t["ev"], t["ef"])
+    mod = TruncatedHernquist()
+    assert np.max(np.abs(pot0 / mod.potential(r) - 1.0)) < 0.02
+    assert np.max(np.abs(potr / mod.dpotential(r) - 1.0)) < 0.05
+
+
+def test_disc_full(disc):
+    from exptool_gb300.basis import eof
+    from oracle import eof as oeof
+    path, (x, y, z, m), t = disc
+    E = eof.compute_coefficients(PD(x, y, z, m), path, verbose=0)
+    kw = dict(MMAX=t["mmax"], NMAX=t["norder"], XMIN=t["XMIN"], dX=t["dX"], YMIN=t["YMIN"], dY=t["dY"],
+              NUMX=t["numx"], NUMY=t["numy"], ASCALE=t["ascale"], HSCALE=t["hscale"], CMAP=t["cmap"])
+    c, s = oeof.accumulate(x, y, z, m, t["potC"], t["potS"], **kw)
+    for mm in range(t["mmax"] + 1):
+        assert rel(E.cos[mm], c[mm]) <= 1e-10, mm
+        if mm:
+            assert rel(E.sin[mm], s[mm]) <= 1e-10, mm
+    sub = slice(0, 20000)
+    got = eof.compute_forces(PD(x[sub], y[sub], z[sub], m[sub]), E, verbose=0)
+    tabs = [t[k] for k in ("potC", "rforceC", "zforceC", "potS", "rforceS", "zforceS")]
+    want = oeof.accumulated_eval_particles(x[sub], y[sub], z[sub], E.cos, E.sin, *tabs, t["XMIN"], t["dX"],
+                                           t["YMIN"], t["dY"], t["numx"], t["numy"], t["mmax"], t["norder"],
+                                           t["ascale"], t["hscale"], t["cmap"])
+    for k in range(6):
+        assert rel(got[k], want[k]) <= 1e-10, k
+    F = np.stack([want[2], want[3] / want[5], want[4]])
+    G = np.stack([got[2], got[3] / got[5], got[4]])
+    assert np.max(np.linalg.norm(G - F, axis=0) / np.linalg.norm(F, axis=0)) <= 1e-9
+
+
+def test_disc_mixed_precision_error(disc):
+    from exptool_gb300.basis import eof
+    path, (x, y, z, m), t = disc
+    P = PD(x, y, z, m)
+    E64 = eof.compute_coefficients(P, path, verbose=0)
+    E32 = eof.compute_coefficients(P, path, verbose=0, precision="f32")
+    assert rel(E32.cos[0], E64.cos[0]) < 1e-5
+    sub = slice(0, 100000)
+    Q = PD(x[sub], y[sub], z[sub], m[sub])
+    a = eof.compute_forces(Q, E64, verbose=0)
+    b = eof.compute_forces(Q, E64, verbose=0, precision="f32")
+    F = np.stack([a[2], a[4]])
+    G = np.stack([b[2], b[4]])
+    err = np.linalg.norm(G - F, axis=0) / np.linalg.norm(F, axis=0)
+    assert np.median(err) < 1e-5 and np.max(err) < 1e-2
+
+
+def test_accumulate_reproducible(disc):
+    """FP64 atomics change only the summation order: repeated runs agree to
+    rounding (<= 1e-13 per block)."""
+    from exptool_gb300.basis import eof
+    path, (x, y, z, m), t = disc
+    P = PD(x, y, z, m)
+    a = eof.compute_coefficients(P, path, verbose=0)
+    b = eof.compute_coefficients(P, path, verbose=0)
+    for mm in range(t["mmax"] + 1):
+        assert rel(a.cos[mm], b.cos[mm]) <= 1e-13
