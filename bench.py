@@ -130,7 +130,7 @@ class Clocks:
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": reasons, "samples": len(rows)}
 
@@ -190,6 +190,12 @@ def gpu_arm(args, rank, world):
 
     K, W = args.steps, args.warmup
     with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        # keep the GPU under the same load for ~1.5 s so the sampler sees the
+        # clocks of the timed region, then time exactly K steps
+        t_end = time.perf_counter() + 1.5
+        while time.perf_counter() < t_end:
+            step("f64")
+            torch.cuda.synchronize()
         tot64, ph64 = timed("f64", K, W)
     clocks = clk.summary()
     tot32, ph32 = timed("f32", K, W)
