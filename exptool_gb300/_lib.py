@@ -41,6 +41,7 @@ _SIGS = {
     "xt_sph_table_destroy": (c_int, [c_vp]),
     "xt_sph_accumulate_workspace": (c_sz, [c_vp]),
     "xt_sph_accumulate": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_sph_accumulate_noalloc": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_vp, c_vp]),
     "xt_sph_field_bytes": (c_sz, [c_vp, c_int]),
     "xt_sph_prepare": (c_int, [c_vp, c_vp, c_dbl, c_int, c_int, c_int, c_vp, c_sz, c_vp]),
     "xt_sph_eval_points": (c_int, [c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int, c_int,

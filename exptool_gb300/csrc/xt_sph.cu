@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -146,6 +147,43 @@ bool sph_tabs(void* handle, SphTab<double>* d, SphTab<float>* f) {
   return true;
 }
 
+
+// ------------------------------------------------------------------ allocation-free accumulation
+// Some callers cannot allocate device memory for a workspace: a host
+// application or framework that owns every byte of device memory through its
+// own pool and forbids outside cudaMalloc, a latency-critical loop that cannot
+// afford the synchronisation cudaMalloc/cudaFree may cause, or a plain C /
+// cgo / Fortran binding with no device allocator to hand.  For them
+// xt_sph_accumulate_noalloc keeps the deposit grid in this fixed array, which
+// every GPU that loads the library holds until the process exits.
+#define XT_SPH_NOALLOC_MAX_DOUBLES 262144  // 2 MiB: (lmax+1)^2 * numr must not exceed this
+static __device__ __align__(256) double g_sph_noalloc_grid[XT_SPH_NOALLOC_MAX_DOUBLES];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};   // device address of the array, per device ordinal
+}
+
+// Device address of the static grid on the current device, looked up once per
+// device (cudaGetSymbolAddress with that device current) and then cached.
+static int noalloc_grid(double** out) {
+  int dev = 0;
+  XT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) {
+    set_error("device ordinal %d out of range for the static accumulation grid", dev);
+    return XT_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sph_noalloc_grid);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_sph_noalloc_grid)");
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return XT_OK;
+}
+
 }  // namespace xt
 
 using namespace xt;
@@ -254,6 +292,43 @@ int xt_sph_accumulate(void* handle, const double* x, const double* y, const doub
   }
   k_sph_contract<<<sph_nrow(h->lmax) * h->nmax, 256, 0, st>>>(h->efp, D, h->lmax, h->nmax, h->numr, expcoef_out);
   XT_CHECK_LAUNCH("k_sph_contract");
+  return XT_OK;
+}
+
+int xt_sph_accumulate_noalloc(void* handle, const double* x, const double* y, const double* z, const double* m,
+                              long long n, int no_odd, int precision, double* expcoef_out, void* stream) {
+  SphHandle* h = static_cast<SphHandle*>(handle);
+  XT_REQUIRE(h, "NULL table handle");
+  XT_REQUIRE(n >= 0, "negative particle count");
+  XT_REQUIRE(expcoef_out, "NULL output");
+  XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
+  XT_REQUIRE(precision == XT_F64 || precision == XT_F32, "bad precision %d", precision);
+  const size_t need = (size_t)sph_nrow(h->lmax) * h->numr;
+  XT_REQUIRE(need <= XT_SPH_NOALLOC_MAX_DOUBLES,
+             "xt_sph_accumulate_noalloc: (lmax+1)^2 * numr = %zu exceeds the static grid of %d doubles (2 MiB); "
+             "use xt_sph_accumulate with a caller workspace", need, XT_SPH_NOALLOC_MAX_DOUBLES);
+  double* D = nullptr;
+  int rc = noalloc_grid(&D);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  // the grid keeps the previous call's sums: zero the part this call uses
+  XT_CUDA(cudaMemsetAsync(D, 0, need * sizeof(double), st));
+  if (n > 0) {
+    const int block = 256;
+    const int grid = grid_for(n, block, 8);
+    rc = with_lcap(h->lmax, [&](auto lc) {
+      constexpr int LC = decltype(lc)::value;
+      if (precision == XT_F64)
+        launch_sph_deposit<double, LC>(h->tab_d, x, y, z, m, n, no_odd, D, grid, block, st);
+      else
+        launch_sph_deposit<float, LC>(h->tab_f, x, y, z, m, n, no_odd, D, grid, block, st);
+      return XT_OK;
+    });
+    if (rc) return rc;
+    XT_CHECK_LAUNCH("k_sph_deposit (noalloc)");
+  }
+  k_sph_contract<<<sph_nrow(h->lmax) * h->nmax, 256, 0, st>>>(h->efp, D, h->lmax, h->nmax, h->numr, expcoef_out);
+  XT_CHECK_LAUNCH("k_sph_contract (noalloc)");
   return XT_OK;
 }
 

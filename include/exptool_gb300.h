@@ -69,6 +69,24 @@ int xt_sph_accumulate(void *handle, const double *x, const double *y, const doub
                       long long n, int no_odd, int precision, double *expcoef_out, void *workspace,
                       size_t workspace_bytes, void *stream);
 
+/* Allocation-free variant of xt_sph_accumulate; no counterpart in the
+ * reference.  For callers that cannot allocate device memory for a
+ * workspace: an application or framework that owns all device memory
+ * through its own pool, a latency-critical loop that cannot afford the
+ * synchronisation cudaMalloc/cudaFree may cause, or a C / cgo / Fortran
+ * binding with no device allocator.  The deposit grid lives in a static
+ * 2 MiB device array inside the library (held on every GPU that loads it
+ * until exit), so the call allocates nothing; inputs and the output are
+ * still caller-owned device pointers.  Limit: (lmax+1)^2 * numr <= 262144
+ * doubles, larger tables return XT_ERR_ARG.  The first call on each device
+ * looks up the array's address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the one array, which
+ * keeps the last call's contents (each call zeroes what it uses first), so
+ * calls that overlap on the GPU (concurrent streams) race: serialise them. */
+int xt_sph_accumulate_noalloc(void *handle, const double *x, const double *y, const double *z,
+                              const double *m, long long n, int no_odd, int precision, double *expcoef_out,
+                              void *stream);
+
 /* Contract coefficients (scaled by `coef_scale`, e.g. Fields.halofac) with
  * the radial tables into an evaluation field (kept in `field`, caller-owned).
  * lmax_use/nmax_use truncate the expansion (spheresl.py:1139-1151). */
