@@ -157,6 +157,35 @@ def gpu_arm(args, rank, world):
         outs = table.eval_points(f, xd, yd, zd, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, want=want)
         return c, s, outs
 
+    fws = torch.empty(_lib.load().xt_cyl_accumulate_eval_workspace(table.handle, N1, _lib.XT_F64), dtype=torch.uint8,
+                      device="cuda")
+
+    def fused(prec):
+        return table.accumulate_eval(xd, yd, zd, md, precision=prec, workspace=fws)
+
+    def timed_fused(prec, steps, warmup):
+        for _ in range(warmup):
+            fused(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fused(prec)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        if world > 1:
+            dist.barrier()
+            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            tot = float(tt.item())
+        return tot
+
     def timed(prec, steps, warmup, phases=False):
         for _ in range(warmup):
             step(prec)
@@ -196,10 +225,12 @@ def gpu_arm(args, rank, world):
         while time.perf_counter() < t_end:
             step("f64")
             torch.cuda.synchronize()
-        tot64, ph64 = timed("f64", K, W)
+        ftot64 = timed_fused("f64", K, W)
     clocks = clk.summary()
+    tot64, ph64 = timed("f64", K, W)
     tot32, ph32 = timed("f32", K, W)
-    ms64 = tot64 / K
+    ftot32 = timed_fused("f32", K, W)
+    ms64 = ftot64 / K
     value = world * N1 / (ms64 * 1e-3)
 
     # mixed-precision error against the FP64 path on the same particles
@@ -217,17 +248,22 @@ def gpu_arm(args, rank, world):
     from exptool_gb300.io.particle import ParticleData
     pinned = [torch.from_numpy(a).pin_memory() for a in (x, y, z, m)]
     P = ParticleData(*(t.numpy() for t in pinned))
-    E = eof.compute_coefficients(P, path, verbose=0)
-    eof.compute_forces(P, E, verbose=0)
+    eof.compute_coefficients_and_forces(P, path, verbose=0)
     torch.cuda.synchronize()
     e2e_times = []
     for _ in range(max(3, min(K, 10))):
         t0 = time.perf_counter()
-        E = eof.compute_coefficients(P, path, verbose=0)
-        out = eof.compute_forces(P, E, verbose=0)
+        E, out = eof.compute_coefficients_and_forces(P, path, verbose=0)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = float(np.median(e2e_times))
-    h2d = 2 * 4 * N1 * 8            # x y z m for accumulation, x y z (+z) for evaluation
+    sep_times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        E = eof.compute_coefficients(P, path, verbose=0)
+        eof.compute_forces(P, E, verbose=0)
+        sep_times.append(time.perf_counter() - t0)
+    sep_s = float(np.median(sep_times))
+    h2d = 4 * N1 * 8                # x y z m
     d2h = 6 * N1 * 8 + 2 * 7 * 18 * 8
 
     # spherical workload (halo, lmax 4)
@@ -252,18 +288,39 @@ def gpu_arm(args, rank, world):
     torch.cuda.synchronize()
     sl_ms = e0.elapsed_time(e1) / K
 
+    orbits = orbit_extra(path, c64, s64, cache, model, st, hxd, hyd, hzd, hmd, args)
+
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
-    field_bytes = nnode * 7 * 6 * 8
-    alg = {"accumulate": 32 * N1 + (7 + 6) * 18 * nnode * 8 + 13 * nnode * 8,
-           "prepare": (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * 8 + field_bytes,
-           "eval": 72 * N1 + field_bytes}
     names = ["accumulate", "prepare", "eval"]
-    dom = int(np.argmax(ph64))
-    kname = {"accumulate": "k_cyl_deposit+k_cyl_contract", "prepare": "k_cyl_field", "eval": "k_cyl_eval"}
-    phases = {n: {"ms": round(float(ph64[i]), 4), "alg_bytes": alg[n],
-                  "gbs": round(alg[n] / (ph64[i] * 1e-3) / 1e9, 1)} for i, n in enumerate(names)}
-    ach = alg[names[dom]] / (ph64[dom] * 1e-3) / 1e9
+    sep_alg = {"accumulate": 32 * N1 + (7 + 6) * 18 * nnode * 8 + 13 * nnode * 8,
+               "prepare": (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * 8 + nnode * 7 * 6 * 8,
+               "eval": 72 * N1 + nnode * 7 * 6 * 8}
+    phases = {n: {"ms": round(float(ph64[i]), 4), "alg_bytes": sep_alg[n],
+                  "gbs": round(sep_alg[n] / (ph64[i] * 1e-3) / 1e9, 1)} for i, n in enumerate(names)}
+    stages64 = stage_times(fused, "f64", K)
+    stages32 = stage_times(fused, "f32", K)
+    st_names = ["k_cyl_binrec", "k_scan_cells", "k_cyl_scatter", "k_cyl_deposit_sorted",
+                "k_cyl_contract_partial+final", "k_cyl_field", "k_cyl_eval_sorted"]
+
+    def stage_alg(rs):
+        # algorithmic bytes per launch of each stage (rs = bytes of the compute type)
+        rec = 5 * rs
+        return [N1 * (32 + rec + 8 + 8), 2 * 4 * 65536, N1 * 2 * (rec + 8), N1 * (rec + 4),
+                13 * 18 * nnode * 8 + 13 * nnode * 8,
+                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * 8 + nnode * 7 * 6 * rs,
+                N1 * (rec + 8 + 40) + nnode * 7 * 6 * rs]
+
+    alg64 = stage_alg(8)
+    alg32 = stage_alg(4)
+    dom = int(np.argmax(stages64))
+    ach = alg64[dom] / (stages64[dom] * 1e-3) / 1e9
+    fused_stages = {"f64": {n: {"ms": round(float(stages64[i]), 4),
+                                "gbs": round(alg64[i] / (stages64[i] * 1e-3) / 1e9, 1)}
+                            for i, n in enumerate(st_names)},
+                    "f32": {n: {"ms": round(float(stages32[i]), 4),
+                                "gbs": round(alg32[i] / (stages32[i] * 1e-3) / 1e9, 1)}
+                            for i, n in enumerate(st_names)}}
     line = {
         "metric": "particle-force evals/s & coef-accum particles/s, learned/mixed vs plain FP64",
         "value": value,
@@ -282,20 +339,93 @@ def gpu_arm(args, rank, world):
                    "l2": "flushed between timed steps (512 MB write outside the timed events)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * N1 / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients + eof.compute_forces, pinned numpy"},
-        "gpu_launches": 5 * K,
-        "roofline": {"bound": "hbm", "kernel": kname[names[dom]], "achieved": round(ach, 1), "peak": peak,
+                "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients_and_forces, pinned numpy inputs",
+                "separate_calls_value": world * N1 / sep_s},
+        "pipeline": "fused: per-particle set-up once, counting sort by table cell, run-accumulated deposit, "
+                    "contraction, field, sorted evaluation (8 kernels)",
+        "gpu_launches": 8 * K,
+        "roofline": {"bound": "hbm", "kernel": st_names[dom], "achieved": round(ach, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": None,
-                     "peak_source": peak_kind},
-        "phases_f64": phases,
-        "mixed_f32": {"value": world * N1 / (tot32 / K * 1e-3), "ms_per_step": tot32 / K,
+                     "peak_source": peak_kind, "alg_bytes_per_launch": alg64[dom],
+                     "launch_ms": round(float(stages64[dom]), 4)},
+        "fused_stages": fused_stages,
+        "separate_calls_f64": {"ms_per_step": tot64 / K, "value": world * N1 / (tot64 / K * 1e-3), "phases": phases},
+        "mixed_f32": {"value": world * N1 / (ftot32 / K * 1e-3), "ms_per_step": ftot32 / K,
+                      "separate_calls_ms_per_step": tot32 / K,
                       "phases_ms": [round(float(v), 4) for v in ph32], "coef_rel_err_vs_f64": coef_err,
                       "force_rel_err_median_vs_f64": force_err_med},
         "spherical_halo": {"workload": "Hernquist SL lmax=4 nmax=10 numr=2000 cmap=2, N=1e5, accumulate+eval",
                            "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
+        "orbits": orbits,
         "clocks": clocks,
     }
     return line
+
+
+def stage_times(fused, prec, steps):
+    """Per-stage CUDA-event durations (ms) of the fused pipeline, averaged over
+    `steps` calls with the library's stage timing switched on."""
+    import ctypes
+    import torch
+    from exptool_gb300 import _lib
+    lib = _lib.load()
+    lib.xt_timing_enable(1)
+    acc = np.zeros(7)
+    buf = (ctypes.c_double * 8)()
+    for _ in range(steps):
+        fused(prec)
+        k = lib.xt_timing_read(buf, 8)
+        acc[:k] += np.array(buf[:k])
+    lib.xt_timing_enable(0)
+    torch.cuda.synchronize()
+    return acc / steps
+
+
+def orbit_extra(eof_path, cos_d, sin_d, sph_cache, sph_model, sph_table, hx, hy, hz, hm, args, n=N1, nint=2000,
+                dt=0.002):
+    """Orbit ensemble in the frozen halo + disc field: n disc orbits (seed 2),
+    v_phi = v_c(R) from the field, 10 % Gaussian dispersion, velocity Verlet
+    dt = 0.002 for nint steps, FP32 forces / FP64 kick-drift, CUDA-graph replay."""
+    import torch
+    from exptool_gb300.basis import eof, potential, spheresl
+    from exptool_gb300.tables.samplers import disc_cylindrical
+    from exptool_gb300.utils import integrate
+    F = potential.Fields("synthetic", eof_path, sph_cache, sph_model, verbose=0, precision="f32",
+                         halo_correct_m=True)
+    F.EOF = eof.EOF_Object()
+    F.EOF.eof_file, F.EOF.cos, F.EOF.sin = eof_path, cos_d.cpu().numpy(), sin_d.cpu().numpy()
+    F.SL = spheresl.SL_Object()
+    F.SL.sph_file, F.SL.model_file = sph_cache, sph_model
+    F.SL.expcoef = sph_table.accumulate(hx, hy, hz, hm).cpu().numpy()
+    F.prep_tables()
+    R, z, phi = disc_cylindrical(n, 2)
+    Rg = np.geomspace(0.01, 25.0, 512)
+    fr = F.return_forces_cart(Rg, np.zeros_like(Rg), np.zeros_like(Rg))
+    vc = np.sqrt(np.maximum(0.0, -Rg * (fr[0] + fr[1])))
+    vcR = np.interp(R, Rg, vc)
+    rng = np.random.default_rng(2)
+    vR = rng.normal(0.0, 0.1, n) * vcR
+    vp = vcR + rng.normal(0.0, 0.1, n) * vcR
+    vz = rng.normal(0.0, 0.1, n) * vcR
+    c, s_ = np.cos(phi), np.sin(phi)
+    pos = np.stack([R * c, R * s_, z], axis=1)
+    vel = np.stack([vR * c - vp * s_, vR * s_ + vp * c, vz], axis=1)
+    ens = integrate.Ensemble(F, pos, vel, nint, dt, precision="f32", chunk=100)
+    ens.run(graph=True)                         # capture + first run
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ens.run(graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    drift = ens.energy_drift()
+    return {"workload": "1e6 disc orbits in frozen halo(SL lmax4)+disc(EOF m6 n18) field, dt=0.002, 2000 steps, "
+                        "FP32 force / FP64 kick-drift, CUDA graph",
+            "ms_per_run": ms, "orbit_steps_per_s": n * (nint - 1) / (ms * 1e-3),
+            "launches_per_run": ens.launches_per_run(),
+            "energy_drift_rel_median": float(np.median(drift)), "energy_drift_rel_p99": float(np.quantile(drift, 0.99)),
+            "energy_drift_rel_max": float(np.max(drift))}
 
 
 # ------------------------------------------------------------------ CPU (oracle) arm
@@ -370,6 +500,21 @@ def reference_arm(args, rank, world):
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def profile_run(args):
+    """Warm-up steps, then one FP64 and one FP32 fused accumulate + eval step."""
+    import torch
+    from exptool_gb300 import _lib, device as dev
+    from exptool_gb300.basis import eof
+    path = eof_table_path()
+    table = eof.table_from_file(path)
+    xd, yd, zd, md = (dev.to_dev(a) for a in disc_particles())
+    for prec in ["f64"] * args.warmup + ["f64", "f32"]:
+        table.accumulate_eval(xd, yd, zd, md, precision=prec)
+    torch.cuda.synchronize()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -377,7 +522,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
+                         "(a short, fixed launch sequence for ncu captures)")
     args = ap.parse_args()
+    if args.profile:
+        return profile_run(args)
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

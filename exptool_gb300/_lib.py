@@ -55,6 +55,11 @@ _SIGS = {
     "xt_cyl_prepare": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_sz, c_vp]),
     "xt_cyl_eval_points": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int,
                                    c_int, c_int, c_int, c_dpp, c_vp]),
+    "xt_cyl_accumulate_eval_workspace": (c_sz, [c_vp, c_ll, c_int]),
+    "xt_cyl_accumulate_eval": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int, c_int, c_vp, c_vp,
+                                       c_dpp, c_vp, c_sz, c_vp]),
+    "xt_timing_enable": (c_int, [c_int]),
+    "xt_timing_read": (c_int, [c_dp, c_int]),
     "xt_fields_forces": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp,
                                  c_dbl, c_ll, c_dpp, c_vp]),
     "xt_leapfrog": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_dpp, c_ll, c_int, c_int,

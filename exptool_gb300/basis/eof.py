@@ -170,7 +170,7 @@ def accumulate(ParticleInstance, potC, potS, MMAX, NMAX, XMIN, dX, YMIN, dY, NUM
     table = table_from_arrays(MMAX, NMAX, NUMX, NUMY, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, pC, potS=pS)
     x, y, z, m = (dev.to_dev(a) for a in positions(ParticleInstance))
     c, s = table.accumulate(x, y, z, m, precision=precision)
-    return c.cpu().numpy(), s.cpu().numpy()
+    return dev.to_host(c), dev.to_host(s)
 
 
 def make_coefficients_multi(ParticleInstance, nprocs, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy,
@@ -205,9 +205,33 @@ def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max
     out.mmax = table.mmax
     out.nmax = table.norder
     c, s = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision)
-    out.cos = c.cpu().numpy()
-    out.sin = s.cpu().numpy()
+    out.cos = dev.to_host(c)
+    out.sin = dev.to_host(s)
     return out
+
+
+def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000, nanblock=False, precision="f64"):
+    """compute_coefficients followed by compute_forces on the same particles
+    (eof.py:1158-1317) as one GPU pipeline: per-particle set-up is done once
+    and particles are sorted by table cell on the device.  Returns
+    (EOF_Object, (p0, p, fr, fp, fz, R)).  Particles with a NaN coordinate
+    are placed at the origin (unless nanblock) for both passes."""
+    x, y, z, m = positions(PSPInput)
+    table = table_from_file(eof_file)
+    # particles with a NaN coordinate are placed at the origin on the device
+    c, s, outs = table.accumulate_eval(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision, m1=m1, m2=m2,
+                                       nan_to_origin=not nanblock)
+    out = EOF_Object()
+    out.time = getattr(PSPInput, "time", None)
+    out.filename = getattr(PSPInput, "filename", None)
+    out.comp = getattr(PSPInput, "comp", None)
+    out.nbodies = m.size
+    out.eof_file = eof_file
+    out.mmax = table.mmax
+    out.nmax = table.norder
+    out.cos = dev.to_host(c)
+    out.sin = dev.to_host(s)
+    return out, tuple(dev.to_host(t) for t in outs)
 
 
 # ---------------------------------------------------------------- evaluation
@@ -240,7 +264,7 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
     z = dev.to_dev(Particles.zpos if hasattr(Particles, "zpos") and Particles.zpos is not None else d["z"])
     outs = table.eval_points(field, x, y, z, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, m1=m1, m2=m2,
                              want=[1, 1, 1, 1, 1, 1, int(density), int(density)])
-    p0, p, fr, fp, fz, R, d0, dd = (t.cpu().numpy() if t is not None else None for t in outs)
+    p0, p, fr, fp, fz, R, d0, dd = (dev.to_host(t) if t is not None else None for t in outs)
     if density:
         return p0, p, d0, dd, fr, fp, fz, R
     return p0, p, fr, fp, fz, R
@@ -276,7 +300,7 @@ def force_eval(r, z, phi, accum_cos, accum_sin, potC, rforceC, zforceC, potS, rf
     outs = table.eval_points(field, dev.to_dev(ra), dev.to_dev(za), dev.to_dev(pa), _lib.XT_CYL_FORCE_EVAL,
                              _lib.XT_COORD_CYL, mmax_use=min(MM, full_m), no_odd=no_odd, perturb=perturb)
     k = 7 if perturb else 5
-    res = [t.cpu().numpy() for t in outs[:k]]
+    res = [dev.to_host(t) for t in outs[:k]]
     return tuple(float(v[0]) for v in res) if scalar else tuple(res)
 
 
@@ -298,5 +322,5 @@ def accumulated_eval(r, z, phi, accum_cos, accum_sin, potC, rforceC, zforceC, de
     (ra, za, pa), scalar = _pts(r, z, phi)
     outs = table.eval_points(field, dev.to_dev(ra), dev.to_dev(za), dev.to_dev(pa), _lib.XT_CYL_ACCUMULATED_EVAL,
                              _lib.XT_COORD_CYL, no_odd=no_odd)
-    res = [t.cpu().numpy() for t in outs[:7]]
+    res = [dev.to_host(t) for t in outs[:7]]
     return tuple(float(v[0]) for v in res) if scalar else tuple(res)

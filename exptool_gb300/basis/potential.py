@@ -144,7 +144,7 @@ class Fields:
         outs = dev.fields_forces(sf, cf, dev.to_dev(x), dev.to_dev(y), dev.to_dev(z), rotpos=rot, rotpos_scalar=rs,
                                  halo_l=self._halo_l(), disk_m=self._disk_m(), no_odd=self.no_odd,
                                  trig_l=not self.halo_correct_m)
-        res = [t.cpu().numpy() for t in outs]
+        res = [dev.to_host(t) for t in outs]
         return tuple(float(v[0]) for v in res) if scalar else tuple(res)
 
     def return_forces_cyl(self, xval, yval, zval, rotpos=0.0):
@@ -168,7 +168,7 @@ class Fields:
         hfr, hft, hfp, hp, hp0 = self._sph.eval_points(sf, dev.to_dev(r3), dev.to_dev(costh), dev.to_dev(phi),
                                                        _lib.XT_SPH_FORCE_EVAL, _lib.XT_COORD_SPH, no_odd=self.no_odd,
                                                        lmax_use=self._halo_l(), trig_l=not self.halo_correct_m)[:5]
-        dfr, dfp, dfz, dp, hfr, hft, hfp, hp, hp0 = (t.cpu().numpy() for t in (dfr, dfp, dfz, dp, hfr, hft, hfp, hp,
+        dfr, dfp, dfz, dp, hfr, hft, hfp, hp, hp0 = (dev.to_host(t) for t in (dfr, dfp, dfz, dp, hfr, hft, hfp, hp,
                                                                              hp0))
         inner = r3 < np.min(self.xihalo)
         hfp = np.where(inner, 0.0, hfp)

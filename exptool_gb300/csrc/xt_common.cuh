@@ -66,6 +66,23 @@ __device__ __forceinline__ R r_to_xi(R r, int cmap, R scale) {
   return (r < R(0)) ? R(0) : out;
 }
 
+// r_to_xi with the scale division replaced by a multiplication by its
+// reciprocal (one rounding of difference; FP64 division is a multi-instruction
+// sequence on the FP64 pipe).
+template <typename R>
+__device__ __forceinline__ R r_to_xi_inv(R r, int cmap, R inv_scale) {
+  R out;
+  if (cmap == 1) {
+    const R u = r * inv_scale;
+    out = (u - R(1)) / (u + R(1));
+  } else if (cmap == 2) {
+    out = log(r);
+  } else {
+    out = r;
+  }
+  return (r < R(0)) ? R(0) : out;
+}
+
 // compatibility.d_xi_to_r (compatibility.py:65-80)
 template <typename R>
 __device__ __forceinline__ R d_xi_to_r(R xi, int cmap, R scale) {
@@ -78,6 +95,12 @@ __device__ __forceinline__ R d_xi_to_r(R xi, int cmap, R scale) {
 template <typename R>
 __device__ __forceinline__ R z_to_y(R z, R hscale) {
   return (z / (fabs(z) + R(1.0e-8))) * asinh(fabs(z / hscale));
+}
+
+// z_to_y with z/h as a multiplication by 1/h.
+template <typename R>
+__device__ __forceinline__ R z_to_y_inv(R z, R inv_hscale) {
+  return (z / (fabs(z) + R(1.0e-8))) * asinh(fabs(z * inv_hscale));
 }
 
 // cos(phi), sin(phi) of phi = atan2(y, x) without the arctangent:

@@ -11,10 +11,12 @@
 // contracts the coefficients with the tables into per-node fields first
 // (cos/sin-weighted pot, rforce, zforce[, dens] per m), so each particle
 // reads 4 corners x (mmax+1) x 6 values instead of 4 x 6 x (mmax+1) x norder.
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
 
+#include "xt_df.cuh"
 #include "xt_internal.cuh"
 
 namespace xt {
@@ -24,12 +26,22 @@ struct CylHandle {
   double XMIN, dX, YMIN, dY, ascale, hscale;
   size_t nnode;
   double* tab = nullptr;   // [8][mmax+1][norder][nnode]: potC rforceC zforceC densC potS rforceS zforceS densS
+  float* tab_f32 = nullptr;  // the same tables rounded to FP32 (mixed path)
   CylTab<double> tab_d;
   CylTab<float> tab_f;
 };
 
 static inline const double* tab_ptr(const CylHandle* h, int which) {
   return h->tab + (size_t)which * (h->mmax + 1) * h->norder * h->nnode;
+}
+
+static inline const float* tab_ptr_f32(const CylHandle* h, int which) {
+  return h->tab_f32 + (size_t)which * (h->mmax + 1) * h->norder * h->nnode;
+}
+
+__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
 }
 
 constexpr double FOUR_PI_C = 4.0 * PI;
@@ -79,8 +91,9 @@ __global__ void __launch_bounds__(256) k_cyl_deposit(CylTab<R> T, const double* 
 }
 
 // Partial dot products: block (chunk, out) with out = (m*norder + k)*2 + cs.
-__global__ void __launch_bounds__(256) k_cyl_contract_partial(const double* __restrict__ potC,
-                                                              const double* __restrict__ potS,
+template <typename TT>
+__global__ void __launch_bounds__(256) k_cyl_contract_partial(const TT* __restrict__ potC,
+                                                              const TT* __restrict__ potS,
                                                               const double* __restrict__ D, int mmax, int norder,
                                                               size_t nnode, int nchunk, double* __restrict__ part) {
   const int chunk = blockIdx.x;
@@ -90,12 +103,24 @@ __global__ void __launch_bounds__(256) k_cyl_contract_partial(const double* __re
   const int m = mk / norder;
   double acc = 0.0;
   if (!(cs == 1 && m == 0)) {
-    const double* t = (cs ? potS : potC) + (size_t)mk * nnode;
+    const TT* t = (cs ? potS : potC) + (size_t)mk * nnode;
     const double* d = D + (size_t)(2 * m + cs) * nnode;
     const size_t per = (nnode + nchunk - 1) / nchunk;
     const size_t lo = (size_t)chunk * per;
     const size_t hi = lo + per < nnode ? lo + per : nnode;
-    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) acc += t[i] * d[i];
+    const size_t step = blockDim.x;
+    size_t i = lo + threadIdx.x;
+    double a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (; i + 3 * step < hi; i += 4 * step) {
+      const TT t0 = t[i], t1 = t[i + step], t2 = t[i + 2 * step], t3 = t[i + 3 * step];
+      const double d0 = d[i], d1 = d[i + step], d2 = d[i + 2 * step], d3 = d[i + 3 * step];
+      acc += (double)t0 * d0;
+      a1 += (double)t1 * d1;
+      a2 += (double)t2 * d2;
+      a3 += (double)t3 * d3;
+    }
+    for (; i < hi; i += step) acc += (double)t[i] * d[i];
+    acc += a1 + a2 + a3;
   }
   __shared__ double sh[32];
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
@@ -123,8 +148,8 @@ __global__ void k_cyl_contract_final(const double* __restrict__ part, int nout, 
 // Fields F[(node*(mmax+1) + m)*nf + f] for m <= muse (m > muse left 0).
 // A block owns TN consecutive nodes; thread t reads table rows coalesced
 // along nodes and the tile is written back contiguously through shared memory.
-template <typename R, int TN>
-__global__ void __launch_bounds__(256) k_cyl_field(const double* __restrict__ tab, const double* __restrict__ cosc,
+template <typename R, int TN, typename TT>
+__global__ void __launch_bounds__(256) k_cyl_field(const TT* __restrict__ tab, const double* __restrict__ cosc,
                                                    const double* __restrict__ sinc, int mmax, int norder,
                                                    size_t nnode, int muse, int nuse, int nf, R* __restrict__ F) {
   extern __shared__ unsigned char smem_raw[];
@@ -143,8 +168,8 @@ __global__ void __launch_bounds__(256) k_cyl_field(const double* __restrict__ ta
     if (node < nnode && m <= muse && !(m == 0 && (f == 3 || f == 4 || f == 5 || f == 7))) {
       const int ti = tmap[f];
       const double* coef = (ti >= 4) ? sinc : cosc;
-      const double* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
-      for (int k = 0; k < nuse; ++k) acc += coef[m * norder + k] * t[(size_t)k * nnode];
+      const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
+      for (int k = 0; k < nuse; ++k) acc += coef[m * norder + k] * (double)t[(size_t)k * nnode];
     }
     tile[nl * mf_total + mf] = (R)acc;
   }
@@ -213,6 +238,453 @@ __global__ void __launch_bounds__(128) k_cyl_eval(CylTab<R> T, const R* __restri
   }
 }
 
+
+// ------------------------------------------------------------------ fused accumulate + evaluate
+// Used when coefficients are accumulated from, and forces evaluated at, the
+// same particles (eof.compute_coefficients followed by eof.compute_forces on
+// one snapshot).  The per-particle set-up (maps, bins, bilinear weights,
+// cos/sin phi) is computed once; particles are counting-sorted by table cell
+// so that warps deposit into and gather from the same few nodes.
+
+// Records, structure of arrays with n entries each: the fractional cell
+// coordinates dx = X - ix, dy = Y - iy (the bilinear weights are products of
+// dx, dy and their complements), cos phi, sin phi, -4 pi m.
+constexpr int kRec = 5;
+
+template <typename R>
+__device__ __forceinline__ void weights_from_frac(R dx, R dy, R w[4]) {
+  const R ex = R(1) - dx, ey = R(1) - dy;
+  w[0] = ex * ey;   // c00 = (ix+1-X)(iy+1-Y)
+  w[1] = dx * ey;   // c10
+  w[2] = ex * dy;   // c01
+  w[3] = dx * dy;   // c11
+}
+
+template <typename RT, typename R>
+__device__ __forceinline__ RT to_rec(R v);
+template <>
+__device__ __forceinline__ float to_rec<float, float>(float v) { return v; }
+template <>
+__device__ __forceinline__ double to_rec<double, double>(double v) { return v; }
+template <>
+__device__ __forceinline__ df to_rec<df, double>(double v) { return df_from(v); }
+
+// RT = record type: float (mixed path), df (FP64 path: values computed in FP64,
+// stored as hi/lo FP32 pairs for the double-float deposit and evaluation).
+template <typename R, typename RT>
+__global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* __restrict__ x,
+                                                    const double* __restrict__ y, const double* __restrict__ z,
+                                                    const double* __restrict__ mass, long long n,
+                                                    int* __restrict__ hist, int* __restrict__ cell,
+                                                    int* __restrict__ slot, RT* __restrict__ rec,
+                                                    double* __restrict__ Rout, int nan_to_origin) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    R xx = (R)x[p], yy = (R)y[p], zz = (R)z[p];
+    // eof.compute_coefficients places particles with NaN coordinates at the origin (eof.py:1189-1204)
+    if (nan_to_origin && (isnan(xx) || isnan(yy) || isnan(zz))) xx = yy = zz = R(0);
+    const R Rc = sqrt(xx * xx + yy * yy + R(1.0e-10));
+    R c1, s1;
+    unit_phi(xx, yy, c1, s1);
+    // the mapping and clamps of cyl_bins (eof.return_bins), keeping X - ix and Y - iy
+    R X = (r_to_xi_inv(Rc, T.cmap, T.inv_ascale) - T.XMIN) * T.inv_dX;
+    R Y = (z_to_y_inv(zz, T.inv_hscale) - T.YMIN) * T.inv_dY;
+    R fx = trunc(X), fy = trunc(Y);
+    if (!(fx >= R(0))) fx = R(0);
+    if (!(fy >= R(0))) fy = R(0);
+    if (X < R(0)) X = R(0);
+    if (Y < R(0)) Y = R(0);
+    if (fx >= R(T.numx)) fx = R(T.numx - 1);
+    if (fy >= R(T.numy)) fy = R(T.numy - 1);
+    const int ix = (int)fx, iy = (int)fy;
+    const int c = ix * T.numy + iy;
+    cell[p] = c;
+    slot[p] = atomicAdd(hist + c, 1);
+    rec[0 * n + p] = to_rec<RT, R>(X - fx);
+    rec[1 * n + p] = to_rec<RT, R>(Y - fy);
+    rec[2 * n + p] = to_rec<RT, R>(c1);
+    rec[3 * n + p] = to_rec<RT, R>(s1);
+    rec[4 * n + p] = to_rec<RT, R>(R(-FOUR_PI_C) * (R)mass[p]);
+    if (Rout) Rout[p] = (double)Rc;
+  }
+}
+
+// Exclusive prefix sum of hist[0..ncell) into off[] in two levels: tiles of
+// 1024 cells scanned by one block each (warp shuffles), then the tile totals.
+constexpr int kScanTile = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan_1024(int v, int* warp_tot, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = warp_tot[lane];
+    int u = t;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, u, d);
+      if (lane >= d) u += y;
+    }
+    warp_tot[lane] = u - t;           // exclusive prefix of warp totals
+    if (lane == 31) warp_tot[32] = u;
+  }
+  __syncthreads();
+  total = warp_tot[32];
+  return x - v + warp_tot[wid];
+}
+
+__global__ void __launch_bounds__(kScanTile) k_scan_tiles(const int* __restrict__ hist, int* __restrict__ off,
+                                                          int* __restrict__ tile_sum, int ncell) {
+  __shared__ int wt[33];
+  const int i = blockIdx.x * kScanTile + threadIdx.x;
+  const int v = i < ncell ? hist[i] : 0;
+  int total;
+  const int ex = block_exclusive_scan_1024(v, wt, total);
+  if (i < ncell) off[i] = ex;
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// Adds the exclusive prefix of the tile totals (scanned by every block from
+// the tile_sum array; ntile <= 1024) to each cell offset.
+__global__ void __launch_bounds__(kScanTile) k_scan_add(int* __restrict__ off, const int* __restrict__ tile_sum,
+                                                        int ncell, int ntile) {
+  __shared__ int wt[33];
+  __shared__ int pref;
+  const int t = threadIdx.x;
+  int total;
+  const int ex = block_exclusive_scan_1024(t < ntile ? tile_sum[t] : 0, wt, total);
+  if (t == blockIdx.x) pref = ex;
+  __syncthreads();
+  const int i = blockIdx.x * kScanTile + t;
+  if (i < ncell) off[i] += pref;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __restrict__ cell,
+                                                     const int* __restrict__ slot, const int* __restrict__ off,
+                                                     const R* __restrict__ rec, R* __restrict__ srec,
+                                                     int* __restrict__ scell, int* __restrict__ sorig) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int c = cell[p];
+    const long long q = (long long)off[c] + slot[p];
+#pragma unroll
+    for (int k = 0; k < kRec; ++k) srec[k * n + q] = rec[k * n + p];
+    scell[q] = c;
+    sorig[q] = (int)p;
+  }
+}
+
+// Deposit of sorted records: each thread takes RUN consecutive particles and
+// sums their contributions per (m, cos/sin, corner) in registers while the
+// cell stays the same, issuing the FP64 atomics once per run and cell.
+template <typename R, int MCAP, int RUN>
+__global__ void __launch_bounds__(128) k_cyl_deposit_sorted(CylTab<R> T, long long n, const R* __restrict__ srec,
+                                                            const int* __restrict__ scell, double* __restrict__ D,
+                                                            size_t nnode) {
+  const int ny1 = T.numy + 1;
+  const int mmax = T.mmax;
+  const long long nrun = (n + RUN - 1) / RUN;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nrun;
+       r += (long long)gridDim.x * blockDim.x) {
+    R acc[2 * MCAP + 1][4];
+#pragma unroll
+    for (int j = 0; j < 2 * MCAP + 1; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[j][k] = R(0);
+    int cur = -1;
+    auto flush = [&](int c) {
+      const int ix = c / T.numy, iy = c - ix * T.numy;
+      const size_t n00 = (size_t)ix * ny1 + iy, n10 = n00 + ny1, n01 = n00 + 1, n11 = n10 + 1;
+#pragma unroll
+      for (int j = 0; j < 2 * MCAP + 1; ++j) {
+        if (j > 2 * mmax) break;
+        const int m = (j + 1) / 2;             // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
+        const int cs = (j == 0) ? 0 : ((j & 1) ? 0 : 1);
+        double* d = D + (size_t)(2 * m + cs) * nnode;
+        atomicAdd(d + n00, (double)acc[j][0]);
+        atomicAdd(d + n10, (double)acc[j][1]);
+        atomicAdd(d + n01, (double)acc[j][2]);
+        atomicAdd(d + n11, (double)acc[j][3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[j][k] = R(0);
+      }
+    };
+    const long long q0 = r * RUN;
+#pragma unroll 1
+    for (int u = 0; u < RUN; ++u) {
+      const long long q = q0 + u;
+      if (q >= n) break;
+      const int c = scell[q];
+      if (c != cur) {
+        if (cur >= 0) flush(cur);
+        cur = c;
+      }
+      R w[4];
+      weights_from_frac(srec[0 * n + q], srec[1 * n + q], w);
+      const R c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
+      R cprev = R(1), sprev = R(0), ccur = c1, scur = s1;
+#pragma unroll
+      for (int m = 0; m <= MCAP; ++m) {
+        if (m > mmax) break;
+        R cm, sm;
+        if (m == 0) { cm = R(1); sm = R(0); }
+        else if (m == 1) { cm = c1; sm = s1; }
+        else {
+          cm = R(2) * c1 * ccur - cprev;
+          sm = R(2) * c1 * scur - sprev;
+          cprev = ccur; sprev = scur; ccur = cm; scur = sm;
+        }
+        const R wc = base * cm;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[m == 0 ? 0 : 2 * m - 1][k] += wc * w[k];
+        if (m > 0) {
+          const R ws = base * sm;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[2 * m][k] += ws * w[k];
+        }
+      }
+    }
+    if (cur >= 0) flush(cur);
+  }
+}
+
+// Evaluation of sorted records (accumulated_eval_particles outputs p0 p fr fp fz),
+// written back to the particles' original slots.
+template <typename R>
+__global__ void __launch_bounds__(128) k_cyl_eval_sorted(CylTab<R> T, const R* __restrict__ F, long long n,
+                                                         const R* __restrict__ srec, const int* __restrict__ scell,
+                                                         const int* __restrict__ sorig, CylEvalOpts o, double* o0,
+                                                         double* o1, double* o2, double* o3, double* o4) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int c = scell[q];
+    const int ix = c / T.numy, iy = c - ix * T.numy;
+    CylBins<R> B;
+    B.node = ix * (T.numy + 1) + iy;
+    R w[4];
+    weights_from_frac(srec[0 * n + q], srec[1 * n + q], w);
+    B.c00 = w[0];
+    B.c10 = w[1];
+    B.c01 = w[2];
+    B.c11 = w[3];
+    R v[9];
+    cyl_eval_bins(T, F, B, srec[2 * n + q], srec[3 * n + q], o, v);
+    const int p = sorig[q];
+    if (o0) o0[p] = v[0];
+    if (o1) o1[p] = v[1];
+    if (o2) o2[p] = v[2];
+    if (o3) o3[p] = v[3];
+    if (o4) o4[p] = v[4];
+  }
+}
+
+
+__device__ __forceinline__ void df_weights(df dx, df dy, df w[4]) {
+  const df one{1.f, 0.f};
+  const df ex = df_sub(one, dx), ey = df_sub(one, dy);
+  w[0] = df_mul(ex, ey);
+  w[1] = df_mul(dx, ey);
+  w[2] = df_mul(ex, dy);
+  w[3] = df_mul(dx, dy);
+}
+
+// Double-float deposit of sorted records (FP64 path): as k_cyl_deposit_sorted,
+// with the per-run sums kept as df and converted to FP64 for the atomics.
+template <int MCAP, int RUN>
+__global__ void __launch_bounds__(128) k_cyl_deposit_sorted_df(CylTab<double> T, long long n,
+                                                               const df* __restrict__ srec,
+                                                               const int* __restrict__ scell, double* __restrict__ D,
+                                                               size_t nnode) {
+  const int ny1 = T.numy + 1;
+  const int mmax = T.mmax;
+  const long long nrun = (n + RUN - 1) / RUN;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nrun;
+       r += (long long)gridDim.x * blockDim.x) {
+    df acc[2 * MCAP + 1][4];
+#pragma unroll
+    for (int j = 0; j < 2 * MCAP + 1; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[j][k] = df{0.f, 0.f};
+    int cur = -1;
+    auto flush = [&](int c) {
+      const int ix = c / T.numy, iy = c - ix * T.numy;
+      const size_t n00 = (size_t)ix * ny1 + iy, n10 = n00 + ny1, n01 = n00 + 1, n11 = n10 + 1;
+#pragma unroll
+      for (int j = 0; j < 2 * MCAP + 1; ++j) {
+        if (j > 2 * mmax) break;
+        const int m = (j + 1) / 2;
+        const int cs = (j == 0) ? 0 : ((j & 1) ? 0 : 1);
+        double* d = D + (size_t)(2 * m + cs) * nnode;
+        atomicAdd(d + n00, df_to(acc[j][0]));
+        atomicAdd(d + n10, df_to(acc[j][1]));
+        atomicAdd(d + n01, df_to(acc[j][2]));
+        atomicAdd(d + n11, df_to(acc[j][3]));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[j][k] = df{0.f, 0.f};
+      }
+    };
+    const long long q0 = r * RUN;
+#pragma unroll 1
+    for (int u = 0; u < RUN; ++u) {
+      const long long q = q0 + u;
+      if (q >= n) break;
+      const int c = scell[q];
+      if (c != cur) {
+        if (cur >= 0) flush(cur);
+        cur = c;
+      }
+      df w[4];
+      df_weights(srec[0 * n + q], srec[1 * n + q], w);
+      const df c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
+      df cprev{1.f, 0.f}, sprev{0.f, 0.f}, ccur = c1, scur = s1;
+#pragma unroll
+      for (int m = 0; m <= MCAP; ++m) {
+        if (m > mmax) break;
+        df cm, sm;
+        if (m == 0) { cm = df{1.f, 0.f}; sm = df{0.f, 0.f}; }
+        else if (m == 1) { cm = c1; sm = s1; }
+        else {
+          cm = df_sub(df_scale(df_mul(c1, ccur), 2.f), cprev);
+          sm = df_sub(df_scale(df_mul(c1, scur), 2.f), sprev);
+          cprev = ccur; sprev = scur; ccur = cm; scur = sm;
+        }
+        const df wc = df_mul(base, cm);
+        const int jc = (m == 0) ? 0 : 2 * m - 1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[jc][k] = df_fma(wc, w[k], acc[jc][k]);
+        if (m > 0) {
+          const df ws = df_mul(base, sm);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[2 * m][k] = df_fma(ws, w[k], acc[2 * m][k]);
+        }
+      }
+    }
+    if (cur >= 0) flush(cur);
+  }
+}
+
+// In-place FP64 -> df conversion of a field (8 bytes either way).
+__global__ void k_split_df(double* __restrict__ f, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = f[i];
+    reinterpret_cast<df*>(f)[i] = df_from(v);
+  }
+}
+
+__device__ __forceinline__ df load_df(const df* p) { return *p; }
+__device__ __forceinline__ df load_df(const float* p) { return df{*p, 0.f}; }
+
+template <typename OT>
+__device__ __forceinline__ OT from_df(df v);
+template <>
+__device__ __forceinline__ df from_df<df>(df v) { return v; }
+template <>
+__device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
+
+// Field for the mixed fused path: coefficients staged in shared memory as df,
+// accumulation in df over the FP32 table rows, FP32 output (no FP64 pipe
+// work at all).  Layout as k_cyl_field with nf = 6.
+template <typename TT, typename OT, int TN>
+__global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, const double* __restrict__ cosc,
+                                                    const double* __restrict__ sinc, int mmax, int norder,
+                                                    size_t nnode, OT* __restrict__ F) {
+  extern __shared__ unsigned char smem_raw[];
+  df* cf = reinterpret_cast<df*>(smem_raw);                       // [2][(mmax+1)*norder]
+  OT* tile = reinterpret_cast<OT*>(cf + 2 * (mmax + 1) * norder);
+  const int ncoef = (mmax + 1) * norder;
+  for (int i = threadIdx.x; i < 2 * ncoef; i += blockDim.x) cf[i] = df_from(i < ncoef ? cosc[i] : sinc[i - ncoef]);
+  __syncthreads();
+  const int nf = 6;
+  const int mf_total = (mmax + 1) * nf;
+  const size_t node0 = (size_t)blockIdx.x * TN;
+  const size_t tsize = (size_t)(mmax + 1) * norder * nnode;
+  const int tmap[6] = {0, 1, 2, 4, 5, 6};
+  for (int idx = threadIdx.x; idx < TN * mf_total; idx += blockDim.x) {
+    const int nl = idx % TN;
+    const int mf = idx / TN;
+    const int m = mf / nf, f = mf % nf;
+    const size_t node = node0 + nl;
+    df acc{0.f, 0.f};
+    if (node < nnode && !(m == 0 && f >= 3)) {
+      const int ti = tmap[f];
+      const df* coef = cf + ((ti >= 4) ? ncoef : 0) + m * norder;
+      const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
+      for (int k = 0; k < norder; ++k) acc = df_fma(coef[k], load_df(t + (size_t)k * nnode), acc);
+    }
+    tile[nl * mf_total + mf] = from_df<OT>(acc);
+  }
+  __syncthreads();
+  const size_t nvalid = (node0 + TN <= nnode) ? TN : (nnode - node0);
+  OT* dst = F + node0 * mf_total;
+  for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) dst[idx] = tile[idx];
+}
+
+// Double-float evaluation of sorted records (FP64 path, accumulated_eval_particles).
+__global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
+                                                            const df* __restrict__ srec,
+                                                            const int* __restrict__ scell,
+                                                            const int* __restrict__ sorig, int m1, int m2,
+                                                            double* o0, double* o1, double* o2, double* o3,
+                                                            double* o4) {
+  const int ny1 = T.numy + 1;
+  const int stride = (T.mmax + 1) * 6;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int c = scell[q];
+    const int ix = c / T.numy, iy = c - ix * T.numy;
+    const df* f00 = F + (size_t)(ix * ny1 + iy) * stride;
+    const df* f01 = f00 + stride;
+    const df* f10 = f00 + (size_t)ny1 * stride;
+    const df* f11 = f10 + stride;
+    df w[4];
+    df_weights(srec[0 * n + q], srec[1 * n + q], w);
+    const df w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+    const df c1 = srec[2 * n + q], s1 = srec[3 * n + q];
+    const df zero{0.f, 0.f};
+    df p0 = zero, p = zero, fr = zero, fp = zero, fz = zero;
+    df cprev{1.f, 0.f}, sprev = zero, ccur = c1, scur = s1;
+#pragma unroll 1
+    for (int m = 0; m <= T.mmax; ++m) {
+      df cm, sm;
+      if (m == 0) { cm = df{1.f, 0.f}; sm = zero; }
+      else if (m == 1) { cm = c1; sm = s1; }
+      else {
+        cm = df_sub(df_scale(df_mul(c1, ccur), 2.f), cprev);
+        sm = df_sub(df_scale(df_mul(c1, scur), 2.f), sprev);
+        cprev = ccur; sprev = scur; ccur = cm; scur = sm;
+      }
+      if (m < m1 || m > m2) continue;
+      const int b = m * 6;
+      df v[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+        v[k] = df_fma(f11[b + k], w3, df_fma(f01[b + k], w2, df_fma(f10[b + k], w1, df_mul(f00[b + k], w0))));
+      const df pm = df_fma(cm, v[0], df_mul(sm, v[3]));
+      const df frm = df_fma(cm, v[1], df_mul(sm, v[4]));
+      const df fzm = df_fma(cm, v[2], df_mul(sm, v[5]));
+      const df fpm = df_scale(df_sub(df_mul(sm, v[0]), df_mul(cm, v[3])), (float)m);
+      if (m == 0) p0 = pm;
+      else p = df_add(p, pm);
+      fr = df_add(fr, frm);
+      fz = df_add(fz, fzm);
+      fp = df_add(fp, fpm);
+    }
+    const int pidx = sorig[q];
+    if (o0) o0[pidx] = df_to(p0);
+    if (o1) o1[pidx] = df_to(p);
+    if (o2) o2[pidx] = df_to(fr);
+    if (o3) o3[pidx] = df_to(fp);
+    if (o4) o4[pidx] = df_to(fz);
+  }
+}
+
 static const int kContractChunks = 8;
 
 bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f) {
@@ -263,9 +735,25 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
       return cuda_fail(e, "upload EOF tables");
     }
   }
-  h->tab_d = CylTab<double>{mmax, norder, numx, numy, cmap, XMIN, dX, YMIN, dY, ascale, hscale};
+  h->tab_d = CylTab<double>{mmax, norder, numx, numy, cmap, XMIN, dX, YMIN, dY, ascale, hscale,
+                            1.0 / dX, 1.0 / dY, 1.0 / ascale, 1.0 / hscale};
   h->tab_f = CylTab<float>{mmax, norder, numx, numy, cmap, (float)XMIN, (float)dX, (float)YMIN, (float)dY,
-                           (float)ascale, (float)hscale};
+                           (float)ascale, (float)hscale, (float)(1.0 / dX), (float)(1.0 / dY),
+                           (float)(1.0 / ascale), (float)(1.0 / hscale)};
+  // FP32 copy of the tables for the mixed path (halves the table traffic of
+  // its contraction and field kernels)
+  e = cudaMalloc((void**)&h->tab_f32, 8 * tsize * sizeof(float));
+  if (e == cudaSuccess) {
+    k_to_f32<<<grid_for((long long)(8 * tsize), 256, 8), 256>>>(h->tab, h->tab_f32, 8 * tsize);
+    e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    cudaFree(h->tab);
+    if (h->tab_f32) cudaFree(h->tab_f32);
+    delete h;
+    return cuda_fail(e, "FP32 copy of the EOF tables");
+  }
   *handle = h;
   return XT_OK;
 }
@@ -274,6 +762,7 @@ int xt_cyl_table_destroy(void* handle) {
   CylHandle* h = static_cast<CylHandle*>(handle);
   if (h) {
     if (h->tab) cudaFree(h->tab);
+    if (h->tab_f32) cudaFree(h->tab_f32);
     delete h;
   }
   return XT_OK;
@@ -317,8 +806,12 @@ int xt_cyl_accumulate(void* handle, const double* x, const double* y, const doub
   }
   const int nout = (h->mmax + 1) * h->norder * 2;
   dim3 g(kContractChunks, nout);
-  k_cyl_contract_partial<<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder, h->nnode,
-                                            kContractChunks, part);
+  if (precision == XT_F64)
+    k_cyl_contract_partial<double><<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder, h->nnode,
+                                                      kContractChunks, part);
+  else
+    k_cyl_contract_partial<float><<<g, 256, 0, st>>>(tab_ptr_f32(h, 0), tab_ptr_f32(h, 4), D, h->mmax, h->norder,
+                                                     h->nnode, kContractChunks, part);
   XT_CHECK_LAUNCH("k_cyl_contract_partial");
   k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
   XT_CHECK_LAUNCH("k_cyl_contract_final");
@@ -352,15 +845,15 @@ int xt_cyl_prepare(void* handle, const double* cos_c, const double* sin_c, int m
   const size_t mf = (size_t)(h->mmax + 1) * nf;
   if (precision == XT_F64) {
     const size_t sm = TN * mf * sizeof(double);
-    if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<double, TN>,
+    if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<double, TN, double>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field<double, TN><<<blocks, 256, sm, st>>>(h->tab, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
+    k_cyl_field<double, TN, double><<<blocks, 256, sm, st>>>(h->tab, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
                                                     nmax_use, nf, static_cast<double*>(field));
   } else {
     const size_t sm = TN * mf * sizeof(float);
-    if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<float, TN>,
+    if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<float, TN, float>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field<float, TN><<<blocks, 256, sm, st>>>(h->tab, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
+    k_cyl_field<float, TN, float><<<blocks, 256, sm, st>>>(h->tab_f32, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
                                                    nmax_use, nf, static_cast<float*>(field));
   }
   XT_CHECK_LAUNCH("k_cyl_field");
@@ -396,6 +889,229 @@ int xt_cyl_eval_points(void* handle, const void* field, int precision, int densi
                                               outs[7]);
   XT_CHECK_LAUNCH("k_cyl_eval");
   return XT_OK;
+}
+
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static int deposit_run_length() {
+  static int v = 0;
+  if (v == 0) {
+    const char* e = getenv("XT_DEPOSIT_RUN");
+    const int r = e ? atoi(e) : 8;
+    v = (r == 8 || r == 16 || r == 32) ? r : 8;
+  }
+  return v;
+}
+
+// Optional stage timing of xt_cyl_accumulate_eval: CUDA events recorded on the
+// call's stream between its stages (binrec, scan, scatter, deposit, contract,
+// field, eval), read back by xt_timing_read.  Off unless xt_timing_enable(1).
+static thread_local int g_timing = 0;
+static thread_local cudaEvent_t g_ev[8] = {};
+static thread_local int g_nev = 0;
+
+static int timing_mark(int k, cudaStream_t st) {
+  if (!g_timing) return XT_OK;
+  if (!g_ev[k]) XT_CUDA(cudaEventCreate(&g_ev[k]));
+  XT_CUDA(cudaEventRecord(g_ev[k], st));
+  g_nev = k + 1;
+  return XT_OK;
+}
+
+struct FusedLayout {
+  size_t grid, part, hist, off, tsum, cell, slot, rec, srec, scell, sorig, field, total;
+};
+
+static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) {
+  const size_t rs = precision == XT_F32 ? sizeof(float) : sizeof(double);
+  const size_t ncell = (size_t)h->numx * h->numy;
+  FusedLayout L;
+  size_t o = 0;
+  auto take = [&](size_t b) { size_t at = o; o += align256(b); return at; };
+  L.grid = take((size_t)(h->mmax + 1) * 2 * h->nnode * sizeof(double));
+  L.part = take((size_t)(h->mmax + 1) * h->norder * 2 * kContractChunks * sizeof(double));
+  L.hist = take(ncell * sizeof(int));
+  L.off = take(ncell * sizeof(int));
+  L.tsum = take(kScanTile * sizeof(int));
+  L.cell = take((size_t)n * sizeof(int));
+  L.slot = take((size_t)n * sizeof(int));
+  L.rec = take((size_t)n * kRec * rs);
+  L.srec = take((size_t)n * kRec * rs);
+  L.scell = take((size_t)n * sizeof(int));
+  L.sorig = take((size_t)n * sizeof(int));
+  L.field = take(h->nnode * (h->mmax + 1) * 6 * rs);
+  L.total = o;
+  return L;
+}
+
+int xt_timing_enable(int on) {
+  g_timing = on ? 1 : 0;
+  g_nev = 0;
+  return XT_OK;
+}
+
+int xt_timing_read(double* ms_out, int max) {
+  XT_REQUIRE(ms_out && max >= 0, "NULL output");
+  int k = 0;
+  if (g_nev >= 2) {
+    XT_CUDA(cudaEventSynchronize(g_ev[g_nev - 1]));
+    for (; k < g_nev - 1 && k < max; ++k) {
+      float ms = 0.f;
+      XT_CUDA(cudaEventElapsedTime(&ms, g_ev[k], g_ev[k + 1]));
+      ms_out[k] = ms;
+    }
+  }
+  return k;
+}
+
+size_t xt_cyl_accumulate_eval_workspace(void* handle, long long n, int precision) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  if (!h || n < 0) return 0;
+  return fused_layout(h, n, precision).total;
+}
+
+int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const double* z, const double* m,
+                           long long n, int precision, int m1, int m2, int nan_to_origin, double* cos_out,
+                           double* sin_out, double* const* outs, void* workspace, size_t workspace_bytes,
+                           void* stream) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  XT_REQUIRE(h, "NULL table handle");
+  XT_REQUIRE(n >= 0 && n < (1LL << 31), "particle count must be in [0, 2^31)");
+  XT_REQUIRE(cos_out && sin_out && outs, "NULL output");
+  XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
+  XT_REQUIRE(precision == XT_F64 || precision == XT_F32, "bad precision %d", precision);
+  XT_REQUIRE(h->mmax <= 8 && h->norder <= 24, "the fused path supports mmax <= 8, norder <= 24 (got %d, %d)",
+             h->mmax, h->norder);
+  XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
+             "the fused path supports numx*numy <= %d cells", kScanTile * kScanTile);
+  const FusedLayout L = fused_layout(h, n, precision);
+  if (!workspace || workspace_bytes < L.total) {
+    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  cudaStream_t st = as_stream(stream);
+  char* ws = static_cast<char*>(workspace);
+  double* D = reinterpret_cast<double*>(ws + L.grid);
+  double* part = reinterpret_cast<double*>(ws + L.part);
+  int* hist = reinterpret_cast<int*>(ws + L.hist);
+  int* off = reinterpret_cast<int*>(ws + L.off);
+  int* tsum = reinterpret_cast<int*>(ws + L.tsum);
+  int* cell = reinterpret_cast<int*>(ws + L.cell);
+  int* slot = reinterpret_cast<int*>(ws + L.slot);
+  int* scell = reinterpret_cast<int*>(ws + L.scell);
+  int* sorig = reinterpret_cast<int*>(ws + L.sorig);
+  const int ncell = h->numx * h->numy;
+  XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->nnode * sizeof(double), st));
+  XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
+  const int g256 = grid_for(n, 256, 8);
+  const int g128 = grid_for(n, 128, 8);
+  auto run = [&](auto tag) -> int {
+    using R = decltype(tag);
+    constexpr bool F64 = std::is_same<R, double>::value;
+    using RT = typename std::conditional<F64, df, float>::type;   // record type
+    using RM = typename std::conditional<F64, double, float>::type; // same-size type for moving records
+    const CylTab<R>& T = *reinterpret_cast<const CylTab<R>*>(F64 ? (const void*)&h->tab_d : (const void*)&h->tab_f);
+    RT* rec = reinterpret_cast<RT*>(ws + L.rec);
+    RT* srec = reinterpret_cast<RT*>(ws + L.srec);
+    R* field = reinterpret_cast<R*>(ws + L.field);
+    int rc;
+    if ((rc = timing_mark(0, st))) return rc;
+    if (n > 0) {
+      k_cyl_binrec<R, RT><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+      XT_CHECK_LAUNCH("k_cyl_binrec");
+      if ((rc = timing_mark(1, st))) return rc;
+      {
+        const int ntile = (ncell + kScanTile - 1) / kScanTile;
+        k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tsum, ncell);
+        XT_CHECK_LAUNCH("k_scan_tiles");
+        k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tsum, ncell, ntile);
+        XT_CHECK_LAUNCH("k_scan_add");
+      }
+      if ((rc = timing_mark(2, st))) return rc;
+      k_cyl_scatter<RM><<<g256, 256, 0, st>>>(n, cell, slot, off, reinterpret_cast<const RM*>(rec),
+                                              reinterpret_cast<RM*>(srec), scell, sorig);
+      XT_CHECK_LAUNCH("k_cyl_scatter");
+      if ((rc = timing_mark(3, st))) return rc;
+      // run length (particles summed in registers per thread before the FP64
+      // atomics); XT_DEPOSIT_RUN = 8, 16 or 32 overrides the default
+      const int run_len = deposit_run_length();
+      auto dep = [&](auto mc, auto rl) {
+        constexpr int MC = decltype(mc)::value;
+        constexpr int RUN = decltype(rl)::value;
+        const int gr = grid_for((n + RUN - 1) / RUN, 128, 8);
+        if constexpr (F64)
+          k_cyl_deposit_sorted_df<MC, RUN><<<gr, 128, 0, st>>>(T, n, srec, scell, D, h->nnode);
+        else
+          k_cyl_deposit_sorted<R, MC, RUN><<<gr, 128, 0, st>>>(T, n, srec, scell, D, h->nnode);
+      };
+      auto dep_m = [&](auto rl) {
+        if (h->mmax <= 2) dep(std::integral_constant<int, 2>{}, rl);
+        else if (h->mmax <= 4) dep(std::integral_constant<int, 4>{}, rl);
+        else if (h->mmax <= 6) dep(std::integral_constant<int, 6>{}, rl);
+        else dep(std::integral_constant<int, 8>{}, rl);
+      };
+      if (run_len <= 8) dep_m(std::integral_constant<int, 8>{});
+      else if (run_len <= 16) dep_m(std::integral_constant<int, 16>{});
+      else dep_m(std::integral_constant<int, 32>{});
+      XT_CHECK_LAUNCH("k_cyl_deposit_sorted");
+    } else {
+      for (int k = 1; k <= 3; ++k)
+        if ((rc = timing_mark(k, st))) return rc;
+    }
+    if ((rc = timing_mark(4, st))) return rc;
+    const int nout = (h->mmax + 1) * h->norder * 2;
+    dim3 g(kContractChunks, nout);
+    // coefficient contraction from the FP64 tables in both precisions: it is a
+    // reduction of the accumulated sums and stays FP64
+    k_cyl_contract_partial<double><<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder,
+                                                      h->nnode, kContractChunks, part);
+    XT_CHECK_LAUNCH("k_cyl_contract_partial");
+    k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
+    XT_CHECK_LAUNCH("k_cyl_contract_final");
+    if ((rc = timing_mark(5, st))) return rc;
+    constexpr int TN = 32;
+    const int fblocks = (int)((h->nnode + TN - 1) / TN);
+    if constexpr (F64) {
+      // FP64 field, then split in place into double-float pairs for the evaluation
+      const size_t sm = TN * (size_t)(h->mmax + 1) * 6 * sizeof(double);
+      if (sm > 48 * 1024)
+        XT_CUDA(cudaFuncSetAttribute(k_cyl_field<double, TN, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm));
+      k_cyl_field<double, TN, double><<<fblocks, 256, sm, st>>>(h->tab, cos_out, sin_out, h->mmax, h->norder,
+                                                               h->nnode, h->mmax, h->norder, 6,
+                                                               reinterpret_cast<double*>(field));
+      XT_CHECK_LAUNCH("k_cyl_field");
+      const size_t nf = h->nnode * (h->mmax + 1) * 6;
+      k_split_df<<<grid_for((long long)nf, 256, 8), 256, 0, st>>>(reinterpret_cast<double*>(field), nf);
+      XT_CHECK_LAUNCH("k_split_df");
+    } else {
+      // FP32 field from the FP32 tables, coefficients staged as double-float
+      const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) + TN * (size_t)(h->mmax + 1) * 6 * sizeof(float);
+      if (sm > 48 * 1024)
+        XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<float, float, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm));
+      k_cyl_field2<float, float, TN><<<fblocks, 256, sm, st>>>(h->tab_f32, cos_out, sin_out, h->mmax, h->norder,
+                                                              h->nnode, reinterpret_cast<float*>(field));
+      XT_CHECK_LAUNCH("k_cyl_field2");
+    }
+    if ((rc = timing_mark(6, st))) return rc;
+    if (n > 0) {
+      if constexpr (F64) {
+        k_cyl_eval_sorted_df<<<g128, 128, 0, st>>>(T, reinterpret_cast<const df*>(field), n, srec, scell, sorig, m1,
+                                                   m2, outs[0], outs[1], outs[2], outs[3], outs[4]);
+      } else {
+        CylEvalOpts o;
+        o.mode = XT_CYL_ACCUMULATED_EVAL_PARTICLES; o.m1 = m1; o.m2 = m2; o.mmax_use = h->mmax; o.no_odd = 0;
+        o.perturb = 0; o.density = 0; o.nf = 6;
+        k_cyl_eval_sorted<R><<<g128, 128, 0, st>>>(T, field, n, srec, scell, sorig, o, outs[0], outs[1], outs[2],
+                                                   outs[3], outs[4]);
+      }
+      XT_CHECK_LAUNCH("k_cyl_eval_sorted");
+    }
+    return timing_mark(7, st);
+  };
+  return precision == XT_F64 ? run(double{}) : run(float{});
 }
 
 }  // extern "C"

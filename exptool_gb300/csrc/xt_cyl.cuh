@@ -13,6 +13,7 @@ template <typename R>
 struct CylTab {
   int mmax, norder, numx, numy, cmap;
   R XMIN, dX, YMIN, dY, ascale, hscale;
+  R inv_dX, inv_dY, inv_ascale, inv_hscale;
 };
 
 // eof.return_bins + bilinear weights (eof.py:354-427, 436-449).  The lower
@@ -27,8 +28,8 @@ struct CylBins {
 
 template <typename R>
 __device__ __forceinline__ CylBins<R> cyl_bins(const CylTab<R>& T, R Rcyl, R z) {
-  R X = (r_to_xi(Rcyl, T.cmap, T.ascale) - T.XMIN) / T.dX;
-  R Y = (z_to_y(z, T.hscale) - T.YMIN) / T.dY;
+  R X = (r_to_xi_inv(Rcyl, T.cmap, T.inv_ascale) - T.XMIN) * T.inv_dX;
+  R Y = (z_to_y_inv(z, T.inv_hscale) - T.YMIN) * T.inv_dY;
   R fx = trunc(X), fy = trunc(Y);
   if (!(fx >= R(0))) fx = R(0);       // negative or NaN
   if (!(fy >= R(0))) fy = R(0);
@@ -60,11 +61,10 @@ struct CylEvalOpts {
 
 // Field F: per node, per m, nf values
 //   [PC RC ZC PS RS ZS (DC DS)] = sum_n {cos,sin}[m,n] * {pot,rforce,zforce,dens}{C,S}[m,n,node]
-// One point: out = p0 p fr fp fz d0 d fr0 fz0 (mode-specific meaning).
-template <typename R, int MCAP>
-__device__ __forceinline__ void cyl_eval_point(const CylTab<R>& T, const R* __restrict__ F, R Rcyl, R z, R c1,
-                                               R s1, const CylEvalOpts& o, R out[9]) {
-  const CylBins<R> B = cyl_bins(T, Rcyl, z);
+// One point with precomputed bins: out = p0 p fr fp fz d0 d fr0 fz0 (mode-specific meaning).
+template <typename R>
+__device__ __forceinline__ void cyl_eval_bins(const CylTab<R>& T, const R* __restrict__ F, const CylBins<R>& B,
+                                              R c1, R s1, const CylEvalOpts& o, R out[9]) {
   const int ny1 = T.numy + 1;
   const int stride = (T.mmax + 1) * o.nf;
   const R* f00 = F + (size_t)B.node * stride;
@@ -119,6 +119,13 @@ __device__ __forceinline__ void cyl_eval_point(const CylTab<R>& T, const R* __re
   }
   out[0] = p0; out[1] = p; out[2] = fr; out[3] = fp; out[4] = fz;
   out[5] = d0; out[6] = d; out[7] = fr0; out[8] = fz0;
+}
+
+template <typename R, int MCAP>
+__device__ __forceinline__ void cyl_eval_point(const CylTab<R>& T, const R* __restrict__ F, R Rcyl, R z, R c1,
+                                               R s1, const CylEvalOpts& o, R out[9]) {
+  const CylBins<R> B = cyl_bins(T, Rcyl, z);
+  cyl_eval_bins(T, F, B, c1, s1, o, out);
 }
 
 }  // namespace xt

@@ -241,9 +241,11 @@ int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, dou
     return rc;
   }
   const double lo = (cmap == 2) ? log(rmin) : 0.0, hi = (cmap == 2) ? log(rmax) : 0.0;
-  h->tab_d = SphTab<double>{lmax, nmax, numr, cmap, scale, xi0, xi[1] - xi[0], lo, hi, h->xi, h->p0, h->d0, h->fact};
-  h->tab_f = SphTab<float>{lmax, nmax, numr, cmap, (float)scale, (float)xi0, (float)(xi[1] - xi[0]),
-                           (float)lo, (float)hi, h->xi_f, h->p0_f, h->d0_f, h->fact_f};
+  const double dxi = xi[1] - xi[0];
+  h->tab_d = SphTab<double>{lmax, nmax, numr, cmap, scale, xi0, dxi, lo, hi, 1.0 / scale, 1.0 / dxi,
+                            h->xi, h->p0, h->d0, h->fact};
+  h->tab_f = SphTab<float>{lmax, nmax, numr, cmap, (float)scale, (float)xi0, (float)dxi, (float)lo, (float)hi,
+                           (float)(1.0 / scale), (float)(1.0 / dxi), h->xi_f, h->p0_f, h->d0_f, h->fact_f};
   *handle = h;
   return XT_OK;
 }

@@ -14,6 +14,7 @@ template <typename R>
 struct SphTab {
   int lmax, nmax, numr, cmap;
   R scale, xi0, dxi, lo, hi;   // xi0 = min(xi), dxi = xi[1]-xi[0]; lo/hi: cmap=2 clamp
+  R inv_scale, inv_dxi;
   const R* xi;                 // [numr]
   const R* p0;                 // [numr]  model potential on the grid
   const R* d0;                 // [numr]  4 pi rho0 on the grid
@@ -41,7 +42,7 @@ struct SphBins {
 
 template <typename R>
 __device__ __forceinline__ SphBins<R> sph_bins(const SphTab<R>& T, R r, bool need_force, bool need_dens) {
-  R x = r_to_xi(r, T.cmap, T.scale);
+  R x = r_to_xi_inv(r, T.cmap, T.inv_scale);
   if (T.cmap == 1) {
     if (x < R(-1)) x = R(-1);
     if (x >= R(1)) x = R(1) - R(1.0e-08);
@@ -50,12 +51,12 @@ __device__ __forceinline__ SphBins<R> sph_bins(const SphTab<R>& T, R r, bool nee
     if (x < T.lo) x = T.lo;
     if (x > T.hi) x = T.hi;
   }
-  R fi = floor((x - T.xi0) / T.dxi);
+  R fi = floor((x - T.xi0) * T.inv_dxi);
   if (!(fi >= R(0))) fi = R(0);                 // negative or NaN
   if (fi > R(T.numr - 2)) fi = R(T.numr - 2);
   int i = (int)fi;
-  R x1 = (T.xi[i + 1] - x) / T.dxi;
-  R x2 = (x - T.xi[i]) / T.dxi;
+  R x1 = (T.xi[i + 1] - x) * T.inv_dxi;
+  R x2 = (x - T.xi[i]) * T.inv_dxi;
   SphBins<R> B;
   int j = i < 1 ? 1 : i;
   B.i = i;
@@ -69,7 +70,7 @@ __device__ __forceinline__ SphBins<R> sph_bins(const SphTab<R>& T, R r, bool nee
     B.wp[0] = B.lw0; B.wp[1] = B.lw1; B.wp[2] = R(0);
   }
   if (need_force) {
-    R fac = d_xi_to_r(x, T.cmap, T.scale) / T.dxi;
+    R fac = d_xi_to_r(x, T.cmap, T.scale) * T.inv_dxi;
     B.wf[0] = fac * (x2 - R(0.5)) * T.p0[j - 1];
     B.wf[1] = fac * (R(-2) * x2) * T.p0[j];
     B.wf[2] = fac * (x2 + R(0.5)) * T.p0[j + 1];

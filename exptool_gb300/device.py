@@ -46,6 +46,15 @@ def to_dev(a, dtype=torch.float64) -> torch.Tensor:
     return t.contiguous()
 
 
+def to_host(t: torch.Tensor) -> np.ndarray:
+    """Device tensor -> NumPy array in pinned host memory (torch's caching
+    host allocator), so the device-to-host copy is a direct DMA; the array
+    owns its buffer."""
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h.numpy()
+
+
 def dptr(t) -> int:
     return 0 if t is None else t.data_ptr()
 
@@ -217,6 +226,23 @@ class CylTable:
                                                precision_code(precision), dptr(cos), dptr(sin), dptr(ws), ws.numel(),
                                                stream_ptr()), "xt_cyl_accumulate")
         return cos, sin
+
+    def accumulate_eval(self, x, y, z, m, precision="f64", m1=0, m2=1000, workspace=None, nan_to_origin=True):
+        """Fused accumulate + accumulated_eval_particles at the same particles:
+        returns cos, sin, [p0, p, fr, fp, fz, R]."""
+        n = int(x.numel())
+        pc = precision_code(precision)
+        cos = torch.empty((self.mmax + 1, self.norder), dtype=torch.float64, device=x.device)
+        sin = torch.empty_like(cos)
+        outs = [torch.empty(n, dtype=torch.float64, device=x.device) for _ in range(6)]
+        need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
+        ws = workspace if (workspace is not None and workspace.numel() >= need) else \
+            torch.empty(need, dtype=torch.uint8, device=x.device)
+        pp, keep = _lib.ptr_array([dptr(t) for t in outs])
+        _lib.check(self._lib.xt_cyl_accumulate_eval(self.handle, dptr(x), dptr(y), dptr(z), dptr(m), n, pc, int(m1),
+                                                    int(m2), int(bool(nan_to_origin)), dptr(cos), dptr(sin), pp,
+                                                    dptr(ws), ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
+        return cos, sin, outs
 
     def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):
         pc = precision_code(precision)

@@ -139,6 +139,29 @@ int xt_cyl_eval_points(void *handle, const void *field, int precision, int densi
                        const double *a, const double *b, const double *c, long long n, int mode, int m1, int m2,
                        int mmax_use, int no_odd, int perturb, double *const *outs, void *stream);
 
+/* Accumulate and evaluate at the same particles in one pipeline:
+ * eof.compute_coefficients followed by eof.compute_forces on one snapshot
+ * (eof.py:1158-1317).  Writes cos_out/sin_out ((mmax+1) x norder) and outs =
+ * p0 p fr fp fz R (6 device arrays of n) for m1 <= m <= m2.  Per-particle
+ * set-up is computed once and particles are counting-sorted by table cell
+ * inside the workspace (size from xt_cyl_accumulate_eval_workspace).
+ * nan_to_origin != 0 places particles with a NaN coordinate at the origin
+ * for both accumulation and evaluation (eof.py:1189-1204).  mmax <= 8,
+ * norder <= 24. */
+size_t xt_cyl_accumulate_eval_workspace(void *handle, long long n, int precision);
+int xt_cyl_accumulate_eval(void *handle, const double *x, const double *y, const double *z, const double *m,
+                           long long n, int precision, int m1, int m2, int nan_to_origin, double *cos_out,
+                           double *sin_out, double *const *outs, void *workspace, size_t workspace_bytes,
+                           void *stream);
+
+/* Stage timing (diagnostics, no counterpart in the reference): with
+ * xt_timing_enable(1), xt_cyl_accumulate_eval records CUDA events on its
+ * stream between its stages; xt_timing_read waits for the last one and writes
+ * up to `max` stage durations in ms (binrec, scan, scatter, deposit,
+ * contract, field, eval), returning how many it wrote (< 0 on error). */
+int xt_timing_enable(int on);
+int xt_timing_read(double *ms_out, int max);
+
 /* --------------------------------------------------------------- fields + orbits */
 /* potential.Fields.return_forces_cart (potential.py:445-497) at n points:
  * outs = fxdisk fxhalo fydisk fyhalo fzdisk fzhalo diskp halop+halop0.

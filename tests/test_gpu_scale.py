@@ -141,3 +141,45 @@ def test_accumulate_reproducible(disc):
     b = eof.compute_coefficients(P, path, verbose=0)
     for mm in range(t["mmax"] + 1):
         assert rel(a.cos[mm], b.cos[mm]) <= 1e-13
+
+
+def test_disc_fused_matches_separate_calls(disc):
+    """Fused accumulate + evaluate (sorted by cell) == separate calls, both precisions."""
+    from exptool_gb300.basis import eof
+    path, (x, y, z, m), t = disc
+    P = PD(x, y, z, m)
+    E = eof.compute_coefficients(P, path, verbose=0)
+    ref = eof.compute_forces(P, E, verbose=0)
+    E2, got = eof.compute_coefficients_and_forces(P, path, verbose=0)
+    for mm in range(t["mmax"] + 1):
+        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-12
+        if mm:
+            assert rel(E2.sin[mm], E.sin[mm]) <= 1e-12
+    for k in range(6):
+        assert rel(got[k], ref[k]) <= 1e-10, k
+    E3, got32 = eof.compute_coefficients_and_forces(P, path, verbose=0, precision="f32")
+    assert rel(E3.cos[0], E.cos[0]) < 1e-5
+    F = np.stack([ref[2], ref[4]])
+    G = np.stack([got32[2], got32[4]])
+    assert np.median(np.linalg.norm(G - F, axis=0) / np.linalg.norm(F, axis=0)) < 1e-5
+    # m range
+    _, g12 = eof.compute_coefficients_and_forces(P, path, verbose=0, m1=1, m2=2)
+    r12 = eof.compute_forces(P, E, verbose=0, m1=1, m2=2)
+    for k in range(6):
+        assert rel(g12[k], r12[k]) <= 1e-10, k
+
+
+def test_disc_fused_nan_particles(disc):
+    """NaN coordinates are placed at the origin by both accumulation paths."""
+    from exptool_gb300.basis import eof
+    path, (x, y, z, m), t = disc
+    n = 50000
+    x, y, z, m = x[:n].copy(), y[:n].copy(), z[:n].copy(), m[:n]
+    x[::997] = np.nan
+    z[5::1009] = np.nan
+    P = PD(x, y, z, m)
+    E = eof.compute_coefficients(P, path, verbose=0)
+    E2, _ = eof.compute_coefficients_and_forces(P, path, verbose=0)
+    assert np.all(np.isfinite(E2.cos))
+    for mm in range(t["mmax"] + 1):
+        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-12
