@@ -71,6 +71,108 @@ def sl_table_paths():
     return cache, model
 
 
+def sl6_table_paths():
+    """Hernquist SL basis lmax 6, nmax 20, 2000-point log-r table (batched workload)."""
+    d = cache_dir()
+    cache = os.path.join(d, "SLGridSph.cache.hernquist_l6n20")
+    model = os.path.join(d, "SLGridSph.model.hernquist_l6n20")
+    if not (os.path.exists(cache) and os.path.exists(model)):
+        from exptool_gb300.tables.sl_solver import make_hernquist_sl
+        make_hernquist_sl(d, lmax=6, nmax=20, numr=2000, rmin=1e-3, rmax=100.0, cmap=2, scale=1.0,
+                          tag="hernquist_l6n20")
+    return cache, model
+
+
+def batched_snapshots(nsnap=256):
+    """Hernquist snapshots (a=1, r<100) with log-uniform counts in [1e4, 4e6)
+    from default_rng(3); snapshot i drawn on the GPU by a torch generator seeded
+    1000+i in the order u, cos(theta), phi.  Returns (xyzm float32 (N,4), offsets)."""
+    import torch
+    rng = np.random.default_rng(3)
+    counts = np.round(np.exp(rng.uniform(np.log(1e4), np.log(4e6), nsnap))).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    xyzm = torch.empty((int(offs[-1]), 4), dtype=torch.float32, device="cuda")
+    umax = (100.0 / 101.0) ** 2
+    for i in range(nsnap):
+        n = int(counts[i])
+        g = torch.Generator(device="cuda")
+        g.manual_seed(1000 + i)
+        u = torch.rand(n, generator=g, device="cuda", dtype=torch.float64) * umax
+        su = torch.sqrt(u)
+        r = su / (1.0 - su)
+        c = torch.rand(n, generator=g, device="cuda", dtype=torch.float64) * 2.0 - 1.0
+        ph = torch.rand(n, generator=g, device="cuda", dtype=torch.float64) * (2.0 * np.pi)
+        st = torch.sqrt(torch.clamp(1.0 - c * c, min=0.0))
+        blk = xyzm[int(offs[i]):int(offs[i + 1])]
+        blk[:, 0] = (r * st * torch.cos(ph)).float()
+        blk[:, 1] = (r * st * torch.sin(ph)).float()
+        blk[:, 2] = (r * c).float()
+        blk[:, 3] = 1.0 / n
+    return xyzm, offs
+
+
+def batched_extra(K=5):
+    """256 snapshots, SL lmax 6 / nmax 20: one persistent mixed-precision launch
+    vs the FP64 path snapshot by snapshot; per-snapshot error vs FP64."""
+    import torch
+    from exptool_gb300 import autotune as at
+    from exptool_gb300.basis import spheresl
+    cache, model = sl6_table_paths()
+    table = spheresl.table_from_files(cache, model)
+    xyzm, offs = batched_snapshots()
+    ntot = int(offs[-1])
+    cfg, tune_ms = at.sph_batched_config(table, xyzm, offs)
+    need = table._lib.xt_sph_batched_workspace(table.handle, len(offs) - 1, ntot, int(cfg["chunk"]))
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+    out = table.accumulate_batched(xyzm, offs, chunk=cfg["chunk"], threads=cfg["threads"], workspace=ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        table.accumulate_batched(xyzm, offs, chunk=cfg["chunk"], threads=cfg["threads"], workspace=ws)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    # FP64 path snapshot by snapshot on the same (FP32-rounded) particles
+    sws = torch.empty(table._lib.xt_sph_accumulate_workspace(table.handle), dtype=torch.uint8, device="cuda")
+    errs = []
+    f64_ms = 0.0
+    for i in range(len(offs) - 1):
+        blk = xyzm[int(offs[i]):int(offs[i + 1])].double()
+        x, y, z, m = (blk[:, k].contiguous() for k in range(4))
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        ref = table.accumulate(x, y, z, m, workspace=sws)
+        a1.record()
+        torch.cuda.synchronize()
+        f64_ms += a0.elapsed_time(a1)
+        a, b = out[i].cpu().numpy(), ref.cpu().numpy()
+        errs.append((float(np.max(np.abs(a - b)) / np.max(np.abs(b))), _block_err(a, b, table.lmax)))
+    errs = np.array(errs)
+    return {"workload": "256 Hernquist snapshots (counts log-uniform in [1e4,4e6), total %d), SL lmax=6 nmax=20 "
+                        "numr=2000, one persistent launch (FP32 per particle + shared-memory grids, FP64 "
+                        "cross-item sums and contraction)" % ntot,
+            "ms": ms, "particles_per_s": ntot / (ms * 1e-3), "autotuned": cfg,
+            "autotune_candidates_ms": {k: round(v, 3) for k, v in tune_ms.items()},
+            "fp64_per_snapshot_ms": f64_ms, "fp64_particles_per_s": ntot / (f64_ms * 1e-3),
+            "speedup_vs_fp64": f64_ms / ms,
+            "err_vs_fp64_per_snapshot": {
+                "normwise_median": float(np.median(errs[:, 0])), "normwise_max": float(np.max(errs[:, 0])),
+                "per_l_block_median": float(np.median(errs[:, 1])), "per_l_block_max": float(np.max(errs[:, 1])),
+                "metric": "normwise: max|dc|/max|c| over all rows; per_l_block: max over l of the same within "
+                          "each l block"}}
+
+
+def _block_err(a, b, lmax):
+    worst, row = 0.0, 0
+    for l in range(lmax + 1):
+        blk = slice(row, row + 2 * l + 1)
+        s_ = np.max(np.abs(b[blk]))
+        worst = max(worst, float(np.max(np.abs(a[blk] - b[blk])) / s_) if s_ > 0 else 0.0)
+        row += 2 * l + 1
+    return worst
+
+
 def disc_particles(n=N1, seed=1):
     from exptool_gb300.tables.samplers import disc_sample
     return disc_sample(n, seed)
@@ -289,6 +391,7 @@ def gpu_arm(args, rank, world):
     sl_ms = e0.elapsed_time(e1) / K
 
     orbits = orbit_extra(path, c64, s64, cache, model, st, hxd, hyd, hzd, hmd, args)
+    batched = batched_extra()
 
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
@@ -357,6 +460,7 @@ def gpu_arm(args, rank, world):
         "spherical_halo": {"workload": "Hernquist SL lmax=4 nmax=10 numr=2000 cmap=2, N=1e5, accumulate+eval",
                            "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
         "orbits": orbits,
+        "batched_spherical": batched,
         "clocks": clocks,
     }
     return line
@@ -515,6 +619,21 @@ def profile_run(args):
     return 0
 
 
+def profile_batched(args):
+    """Batched spherical accumulation on the first 16 snapshots: warm-up calls,
+    then one call, with a fixed launch shape (chunk 65536, 512 threads)."""
+    import torch
+    from exptool_gb300.basis import spheresl
+    cache, model = sl6_table_paths()
+    table = spheresl.table_from_files(cache, model)
+    xyzm, offs = batched_snapshots(16)
+    for _ in range(args.warmup + 1):
+        table.accumulate_batched(xyzm, offs, chunk=65536, threads=512)
+    torch.cuda.synchronize()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -522,12 +641,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="run the batched spherical accumulation on the first 16 snapshots (warm-up + one call) "
+                         "and exit (for ncu captures)")
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
                          "(a short, fixed launch sequence for ncu captures)")
     args = ap.parse_args()
     if args.profile:
         return profile_run(args)
+    if args.profile_batched:
+        return profile_batched(args)
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -46,6 +46,8 @@ _SIGS = {
     "xt_sph_prepare": (c_int, [c_vp, c_vp, c_dbl, c_int, c_int, c_int, c_vp, c_sz, c_vp]),
     "xt_sph_eval_points": (c_int, [c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int, c_int,
                                    c_int, c_int, c_dpp, c_vp]),
+    "xt_sph_batched_workspace": (c_sz, [c_vp, c_int, c_ll, c_int]),
+    "xt_sph_accumulate_batched": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_sz, c_vp]),
     "xt_cyl_table_create": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl,
                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "xt_cyl_table_destroy": (c_int, [c_vp]),

@@ -118,6 +118,43 @@ def compute_coefficients(PSPInput, sph_file, mod_file, verbose=1, no_odd=False, 
     return out
 
 
+def compute_coefficients_batched(snapshots, sph_file, mod_file, no_odd=False, autotune=True, chunk=None,
+                                 threads=None):
+    """Coefficients of many snapshots in one persistent GPU launch (the
+    series spheresl.compute_coefficients would produce one call at a time).
+
+    ``snapshots``: a list of particle containers (holder-like or ``.data``),
+    or a pair (xyzm, offsets) with xyzm an (N, 4) float32 array / CUDA tensor
+    of x y z m and offsets the nsnap+1 snapshot boundaries.  Mixed precision:
+    FP32 per-particle arithmetic and shared-memory accumulation, FP64 sums
+    across work items and FP64 contraction.  Returns an array of shape
+    (nsnap, (lmax+1)^2, nmax)."""
+    table = table_from_files(sph_file, mod_file)
+    if isinstance(snapshots, tuple) and len(snapshots) == 2:
+        xyzm, offsets = snapshots
+        offsets = np.asarray(offsets, dtype=np.int64)
+        if not isinstance(xyzm, torch.Tensor):
+            xyzm = torch.from_numpy(np.ascontiguousarray(np.asarray(xyzm, dtype=np.float32)))
+        xyzm = xyzm.to(dev.device(), dtype=torch.float32).contiguous()
+    else:
+        parts, counts = [], [0]
+        for P in snapshots:
+            x, y, z, m = positions(P)
+            parts.append(np.stack([x, y, z, m], axis=1).astype(np.float32))
+            counts.append(x.size)
+        offsets = np.cumsum(counts).astype(np.int64)
+        xyzm = torch.from_numpy(np.concatenate(parts, axis=0)).to(dev.device()).contiguous()
+    if chunk is None or threads is None:
+        if autotune:
+            from .. import autotune as at
+            cfg, _ = at.sph_batched_config(table, xyzm, offsets)
+        else:
+            cfg = {"chunk": 262144, "threads": 512}
+        chunk = cfg["chunk"] if chunk is None else chunk
+        threads = cfg["threads"] if threads is None else threads
+    return dev.to_host(table.accumulate_batched(xyzm, offsets, no_odd=no_odd, chunk=chunk, threads=threads))
+
+
 # ---------------------------------------------------------------- evaluation
 def all_eval_particles(Particles, expcoef, sph_file, mod_file, verbose=0, L1=-1000, L2=1000, NO_ODD=False,
                        precision="f64"):

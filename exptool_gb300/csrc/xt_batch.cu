@@ -1,0 +1,248 @@
+// Batched spherical accumulation over many snapshots in one persistent launch.
+//
+// Workload: spheresl.compute_coefficients (spheresl.py:439-475) applied to a
+// time series of snapshots, the reference's natural caller for coefficient
+// series.  Particles of all snapshots are one FP32 xyzm stream (float4 per
+// particle); snapshot s owns particles [offsets[s], offsets[s+1]).
+//
+// Each particle's contribution -4 pi m Y_lm(theta, phi) plerp x {x1, x2} goes
+// to the two radial nodes it interpolates between (the reorganisation of the
+// single-snapshot FP64 kernel, xt_sph.cu).  Here the node grid of a block of
+// coefficient rows lives in shared memory: a CTA takes a work item (snapshot,
+// particle chunk, row part) from a global counter, deposits the chunk with
+// FP32 shared-memory atomics, then adds its grid into the snapshot's FP64 grid
+// in global memory (FP64 atomics, one per non-zero node value).  A batched
+// FP64 kernel contracts every snapshot grid with the radial tables.  No CTA
+// ever waits on another; the loop ends when the counter passes the last item.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "xt_internal.cuh"
+#include "xt_launch.cuh"
+
+namespace xt {
+
+struct BatchItem {
+  int snap;
+  int part;           // radial node part
+  long long begin, end;
+};
+
+constexpr float FOUR_PI_F = 12.566370614359172f;
+
+// Work items split the radial nodes: part k owns particles whose lower
+// interpolation node i lies in [ilo_k, ihi_k) and keeps a shared grid of all
+// rows over nodes [ilo_k, ihi_k] (node ihi_k is shared with the next part;
+// both parts add their share of it to the FP64 grid).  Particles outside the
+// part's range are skipped after the radial mapping, so Legendre functions,
+// trigonometry and deposits are computed once per particle.
+template <int LCAP>
+__global__ void k_sph_batched(SphTab<float> T, const float4* __restrict__ xyzm, const BatchItem* __restrict__ items,
+                              int nitems, int* __restrict__ counter, const int* __restrict__ part_nodes, int no_odd,
+                              double* __restrict__ G) {
+  extern __shared__ float sg[];
+  __shared__ int s_item;
+  constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
+  const int numr = T.numr;
+  const int nrow = (T.lmax + 1) * (T.lmax + 1);
+  const int lstride = T.lmax + 1;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= nitems) break;
+    const BatchItem I = items[it];
+    const int ilo = part_nodes[I.part], ihi = part_nodes[I.part + 1];
+    const int span = ihi - ilo + 1;               // nodes ilo..ihi
+    const int ncell = nrow * span;
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) sg[k] = 0.f;
+    __syncthreads();
+    long long p = I.begin + threadIdx.x;
+    float4 q = (p < I.end) ? xyzm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (; p < I.end; p += blockDim.x) {
+      const long long pn = p + blockDim.x;
+      const float4 qn = (pn < I.end) ? xyzm[pn] : q;    // next particle in flight
+      float r = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
+      if (!(r >= 1.0e-10f)) r = 1.0e-10f;
+      const SphBins<float> B = sph_bins(T, r, false, false);
+      if (B.i >= ilo && B.i < ihi) {
+        const float costh = q.z / r;
+        float c1, s1;
+        unit_phi(q.x, q.y, c1, s1);
+        float P[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) P[k] = 0.f;
+        legendre<float, LCAP>(costh, T.lmax, P);
+        float cm[LCAP + 1], sm[LCAP + 1];
+        multiples<float, LCAP>(c1, s1, T.lmax, cm, sm);
+        const float base = -FOUR_PI_F * q.w;
+        const float w0 = B.lw0 * base, w1 = B.lw1 * base;
+        float* g0 = sg + (B.i - ilo);
+#pragma unroll
+        for (int l = 0; l <= LCAP; ++l) {
+          if (l > T.lmax) break;
+          if (no_odd && (l & 1)) continue;
+          const int loff = l * l;
+#pragma unroll
+          for (int m = 0; m <= l; ++m) {
+            const float a = T.fact[l * lstride + m] * P[tri(l, m)];
+            const int rc = (m == 0) ? loff : loff + 2 * m - 1;
+            const float v = (m == 0) ? a : a * cm[m];
+            atomicAdd(g0 + rc * span, v * w0);
+            atomicAdd(g0 + rc * span + 1, v * w1);
+            if (m > 0) {
+              const float u = a * sm[m];
+              atomicAdd(g0 + (rc + 1) * span, u * w0);
+              atomicAdd(g0 + (rc + 1) * span + 1, u * w1);
+            }
+          }
+        }
+      }
+      q = qn;
+    }
+    __syncthreads();
+    double* gs = G + (size_t)I.snap * nrow * numr + ilo;
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+      const float v = sg[k];
+      if (v != 0.f) {
+        const int row = k / span, node = k - row * span;
+        atomicAdd(gs + (size_t)row * numr + node, (double)v);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// expcoef[s, row, n] = sum_i efp[l, n, i] * G[s, row, i]: one warp per output.
+__global__ void __launch_bounds__(256) k_sph_contract_batched(const double* __restrict__ efp,
+                                                              const double* __restrict__ G, int nsnap, int lmax,
+                                                              int nmax, int numr, double* __restrict__ out) {
+  const int nrow = (lmax + 1) * (lmax + 1);
+  const long long nout = (long long)nsnap * nrow * nmax;
+  const int lane = threadIdx.x & 31;
+  for (long long o = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; o < nout;
+       o += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const int n = (int)(o % nmax);
+    const long long sr = o / nmax;
+    const int row = (int)(sr % nrow);
+    int l = 0;
+    while ((l + 1) * (l + 1) <= row) ++l;
+    const double* e = efp + ((size_t)l * nmax + n) * numr;
+    const double* g = G + (size_t)sr * numr;
+    double acc = 0.0;
+    for (int i = lane; i < numr; i += 32) acc += e[i] * g[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) out[o] = acc;
+  }
+}
+
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace xt
+
+using namespace xt;
+
+extern "C" {
+
+size_t xt_sph_batched_workspace(void* handle, int nsnap, long long n_total, int chunk) {
+  SphTab<double> d;
+  if (!sph_tabs(handle, &d, nullptr) || nsnap <= 0 || chunk <= 0) return 0;
+  const size_t nrow = (size_t)(d.lmax + 1) * (d.lmax + 1);
+  const size_t maxitems = (size_t)(n_total / chunk + nsnap + 1) * 8;
+  return al256((size_t)nsnap * nrow * d.numr * sizeof(double)) + al256(maxitems * sizeof(BatchItem)) +
+         al256(64 * sizeof(int)) + al256(sizeof(int));
+}
+
+int xt_sph_accumulate_batched(void* handle, const float* xyzm, const long long* offsets_host, int nsnap,
+                              int no_odd, int chunk, int threads, double* expcoef_out, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+  SphTab<double> d;
+  SphTab<float> f;
+  XT_REQUIRE(sph_tabs(handle, &d, &f), "NULL table handle");
+  XT_REQUIRE(nsnap > 0 && offsets_host && expcoef_out, "need nsnap > 0, host offsets and an output");
+  XT_REQUIRE(chunk >= 256, "chunk must be >= 256 particles");
+  XT_REQUIRE(threads == 128 || threads == 256 || threads == 512 || threads == 768 || threads == 1024,
+             "threads must be 128, 256, 512, 768 or 1024");
+  XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
+  const long long n_total = offsets_host[nsnap] - offsets_host[0];
+  XT_REQUIRE(n_total >= 0 && offsets_host[0] == 0, "offsets must start at 0 and be non-decreasing");
+  for (int s = 0; s < nsnap; ++s) XT_REQUIRE(offsets_host[s + 1] >= offsets_host[s], "offsets must be non-decreasing");
+  XT_REQUIRE(n_total == 0 || xyzm, "NULL particle stream");
+  XT_REQUIRE(((uintptr_t)xyzm & 15) == 0, "xyzm must be 16-byte aligned (float4 per particle)");
+  const size_t need = xt_sph_batched_workspace(handle, nsnap, n_total, chunk);
+  if (!workspace || workspace_bytes < need) {
+    set_error("workspace of %zu bytes needed, %zu given", need, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  // node parts: each part's shared grid (all rows x its nodes + 1) must fit
+  // in 200 KB of shared memory
+  const int nrow = (d.lmax + 1) * (d.lmax + 1);
+  const size_t smem_cap = 200 * 1024;
+  const int nodes_per_part = (int)(smem_cap / ((size_t)nrow * sizeof(float))) - 1;
+  XT_REQUIRE(nodes_per_part >= 8, "lmax %d too large for the shared-memory grid", d.lmax);
+  const int nint = d.numr - 1;                          // interpolation intervals i = 0..numr-2
+  const int nparts = (nint + nodes_per_part - 1) / nodes_per_part;
+  XT_REQUIRE(nparts <= 63, "too many node parts");
+  std::vector<int> part_rows(nparts + 1);               // interval bounds ilo_k
+  for (int k = 0; k <= nparts; ++k) part_rows[k] = (int)((long long)nint * k / nparts);
+  int max_span = 0;
+  for (int k = 0; k < nparts; ++k) max_span = std::max(max_span, part_rows[k + 1] - part_rows[k] + 1);
+  const int max_rows = nrow;
+  std::vector<BatchItem> items;
+  for (int s = 0; s < nsnap; ++s)
+    for (long long b = offsets_host[s]; b < offsets_host[s + 1]; b += chunk)
+      for (int k = 0; k < nparts; ++k)
+        items.push_back(BatchItem{s, k, b, std::min(b + (long long)chunk, offsets_host[s + 1])});
+  const size_t maxitems = (size_t)(n_total / chunk + nsnap + 1) * 8;
+  XT_REQUIRE(items.size() <= maxitems, "internal: work item table overflow");
+  cudaStream_t st = as_stream(stream);
+  char* ws = static_cast<char*>(workspace);
+  double* G = reinterpret_cast<double*>(ws);
+  size_t o = al256((size_t)nsnap * nrow * d.numr * sizeof(double));
+  BatchItem* ditems = reinterpret_cast<BatchItem*>(ws + o);
+  o += al256(maxitems * sizeof(BatchItem));
+  int* dparts = reinterpret_cast<int*>(ws + o);
+  o += al256(64 * sizeof(int));
+  int* counter = reinterpret_cast<int*>(ws + o);
+  XT_CUDA(cudaMemsetAsync(G, 0, (size_t)nsnap * nrow * d.numr * sizeof(double), st));
+  XT_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+  if (!items.empty()) {
+    XT_CUDA(cudaMemcpyAsync(ditems, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, st));
+    XT_CUDA(cudaMemcpyAsync(dparts, part_rows.data(), part_rows.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    const size_t smem = (size_t)max_rows * max_span * sizeof(float);
+    int dev = 0, nsm = 0;
+    XT_CUDA(cudaGetDevice(&dev));
+    XT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int rc = with_lcap(d.lmax, [&](auto lc) -> int {
+      constexpr int LC = decltype(lc)::value;
+      {
+        XT_CUDA(cudaFuncSetAttribute(k_sph_batched<LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        XT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sph_batched<LC>, threads, smem));
+        if (per_sm < 1) {
+          set_error("k_sph_batched cannot run %d threads with %zu bytes of shared memory", threads, smem);
+          return XT_ERR_ARG;
+        }
+        const int grid = nsm * per_sm;
+        k_sph_batched<LC><<<grid, threads, smem, st>>>(f, reinterpret_cast<const float4*>(xyzm), ditems,
+                                                      (int)items.size(), counter, dparts, no_odd, G);
+        return XT_OK;
+      }
+    });
+    if (rc) return rc;
+    XT_CHECK_LAUNCH("k_sph_batched");
+  }
+  const long long nout = (long long)nsnap * nrow * d.nmax;
+  const int cgrid = (int)std::min<long long>((nout * 32 + 255) / 256, 152LL * 64);
+  const double* efp = nullptr;
+  XT_REQUIRE(sph_efp(handle, &efp), "NULL table handle");
+  k_sph_contract_batched<<<cgrid, 256, 0, st>>>(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out);
+  XT_CHECK_LAUNCH("k_sph_contract_batched");
+  return XT_OK;
+}
+
+}  // extern "C"

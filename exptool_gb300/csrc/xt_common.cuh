@@ -11,10 +11,6 @@
 
 namespace xt {
 
-// Loops over l, m are fully unrolled (register-resident Legendre tables) for
-// lmax <= 8; the lmax <= 32 fallback keeps them rolled to bound code size.
-template <int L>
-constexpr int unr_v = (L <= 8) ? 64 : 1;
 
 // ------------------------------------------------------------------ errors
 void set_error(const char* fmt, ...);

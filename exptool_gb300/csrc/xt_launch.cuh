@@ -38,14 +38,14 @@ template <typename R, int LC>
 void launch_leapfrog(const SphTab<R>& ST, const R* GH, const CylTab<R>& CT, const R* F, const FieldOpts& fo,
                      const OrbitArgs& A, int grid, int block, cudaStream_t st);
 
-// Compile-time lmax capacity: unrolled register-resident variants for
-// lmax <= 4 and <= 6, a rolled variant up to 32.
+// Compile-time lmax capacity: fully unrolled, register-resident Legendre and
+// trigonometric tables for lmax <= 4, 6 and 8.
 template <typename F>
 inline int with_lcap(int lmax, F&& f) {
   if (lmax <= 4) return f(std::integral_constant<int, 4>{});
   if (lmax <= 6) return f(std::integral_constant<int, 6>{});
-  if (lmax <= 32) return f(std::integral_constant<int, 32>{});
-  set_error("lmax %d exceeds the supported maximum 32", lmax);
+  if (lmax <= 8) return f(std::integral_constant<int, 8>{});
+  set_error("lmax %d exceeds the supported maximum 8", lmax);
   return XT_ERR_ARG;
 }
 

@@ -11,6 +11,6 @@ namespace xt {
                                          const FieldOpts&, const OrbitArgs&, int, int, cudaStream_t);
 XT_INST(4)
 XT_INST(6)
-XT_INST(32)
+XT_INST(8)
 #undef XT_INST
 }  // namespace xt

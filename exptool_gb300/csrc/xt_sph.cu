@@ -59,17 +59,18 @@ struct SphHandle {
   int lmax, nmax, numr, cmap;
   double rmin, rmax, scale;
   // FP64 arrays
-  double *xi = nullptr, *p0 = nullptr, *d0 = nullptr, *fact = nullptr;
+  double *xi = nullptr, *p0 = nullptr, *d0 = nullptr, *fact = nullptr, *rnode = nullptr;
   double *efp = nullptr, *efd = nullptr;   // [(L+1)][K][numr]
   // FP32 copies for the mixed path
-  float *xi_f = nullptr, *p0_f = nullptr, *d0_f = nullptr, *fact_f = nullptr;
+  float *xi_f = nullptr, *p0_f = nullptr, *d0_f = nullptr, *fact_f = nullptr, *rnode_f = nullptr;
   SphTab<double> tab_d;
   SphTab<float> tab_f;
 };
 
 static void free_handle(SphHandle* h) {
   if (!h) return;
-  void* ptrs[] = {h->xi, h->p0, h->d0, h->fact, h->efp, h->efd, h->xi_f, h->p0_f, h->d0_f, h->fact_f};
+  void* ptrs[] = {h->xi, h->p0, h->d0, h->fact, h->efp, h->efd, h->xi_f, h->p0_f, h->d0_f, h->fact_f,
+                  h->rnode, h->rnode_f};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -139,6 +140,13 @@ __global__ void __launch_bounds__(256) k_sph_field(const double* __restrict__ ef
   }
 }
 
+bool sph_efp(void* handle, const double** efp) {
+  SphHandle* h = static_cast<SphHandle*>(handle);
+  if (!h) return false;
+  *efp = h->efp;
+  return true;
+}
+
 bool sph_tabs(void* handle, SphTab<double>* d, SphTab<float>* f) {
   SphHandle* h = static_cast<SphHandle*>(handle);
   if (!h) return false;
@@ -198,7 +206,7 @@ int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, dou
                         void** handle) {
   XT_REQUIRE(handle, "handle out-pointer is NULL");
   *handle = nullptr;
-  XT_REQUIRE(lmax >= 0 && lmax <= 32, "lmax must be in [0, 32], got %d", lmax);
+  XT_REQUIRE(lmax >= 0 && lmax <= 8, "lmax must be in [0, 8], got %d", lmax);
   XT_REQUIRE(nmax >= 1 && numr >= 3, "need nmax >= 1 and numr >= 3 (got %d, %d)", nmax, numr);
   XT_REQUIRE(cmap >= 0 && cmap <= 2, "cmap must be 0, 1 or 2");
   XT_REQUIRE(xi && p0 && d0 && ev && ef, "NULL table array");
@@ -234,6 +242,19 @@ int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, dou
     free_handle(h);
     return rc;
   }
+  // node radii xi_to_r(xi) (compatibility.py:54-62)
+  std::vector<double> rn(numr);
+  for (int i = 0; i < numr; ++i)
+    rn[i] = (cmap == 1) ? (1.0 + xi[i]) / (1.0 - xi[i]) * scale : (cmap == 2 ? exp(xi[i]) : xi[i]);
+  if ((rc = upload(&h->rnode, rn.data(), numr))) {
+    free_handle(h);
+    return rc;
+  }
+  auto rnf = to_f32(rn.data(), numr);
+  if ((rc = upload(&h->rnode_f, rnf.data(), numr))) {
+    free_handle(h);
+    return rc;
+  }
   auto xf = to_f32(xi, numr), pf = to_f32(p0, numr), df = to_f32(d0, numr), ff = to_f32(fact.data(), fact.size());
   if ((rc = upload(&h->xi_f, xf.data(), numr)) || (rc = upload(&h->p0_f, pf.data(), numr)) ||
       (rc = upload(&h->d0_f, df.data(), numr)) || (rc = upload(&h->fact_f, ff.data(), ff.size()))) {
@@ -243,9 +264,10 @@ int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, dou
   const double lo = (cmap == 2) ? log(rmin) : 0.0, hi = (cmap == 2) ? log(rmax) : 0.0;
   const double dxi = xi[1] - xi[0];
   h->tab_d = SphTab<double>{lmax, nmax, numr, cmap, scale, xi0, dxi, lo, hi, 1.0 / scale, 1.0 / dxi,
-                            h->xi, h->p0, h->d0, h->fact};
+                            h->xi, h->p0, h->d0, h->fact, h->rnode};
   h->tab_f = SphTab<float>{lmax, nmax, numr, cmap, (float)scale, (float)xi0, (float)dxi, (float)lo, (float)hi,
-                           (float)(1.0 / scale), (float)(1.0 / dxi), h->xi_f, h->p0_f, h->d0_f, h->fact_f};
+                           (float)(1.0 / scale), (float)(1.0 / dxi), h->xi_f, h->p0_f, h->d0_f, h->fact_f,
+                           h->rnode_f};
   *handle = h;
   return XT_OK;
 }

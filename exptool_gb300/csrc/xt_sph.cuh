@@ -4,6 +4,8 @@
 // :987-1362, radial functions :106-335, Legendre :664-770).
 #pragma once
 
+#include <type_traits>
+
 #include "xt_common.cuh"
 
 namespace xt {
@@ -19,6 +21,7 @@ struct SphTab {
   const R* p0;                 // [numr]  model potential on the grid
   const R* d0;                 // [numr]  4 pi rho0 on the grid
   const R* fact;               // [(lmax+1)^2] factorial_return, index l*(lmax+1)+m
+  const R* rnode;              // [numr] node radii xi_to_r(xi) (FP32 path: accurate in-cell offsets)
 };
 
 __host__ __device__ inline int sph_nrow(int lmax) { return (lmax + 1) * (lmax + 1); }
@@ -57,6 +60,21 @@ __device__ __forceinline__ SphBins<R> sph_bins(const SphTab<R>& T, R r, bool nee
   int i = (int)fi;
   R x1 = (T.xi[i + 1] - x) * T.inv_dxi;
   R x2 = (x - T.xi[i]) * T.inv_dxi;
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32: x carries an absolute rounding of ~ulp(x), a sizeable fraction of
+    // a table cell; take the in-cell offset from the radius ratio instead,
+    // which FP32 resolves to its relative precision.
+    const bool clamped = (T.cmap == 2) ? (x == T.lo || x == T.hi) : (T.cmap == 1 && (x == R(-1) || x >= R(1) - R(2.0e-8)));
+    if (!clamped && r > R(0)) {
+      const R ri = T.rnode[i];
+      R dx;
+      if (T.cmap == 2) dx = log(r / ri);
+      else if (T.cmap == 1) dx = R(2) * (r - ri) * T.inv_scale / ((r * T.inv_scale + R(1)) * (ri * T.inv_scale + R(1)));
+      else dx = r - ri;
+      x2 = dx * T.inv_dxi;
+      x1 = R(1) - x2;
+    }
+  }
   SphBins<R> B;
   int j = i < 1 ? 1 : i;
   B.i = i;
@@ -100,7 +118,7 @@ __device__ __forceinline__ void legendre(R x, int lmax, R* P) {
   if (lmax > 0) {
     R somx2 = sqrt((R(1) - x) * (R(1) + x));
     R fact = R(1);
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int m = 1; m <= LCAP; ++m) {
       if (m > lmax) break;
       pll *= -fact * somx2;
@@ -108,13 +126,13 @@ __device__ __forceinline__ void legendre(R x, int lmax, R* P) {
       fact += R(2);
     }
   }
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int m = 0; m < LCAP; ++m) {
     if (m >= lmax) break;
     R pl2 = P[tri(m, m)];
     R pl1 = x * R(2 * m + 1) * pl2;
     P[tri(m + 1, m)] = pl1;
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int l = m + 2; l <= LCAP; ++l) {
       if (l > lmax) break;
       R v = (x * R(2 * l - 1) * pl1 - R(l + m - 1) * pl2) * (R(1) / R(l - m));
@@ -123,7 +141,7 @@ __device__ __forceinline__ void legendre(R x, int lmax, R* P) {
       pl1 = v;
     }
   }
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int k = 0; k < (LCAP + 1) * (LCAP + 2) / 2; ++k)
     if (!finite(P[k])) P[k] = R(0);
 }
@@ -136,14 +154,14 @@ __device__ __forceinline__ void dlegendre(R x, int lmax, const R* P, R* dP) {
   if (R(1) - fabs(x) < MINEPS) x = (x > R(0)) ? (R(1) - MINEPS) : -(R(1) - MINEPS);
   R somx2 = R(1) / (x * x - R(1));
   dP[0] = R(0);
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int l = 1; l <= LCAP; ++l) {
     if (l > lmax) break;
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int m = 0; m < l; ++m) dP[tri(l, m)] = somx2 * (x * R(l) * P[tri(l, m)] - R(l + m) * P[tri(l - 1, m)]);
     dP[tri(l, l)] = somx2 * x * R(l) * P[tri(l, l)];
   }
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int k = 0; k < (LCAP + 1) * (LCAP + 2) / 2; ++k)
     if (!finite(dP[k])) dP[k] = R(0);
 }
@@ -158,7 +176,7 @@ __device__ __forceinline__ void multiples(R c1, R s1, int kmax, R* c, R* s) {
     c[1] = c1;
     s[1] = s1;
   }
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int k = 2; k <= LCAP; ++k) {
     if (k > kmax) break;
     c[k] = R(2) * c1 * c[k - 1] - c[k - 2];
@@ -189,7 +207,7 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
   SphBins<R> B = sph_bins(T, r, true, dens);
   constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
   R P[NT], dP[NT];
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int k = 0; k < NT; ++k) { P[k] = R(0); dP[k] = R(0); }
   legendre<R, LCAP>(costh, lmax, P);
   dlegendre<R, LCAP>(costh, lmax, P, dP);
@@ -218,7 +236,7 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
   R den1 = (o.mode == XT_SPH_ALL_EVAL) ? den0 : R(0);
   R pot1 = R(0), pott = R(0), potp = R(0);
   const int lstride = T.lmax + 1;
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
   for (int l = 1; l <= LCAP; ++l) {
     if (l > lmax) break;
     if (o.mode == XT_SPH_ALL_EVAL_PARTICLES && (l > o.L2 || l < o.L1)) continue;
@@ -233,7 +251,7 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
       potr += fP * frc;
       pott += f * dP[tri(l, 0)] * pot;
     }
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int m = 1; m <= l; ++m) {
       const R f = T.fact[l * lstride + m];
       R potc, frcc, denc, pots, frcs, dens_;

@@ -10,6 +10,6 @@ namespace xt {
                                          int, cudaStream_t);
 XT_INST(4)
 XT_INST(6)
-XT_INST(32)
+XT_INST(8)
 #undef XT_INST
 }  // namespace xt

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256) k_sph_deposit(SphTab<R> T, const double* 
     R c1, s1;
     unit_phi(xx, yy, c1, s1);
     R P[NT];
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int k = 0; k < NT; ++k) P[k] = R(0);
     legendre<R, LCAP>(costh, lmax, P);
     R cm[LCAP + 1], sm[LCAP + 1];
@@ -42,12 +42,12 @@ __global__ void __launch_bounds__(256) k_sph_deposit(SphTab<R> T, const double* 
     w0 *= base;
     w1 *= base;
     const int lstride = lmax + 1;
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
     for (int l = 0; l <= LCAP; ++l) {
       if (l > lmax) break;
       if (no_odd && (l & 1)) continue;
       const int loff = l * l;
-#pragma unroll (unr_v<LCAP>)
+#pragma unroll
       for (int m = 0; m <= l; ++m) {
         const R a = T.fact[l * lstride + m] * P[tri(l, m)];
         if (m == 0) {

@@ -147,6 +147,24 @@ class SphTable:
                                                stream_ptr()), "xt_sph_accumulate")
         return out
 
+    def accumulate_batched(self, xyzm, offsets, no_odd=False, chunk=262144, threads=512, workspace=None):
+        """Coefficients of many snapshots in one persistent launch.  xyzm: (N, 4)
+        float32 CUDA tensor; offsets: host int64 array (nsnap+1).  Returns a
+        (nsnap, (lmax+1)^2, nmax) float64 tensor."""
+        offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        nsnap = offs.size - 1
+        if xyzm.dtype != torch.float32 or xyzm.dim() != 2 or xyzm.shape[1] != 4 or not xyzm.is_contiguous():
+            raise ValueError("xyzm must be a contiguous (N, 4) float32 CUDA tensor")
+        out = torch.empty((nsnap, self.nrow, self.nmax), dtype=torch.float64, device=xyzm.device)
+        need = self._lib.xt_sph_batched_workspace(self.handle, nsnap, int(offs[-1]), int(chunk))
+        ws = workspace if (workspace is not None and workspace.numel() >= need) else \
+            torch.empty(need, dtype=torch.uint8, device=xyzm.device)
+        _lib.check(self._lib.xt_sph_accumulate_batched(self.handle, dptr(xyzm), offs.ctypes.data, nsnap,
+                                                       int(bool(no_odd)), int(chunk), int(threads), dptr(out),
+                                                       dptr(ws), ws.numel(), stream_ptr()),
+                   "xt_sph_accumulate_batched")
+        return out
+
     def prepare(self, expcoef, coef_scale=1.0, lmax_use=-1, nmax_use=-1, precision="f64"):
         pc = precision_code(precision)
         nbytes = self._lib.xt_sph_field_bytes(self.handle, pc)

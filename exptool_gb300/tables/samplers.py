@@ -27,7 +27,7 @@ def hernquist_sample(n: int, seed: int, a: float = 1.0, rmax: float = 100.0,
     x = r * s * np.cos(phi)
     y = r * s * np.sin(phi)
     z = r * c
-    m = np.full(n, mass_total / n)
+    m = np.full(n, mass_total / max(n, 1))
     return x, y, z, m
 
 
@@ -68,4 +68,4 @@ def disc_sample(n: int, seed: int, a: float = 1.0, h: float = 0.1, rmax: float =
                 zmax: float = 2.0, mass_total: float = 1.0):
     """Cartesian x, y, z, m of :func:`disc_cylindrical` with equal masses."""
     R, z, phi = disc_cylindrical(n, seed, a, h, rmax, zmax)
-    return R * np.cos(phi), R * np.sin(phi), z, np.full(n, mass_total / n)
+    return R * np.cos(phi), R * np.sin(phi), z, np.full(n, mass_total / max(n, 1))

@@ -105,6 +105,20 @@ int xt_sph_eval_points(void *handle, const void *field, int precision, int coord
                        const double *b, const double *c, long long n, int mode, int L1, int L2, int no_odd,
                        int lmax_use, int trig_l, double *const *outs, void *stream);
 
+/* Batched accumulation over many snapshots in one persistent launch: the
+ * coefficient time series spheresl.compute_coefficients (spheresl.py:439)
+ * would produce snapshot by snapshot.  xyzm: FP32 x y z m per particle
+ * (float4, 16-byte aligned), snapshot s owning particles
+ * [offsets_host[s], offsets_host[s+1]) (host array of nsnap+1, starting at 0).
+ * FP32 per-particle arithmetic and shared-memory accumulation per work item
+ * (chunk particles x one block of coefficient rows), FP64 cross-item sums and
+ * FP64 contraction.  expcoef_out: nsnap x (lmax+1)^2 x nmax.  threads: CTA
+ * size (128..1024).  lmax <= 8. */
+size_t xt_sph_batched_workspace(void *handle, int nsnap, long long n_total, int chunk);
+int xt_sph_accumulate_batched(void *handle, const float *xyzm, const long long *offsets_host, int nsnap,
+                              int no_odd, int chunk, int threads, double *expcoef_out, void *workspace,
+                              size_t workspace_bytes, void *stream);
+
 /* --------------------------------------------------------------- cylindrical (EOF) */
 /* Upload EOF tables parsed by eof.parse_eof (eof.py:224-313); each table is
  * (mmax+1) x norder x (numx+1) x (numy+1) float64; force tables may be NULL

@@ -69,7 +69,7 @@ def test_noalloc_rejects_tables_beyond_the_static_grid():
     from exptool_gb300 import device as dev
 
     lib = _lib.load()
-    lmax, nmax, numr = 16, 2, 1000            # (lmax+1)^2 * numr = 289000 > 262144
+    lmax, nmax, numr = 8, 2, 4000             # (lmax+1)^2 * numr = 324000 > 262144
     xi = np.log(np.geomspace(1e-3, 1e2, numr))
     big = dev.SphTable(lmax, nmax, numr, 2, 1e-3, 1e2, 1.0, xi, np.ones(numr), np.ones(numr),
                        np.ones((lmax + 1, nmax)), np.ones((lmax + 1, nmax, numr)))
