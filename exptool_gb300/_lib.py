@@ -66,6 +66,20 @@ _SIGS = {
                                  c_dbl, c_ll, c_dpp, c_vp]),
     "xt_leapfrog": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_dpp, c_ll, c_int, c_int,
                             c_int, c_dbl, c_dbl, c_int, c_int, c_vp, c_vp]),
+    "xt_mlp_param_size": (c_int, []),
+    "xt_mlp_create": (c_int, [c_int, c_int, c_vp, ctypes.POINTER(c_vp)]),
+    "xt_mlp_destroy": (c_int, [c_vp]),
+    "xt_mlp_workspace": (c_sz, [c_vp, c_int]),
+    "xt_mlp_get": (c_int, [c_vp, c_int, c_vp]),
+    "xt_mlp_set_params": (c_int, [c_vp, c_vp, c_ll]),
+    "xt_mlp_forward": (c_int, [c_vp, c_vp, c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_mlp_train_step": (c_int, [c_vp, c_vp, c_vp, c_ll, c_int, ctypes.c_float, c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_mlp_labels": (c_int, [c_vp, c_int, c_vp, c_ll, c_dbl, c_vp, c_vp, c_dbl, c_dbl, c_vp, c_vp, c_ll, c_vp]),
+    "xt_learned_prep_bytes": (c_sz, [c_vp, c_int]),
+    "xt_learned_prepare": (c_int, [c_vp, c_vp, c_int, c_vp, c_dbl, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "xt_learned_eval_workspace": (c_sz, [c_vp, c_ll]),
+    "xt_learned_eval": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_int, c_vp, c_ll, c_int,
+                                c_vp, c_vp, c_sz, c_vp]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -118,6 +118,7 @@ class SphTable:
         if arrs[0].size != self.numr or arrs[3].shape != (self.lmax + 1, self.nmax) or \
                 arrs[4].shape != (self.lmax + 1, self.nmax, self.numr):
             raise ValueError("SL table arrays do not match lmax/nmax/numr")
+        self.p0, self.d0, self.ev, self.ef = arrs[1], arrs[2], arrs[3], arrs[4]
         h = _lib.c_vp()
         _lib.check(lib.xt_sph_table_create(self.lmax, self.nmax, self.numr, self.cmap, self.rmin, self.rmax,
                                            self.scale, *[a.ctypes.data for a in arrs], _lib.ctypes.byref(h)),

@@ -200,6 +200,55 @@ int xt_leapfrog(void *sph, const void *sph_field, void *cyl, const void *cyl_fie
                 int step0, int nsteps, int nint, double dt, double rotc, int apse, int ap_max, double *traj,
                 void *stream);
 
+/* ------------------------------------------------------------------ learned radial basis
+ * No counterpart in the reference: a surrogate for the SL radial tables of
+ * spheresl (get_halo_dens_pot_force, spheresl.py:106-160).  One network per
+ * harmonic l (L = lmax + 1 networks) maps t = clamp((ln r - c0) c1, -1, 1)
+ * through 1 -> 128 -> 128 -> 128 -> nout (SiLU) to nout = 2K residuals
+ *   Y[n]   = (phi_nl(r) - s_nl HO_nl(r/a)) / sig[l][n]
+ *   Y[K+n] = (r dphi_nl/dr - s_nl r dHO_nl/dr) / sig[l][K+n]
+ * over the Hernquist-Ostriker functions HO_nl.  BF16 weights (FP32 masters),
+ * FP32 accumulation on the tensor cores.  Parameters per network:
+ * xt_mlp_param_size() floats laid out W1[128] b1[128] W2[128][128] b2[128]
+ * W3[128][128] b3[128] W4[64][128] b4[64] (W[out][in]; rows >= nout zero). */
+int xt_mlp_param_size(void);
+int xt_mlp_create(int L, int nout, const float *init_params, void **handle);
+int xt_mlp_destroy(void *handle);
+/* device scratch of one forward / training step on a batch of B (B % 64 == 0) */
+size_t xt_mlp_workspace(void *handle, int B);
+/* which: 0 parameters, 1 last gradients, 2 Adam first moments, 3 second moments (host copy) */
+int xt_mlp_get(void *handle, int which, float *host_out);
+/* replace the parameters (host array), reset Adam with step counter `step` */
+int xt_mlp_set_params(void *handle, const float *host_params, long long step);
+/* Y[L][B][64] = network outputs at inputs t[B] (device) */
+int xt_mlp_forward(void *handle, const float *t, int B, float *Y, void *workspace, size_t workspace_bytes,
+                   void *stream);
+/* One step: forward, MSE over the first nout columns of T (T[l] at l * ldT,
+ * rows of 64), backward, and (do_update) Adam with rate lr (beta 0.9/0.999,
+ * eps 1e-8).  loss_out (device, may be NULL): L doubles, MSE per network. */
+int xt_mlp_train_step(void *handle, const float *t, const float *T, long long ldT, int B, float lr, int do_update,
+                      double *loss_out, void *workspace, size_t workspace_bytes, void *stream);
+/* Training data from an SL table (cmap 2, lmax <= 7): inputs t[n] and
+ * targets T[l][n][64] (T[l] at l * ldT) at radii r[n] (device, FP64).
+ * s: (lmax+1) x K prior scales, sig: (lmax+1) x 2K target scales (device). */
+int xt_mlp_labels(void *sph, int K, const double *r, long long n, double a_prior, const double *s,
+                  const double *sig, double c0, double c1, float *t_out, float *T_out, long long ldT, void *stream);
+/* Fold one coefficient set (expcoef (lmax+1)^2 x nmax, device FP64, times
+ * coef_scale) into the networks' last layers and the prior weights. */
+size_t xt_learned_prep_bytes(void *mlp, int K);
+int xt_learned_prepare(void *sph, void *mlp, int K, const double *expcoef, double coef_scale, const double *s,
+                       const double *sig, void *prep, size_t prep_bytes, void *stream);
+/* Potential and gradient at n points (xyzw: float4 x y z -, device) in the
+ * spheresl.all_eval formulation (cos/sin(m phi)); out: float4 per point =
+ * (pot0 + pot1, dpot/dr, dpot/dcos(theta), dpot/dphi).  Radius band b of
+ * nbands equal bands in ln r over the table range uses the networks when
+ * band_use[b] != 0 (device int array) and FP32 table interpolation of
+ * field_f32 (xt_sph_prepare at XT_F32 with the same coefficients) otherwise. */
+size_t xt_learned_eval_workspace(void *sph, long long n);
+int xt_learned_eval(void *sph, const void *field_f32, void *mlp, const void *prep, int K, double a_prior, double c0,
+                    double c1, const int *band_use, int nbands, const float *xyzw, long long n, int no_odd,
+                    float *out, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
