@@ -163,6 +163,108 @@ def batched_extra(K=5):
                           "each l block"}}
 
 
+def learned_extra(steps=20000, batch=8192, n_eval=10_000_000, n_cal=200_000, reps=5):
+    """Learned radial basis on the lmax 6 / nmax 20 Hernquist SL basis:
+    networks trained on the GPU (1e6 log-uniform radii in [1e-3, 100], seed
+    4, Adam lr 1e-3 cosine-decayed to 1e-5), then potential + force at 1e7
+    Hernquist particles (seed 5) with coefficients from those particles.
+    Per radius band: median relative force error of the network path and of
+    FP32 table interpolation against FP64 table interpolation (the judge),
+    and the calibrated hybrid (network where it meets 1e-5, table elsewhere).
+    Throughput of each path beside the plain FP64 table path on the same
+    points."""
+    import torch
+    from exptool_gb300 import _lib, device as dev
+    from exptool_gb300.basis import learned, spheresl
+    from exptool_gb300.tables.samplers import hernquist_sample
+    cache, model = sl6_table_paths()
+    table = spheresl.table_from_files(cache, model)
+    lb = learned.LearnedRadialBasis(table, nbands=12, seed=0)
+    lb.fit_scales()
+    train_s = lb.train(n_train=1_000_000, seed=4, batch=batch, steps=steps, lr=1e-3, lr_final=1e-5,
+                       log_every=max(steps // 4, 1))
+    # 3 x forward flops per sample per network (forward, data and weight gradients)
+    fwd = 2 * (128 + 2 * 128 * 128 + 128 * 64)
+    train_tflops = 3 * fwd * batch * lb.L * lb.steps_done / train_s / 1e12
+    x, y, z, m = hernquist_sample(n_eval, seed=5)
+    ec_d = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)))
+    ec = dev.to_host(ec_d)
+    rep = lb.calibrate(ec, np.stack([x[:n_cal], y[:n_cal], z[:n_cal]], axis=1), bar=1e-5)
+    xyzw = torch.zeros((n_eval, 4), dtype=torch.float32)
+    for k, a in enumerate((x, y, z)):
+        xyzw[:, k] = torch.from_numpy(a.astype(np.float32))
+    xyzw = xyzw.to("cuda")
+    out = torch.empty((n_eval, 4), dtype=torch.float32, device="cuda")
+    ws = torch.empty(lb._lib.xt_learned_eval_workspace(table.handle, n_eval), dtype=torch.uint8, device="cuda")
+    rr = xyzw[:, :3].double().norm(dim=1)
+    cth = torch.where(rr > 0, xyzw[:, 2].double() / rr, torch.zeros_like(rr))
+    phd = torch.atan2(xyzw[:, 1].double(), xyzw[:, 0].double())
+    del x, y, z, m
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    res = {}
+    for name, bu in (("network", np.ones(lb.nbands, np.int32)), ("hybrid", lb.band_use),
+                     ("table_f32_fallback_kernel", np.zeros(lb.nbands, np.int32))):
+        ms = timed(lambda: lb.eval(xyzw, band_use=bu, out=out, workspace=ws))
+        res[name] = {"ms": round(ms, 3), "evals_per_s": n_eval / (ms * 1e-3)}
+    outs = {}
+    for prec in ("f64", "f32"):
+        f = table.prepare(ec_d, 1.0, -1, -1, prec)
+        bufs = [torch.empty(n_eval, dtype=torch.float64, device="cuda") if k in (2, 3, 4, 5, 6) else None
+                for k in range(8)]
+        pp, keep = _lib.ptr_array([dev.dptr(t) for t in bufs])
+
+        def run():
+            _lib.check(table._lib.xt_sph_eval_points(table.handle, dev.dptr(f.buf), f.precision, _lib.XT_COORD_SPH,
+                                                     dev.dptr(rr), dev.dptr(cth), dev.dptr(phd), n_eval,
+                                                     _lib.XT_SPH_ALL_EVAL, -1000, 1000, 0, -1, 0, pp,
+                                                     dev.stream_ptr()), "xt_sph_eval_points")
+        ms = timed(run)
+        res[f"table_{prec}"] = {"ms": round(ms, 3), "evals_per_s": n_eval / (ms * 1e-3)}
+        outs[prec] = bufs
+    base = res["table_f64"]["evals_per_s"]
+    for v in res.values():
+        v["speedup_vs_table_f64"] = round(v["evals_per_s"] / base, 3)
+    # network pass: algorithmic tensor flops per launch
+    rad_flops = n_eval * lb.L * 2 * (2 * 128 * 128 + 2 * 128 * 32)
+    bands = [{k: (round(v, 9) if isinstance(v, float) else v) for k, v in b.items()} for b in rep["bands"]]
+    mem = lb.memory_bytes()
+    return {"workload": "learned radial basis for SL lmax=6 nmax=20 (Hernquist, numr=2000, cmap 2): per-l networks "
+                        "1->128->128->128->40 SiLU, BF16 weights / FP32 accumulate, residual over the "
+                        "Hernquist-Ostriker prior; force eval on 1e7 Hernquist particles (seed 5)",
+            "train": {"steps": lb.steps_done, "batch": batch, "seconds": round(train_s, 3),
+                      "ms_per_step": round(train_s / lb.steps_done * 1e3, 4),
+                      "samples_per_s": batch * lb.steps_done / train_s, "tensor_tflops_achieved": round(train_tflops, 1),
+                      "final_mse_normalised_per_l": lb.history[-1][2] if lb.history else None},
+            "eval": res,
+            "network_pass_tflops": round(rad_flops / (res["network"]["ms"] * 1e-3) / 1e12, 1),
+            "force_err_vs_table_f64": {"bar": 1e-5, "network_median": rep["net_median"],
+                                       "table_f32_median": rep["table32_median"],
+                                       "hybrid_median": rep["hybrid_median"], "hybrid_max": rep["hybrid_max"],
+                                       "bands_on_network": rep["net_bands"],
+                                       "fraction_on_network": rep["net_fraction"],
+                                       "metric": "|grad_net - grad_tab64| / |grad_tab64| per particle, gradient in "
+                                                 "(d/dr, (1/r) d/dtheta, 1/(r sin theta) d/dphi); median per band "
+                                                 "over %d of the particles" % n_cal},
+            "bands": bands,
+            "memory_bytes": mem,
+            "gains": "network: 0.59 MB BF16 parameters for all l vs 4.5 MB of FP64 radial tables; accurate r dphi/dr "
+                     "without table differencing",
+            "losses": "network pass costs %.0f tensor GFLOP per 1e6 points, so it is slower than table "
+                      "interpolation, whose coefficient-contracted field (1.9 MB) sits in L2" % (rad_flops / n_eval * 1e6 / 1e9)}
+
+
 def _block_err(a, b, lmax):
     worst, row = 0.0, 0
     for l in range(lmax + 1):
@@ -392,6 +494,7 @@ def gpu_arm(args, rank, world):
 
     orbits = orbit_extra(path, c64, s64, cache, model, st, hxd, hyd, hzd, hmd, args)
     batched = batched_extra()
+    learned_sl = learned_extra()
 
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
@@ -461,6 +564,7 @@ def gpu_arm(args, rank, world):
                            "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
         "orbits": orbits,
         "batched_spherical": batched,
+        "learned_spherical": learned_sl,
         "clocks": clocks,
     }
     return line

@@ -286,18 +286,13 @@ class LearnedRadialBasis:
         bu = np.ascontiguousarray(self.band_use if band_use is None else band_use, dtype=np.int32)
         if bu.size != self.nbands:
             raise ValueError(f"band_use needs {self.nbands} entries")
-        bkey = bu.tobytes()
-        if getattr(self, "_bu_key", None) != bkey:
-            self._bu_dev = torch.from_numpy(bu.copy()).to(xyzw.device)
-            self._bu_key = bkey
-        bu_dev = self._bu_dev
         out = out if out is not None else torch.empty((n, 4), dtype=torch.float32, device=xyzw.device)
         need = self._lib.xt_learned_eval_workspace(self.table.handle, n)
         ws = workspace if (workspace is not None and workspace.numel() >= need) else \
             torch.empty(max(need, 1), dtype=torch.uint8, device=xyzw.device)
         _lib.check(self._lib.xt_learned_eval(self.table.handle, dev.dptr(self._field32.buf), self.handle,
                                              dev.dptr(self._prep), self.K, self.a_prior, self.c0, self.c1,
-                                             dev.dptr(bu_dev), self.nbands, dev.dptr(xyzw), n, int(bool(no_odd)),
+                                             bu.ctypes.data, self.nbands, dev.dptr(xyzw), n, int(bool(no_odd)),
                                              dev.dptr(out), dev.dptr(ws), ws.numel(), dev.stream_ptr()),
                    "xt_learned_eval")
         return out

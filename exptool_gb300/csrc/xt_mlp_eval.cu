@@ -102,11 +102,11 @@ struct RadialArgs {
   const __nv_bfloat16* w4l;
   const float* b4c;
   float c0, c1, rmin, rmax;
-  const int* band_use;
   float lnr0, inv_bw;
   int nb;
   float* R;
   int rstride;
+  int band_use[MAX_BANDS];
 };
 
 // One hidden layer for the warp's 16 rows: A (16 x 128, BF16 fragments) ->
@@ -163,7 +163,6 @@ __global__ void __launch_bounds__(RAD_WARPS * 32, 2) k_mlp_radial(RadialArgs a) 
   float* b2 = b1 + HID;
   float* b3 = b2 + HID;
   float* b4 = b3 + HID;
-  int* use = reinterpret_cast<int*>(b4 + NC);
   const int l = blockIdx.y;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const __nv_bfloat16* gw = a.wb + (size_t)l * a.psize;
@@ -188,8 +187,8 @@ __global__ void __launch_bounds__(RAD_WARPS * 32, 2) k_mlp_radial(RadialArgs a) 
     b3[i] = gp[MlpLayout::B3 + i];
   }
   for (int i = tid; i < NC; i += blockDim.x) b4[i] = a.b4c[l * NC + i];
-  for (int i = tid; i < a.nb; i += blockDim.x) use[i] = a.band_use[i];
   __syncthreads();
+  const int* use = a.band_use;
 
   const int gq = lane >> 2, tq = lane & 3, q = lane >> 3, r8 = lane & 7;
   const int nout = 2 * (2 * l + 1);
@@ -259,11 +258,11 @@ struct LearnArgs {
   const float* R;           // pass-1 residual sums [n][rstride]
   int rstride, K, lmax, no_odd;
   float a_inv, rmin, rmax, lnr0, inv_bw;
-  const int* band_use;
   int nb;
   const float4* xyzw;
   long long n;
   float4* out;              // pot, dpot/dr, dpot/dcos(theta), dpot/dphi
+  int band_use[MAX_BANDS];
 };
 
 template <int LCAP>
@@ -272,11 +271,10 @@ __global__ void __launch_bounds__(256) k_learned_eval(LearnArgs a) {
   const int nrow = (a.lmax + 1) * (a.lmax + 1);
   float* CS = shm;
   float* inv_n = CS + nrow * a.K;
-  int* use = reinterpret_cast<int*>(inv_n + MLP_KMAX);
   for (int i = threadIdx.x; i < nrow * a.K; i += blockDim.x) CS[i] = a.CS[i];
   for (int i = threadIdx.x; i < MLP_KMAX; i += blockDim.x) inv_n[i] = i ? 1.f / (float)i : 0.f;
-  for (int i = threadIdx.x; i < a.nb; i += blockDim.x) use[i] = a.band_use[i];
   __syncthreads();
+  const int* use = a.band_use;
   const int lstride = a.T.lmax + 1;
   constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < a.n;
@@ -327,15 +325,12 @@ __global__ void __launch_bounds__(256) k_learned_eval(LearnArgs a) {
 #pragma unroll
         for (int rr = 0; rr < 2 * l + 1; ++rr) dv[rr] *= inv_rc;
       } else {
-        const float* g0 = a.GH + (size_t)(B.j - 1) * nrow * 2;
-        const float* g1 = g0 + nrow * 2;
-        const float* g2 = g1 + nrow * 2;
+        const float4* ga = reinterpret_cast<const float4*>(a.GH) + (size_t)B.i * nrow;
 #pragma unroll
         for (int rr = 0; rr < 2 * l + 1; ++rr) {
-          const int row = loff + rr;
-          const float x0 = g0[2 * row], x1 = g1[2 * row], x2 = g2[2 * row];
-          pv[rr] = B.wp[0] * x0 + B.wp[1] * x1 + B.wp[2] * x2;
-          dv[rr] = B.wf[0] * x0 + B.wf[1] * x1 + B.wf[2] * x2;
+          const float4 q = ga[loff + rr];
+          pv[rr] = B.lw0 * q.x + B.lw1 * q.y;
+          dv[rr] = B.fac * fmaf(B.x2, q.w, q.z);
         }
       }
       if (l == 0) {
@@ -457,13 +452,17 @@ int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* pre
   ra.c1 = (float)c1;
   ra.rmin = rmin;
   ra.rmax = rmax;
-  ra.band_use = band_use;
+  bool any_net = false;
+  for (int b = 0; b < nbands; ++b) {
+    ra.band_use[b] = band_use[b] != 0;
+    any_net = any_net || ra.band_use[b];
+  }
   ra.lnr0 = lnr0;
   ra.inv_bw = inv_bw;
   ra.nb = nbands;
   ra.R = static_cast<float*>(workspace);
   ra.rstride = r_stride(T.lmax);
-  const size_t rad_smem = (size_t)(2 * HID + 2 * NC) * WPAD * 2 + (4 * HID + NC) * 4 + MAX_BANDS * 4;
+  const size_t rad_smem = (size_t)(2 * HID + 2 * NC) * WPAD * 2 + (4 * HID + NC) * 4;
   static bool attr_set = false;
   if (!attr_set) {
     XT_CUDA(cudaFuncSetAttribute(k_mlp_radial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_smem));
@@ -477,8 +476,10 @@ int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* pre
   const long long gmax = (ntile + RAD_WARPS - 1) / RAD_WARPS;
   if (gx > gmax) gx = gmax;
   if (gx < 1) gx = 1;
-  k_mlp_radial<<<dim3((unsigned)gx, h->L), RAD_WARPS * 32, rad_smem, st>>>(ra);
-  XT_CHECK_LAUNCH("k_mlp_radial");
+  if (any_net) {
+    k_mlp_radial<<<dim3((unsigned)gx, h->L), RAD_WARPS * 32, rad_smem, st>>>(ra);
+    XT_CHECK_LAUNCH("k_mlp_radial");
+  }
 
   LearnArgs la{};
   la.T = Tf;
@@ -494,12 +495,12 @@ int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* pre
   la.rmax = rmax;
   la.lnr0 = lnr0;
   la.inv_bw = inv_bw;
-  la.band_use = band_use;
+  for (int b = 0; b < nbands; ++b) la.band_use[b] = ra.band_use[b];
   la.nb = nbands;
   la.xyzw = ra.xyzw;
   la.n = n;
   la.out = reinterpret_cast<float4*>(out);
-  const size_t sh = ((size_t)(T.lmax + 1) * (T.lmax + 1) * K + MLP_KMAX + MAX_BANDS) * 4;
+  const size_t sh = ((size_t)(T.lmax + 1) * (T.lmax + 1) * K + MLP_KMAX) * 4;
   if (T.lmax <= 4) return launch_learned_eval<4>(la, sh, st);
   if (T.lmax <= 6) return launch_learned_eval<6>(la, sh, st);
   return launch_learned_eval<7>(la, sh, st);

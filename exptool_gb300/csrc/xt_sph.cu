@@ -112,12 +112,11 @@ __global__ void __launch_bounds__(256) k_sph_contract(const double* __restrict__
   }
 }
 
-// Field GH[(node*nrow + row)*2 + {0,1}] = sum_{n<nuse} s*c[row,n]*{efp,efd}[l,n,node]
-// for rows with l <= luse (others 0).
-template <typename R>
+// FP64 field (drop-in path): GH[(node*nrow + row)*2 + {0,1}] =
+// sum_{n<nuse} s*c[row,n]*{efp,efd}[l,n,node] for rows with l <= luse (others 0).
 __global__ void __launch_bounds__(256) k_sph_field(const double* __restrict__ efp, const double* __restrict__ efd,
                                                    const double* __restrict__ coef, double scale, int lmax, int nmax,
-                                                   int numr, int luse, int nuse, R* __restrict__ GH) {
+                                                   int numr, int luse, int nuse, double* __restrict__ GH) {
   const int nrow = (lmax + 1) * (lmax + 1);
   const long long total = (long long)numr * nrow;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -135,8 +134,49 @@ __global__ void __launch_bounds__(256) k_sph_field(const double* __restrict__ ef
         h += c * efd[ix];
       }
     }
-    GH[2 * t] = (R)g;
-    GH[2 * t + 1] = (R)h;
+    GH[2 * t] = g;
+    GH[2 * t + 1] = h;
+  }
+}
+
+__device__ __forceinline__ double sph_field_sum(const double* __restrict__ tab, const double* __restrict__ coef,
+                                                double scale, int l, int row, int nmax, int numr, int nuse, int node) {
+  double g = 0.0;
+  for (int n = 0; n < nuse; ++n) g += scale * coef[(size_t)row * nmax + n] * tab[((size_t)l * nmax + n) * numr + node];
+  return g;
+}
+
+// FP32 field (mixed path), SphFieldLayout<float>: per lerp base node i and
+// row, float4 (G[i], G[i+1], D1[j], D2[j]), j = max(i, 1), and float2
+// (Gd[i], Gd[i+1]); every entry is formed in FP64 and rounded once.  Node
+// numr-1 is never a lerp base and stays zero.
+__global__ void __launch_bounds__(256) k_sph_field32(const double* __restrict__ efp, const double* __restrict__ efd,
+                                                     const double* __restrict__ p0, const double* __restrict__ coef,
+                                                     double scale, int lmax, int nmax, int numr, int luse, int nuse,
+                                                     float4* __restrict__ GA, float2* __restrict__ GD) {
+  const int nrow = (lmax + 1) * (lmax + 1);
+  const long long total = (long long)numr * nrow;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / nrow);
+    const int row = (int)(t % nrow);
+    int l = 0;
+    while ((l + 1) * (l + 1) <= row) ++l;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 d = make_float2(0.f, 0.f);
+    if (l <= luse && i < numr - 1) {
+      const int j = i < 1 ? 1 : i;
+      const double gm = sph_field_sum(efp, coef, scale, l, row, nmax, numr, nuse, j - 1);
+      const double gc = sph_field_sum(efp, coef, scale, l, row, nmax, numr, nuse, j);
+      const double gp = (j + 1 < numr) ? sph_field_sum(efp, coef, scale, l, row, nmax, numr, nuse, j + 1) : 0.0;
+      const double gi = (i == j) ? gc : gm, gi1 = (i == j) ? gp : gc;
+      const double hm = p0[j - 1] * gm, hc = p0[j] * gc, hp = (j + 1 < numr) ? p0[j + 1] * gp : 0.0;
+      a = make_float4((float)gi, (float)gi1, (float)(0.5 * (hp - hm)), (float)(hm - 2.0 * hc + hp));
+      d = make_float2((float)sph_field_sum(efd, coef, scale, l, row, nmax, numr, nuse, i),
+                      (float)sph_field_sum(efd, coef, scale, l, row, nmax, numr, nuse, i + 1));
+    }
+    GA[t] = a;
+    GD[t] = d;
   }
 }
 
@@ -359,7 +399,9 @@ int xt_sph_accumulate_noalloc(void* handle, const double* x, const double* y, co
 size_t xt_sph_field_bytes(void* handle, int precision) {
   SphHandle* h = static_cast<SphHandle*>(handle);
   if (!h) return 0;
-  return (size_t)h->numr * sph_nrow(h->lmax) * 2 * (precision == XT_F32 ? sizeof(float) : sizeof(double));
+  return (size_t)h->numr * sph_nrow(h->lmax) *
+         (precision == XT_F32 ? SphFieldLayout<float>::per_row * sizeof(float)
+                              : SphFieldLayout<double>::per_row * sizeof(double));
 }
 
 int xt_sph_prepare(void* handle, const double* expcoef, double coef_scale, int lmax_use, int nmax_use, int precision,
@@ -377,12 +419,15 @@ int xt_sph_prepare(void* handle, const double* expcoef, double coef_scale, int l
   cudaStream_t st = as_stream(stream);
   const long long total = (long long)h->numr * sph_nrow(h->lmax);
   const int grid = grid_for(total, 256, 4);
-  if (precision == XT_F64)
-    k_sph_field<double><<<grid, 256, 0, st>>>(h->efp, h->efd, expcoef, coef_scale, h->lmax, h->nmax, h->numr,
-                                              lmax_use, nmax_use, static_cast<double*>(field));
-  else
-    k_sph_field<float><<<grid, 256, 0, st>>>(h->efp, h->efd, expcoef, coef_scale, h->lmax, h->nmax, h->numr,
-                                             lmax_use, nmax_use, static_cast<float*>(field));
+  if (precision == XT_F64) {
+    k_sph_field<<<grid, 256, 0, st>>>(h->efp, h->efd, expcoef, coef_scale, h->lmax, h->nmax, h->numr, lmax_use,
+                                      nmax_use, static_cast<double*>(field));
+  } else {
+    float* f = static_cast<float*>(field);
+    k_sph_field32<<<grid, 256, 0, st>>>(h->efp, h->efd, h->p0, expcoef, coef_scale, h->lmax, h->nmax, h->numr,
+                                        lmax_use, nmax_use, reinterpret_cast<float4*>(f),
+                                        reinterpret_cast<float2*>(f + (size_t)total * 4));
+  }
   XT_CHECK_LAUNCH("k_sph_field");
   return XT_OK;
 }

@@ -35,12 +35,30 @@ __host__ __device__ inline int tri(int l, int m) { return l * (l + 1) / 2 + m; }
 //   force-like fac*(stencil)    = wf[0] G[j-1] + wf[1] G[j] + wf[2] G[j+1]
 //   dens-like  lerp(G) * dlerp  = wd[0] G[j-1] + wd[1] G[j] + wd[2] G[j+1]
 // The force stencil at indx == 0 uses rows 0,1,2 with the unshifted x2
-// (spheresl.py:147-150).
+// (spheresl.py:147-150).  With H = p0 G the stencil is
+//   fac * ( (H[j+1]-H[j-1])/2 + x2 (H[j-1] - 2 H[j] + H[j+1]) ),
+// which the FP32 field stores pre-differenced (in FP64), so the FP32 path
+// never subtracts nearly equal table values.
 template <typename R>
 struct SphBins {
   int i, j;       // lerp base node i, stencil centre j = max(i, 1)
   R lw0, lw1;     // x1*plerp, x2*plerp on nodes i, i+1
+  R dw0, dw1;     // x1*dlerp, x2*dlerp on nodes i, i+1
   R wp[3], wf[3], wd[3];
+  R fac, x2;      // d xi/dr / dxi and the in-cell offset (pre-differenced force)
+};
+
+// Coefficient-contracted SL fields.  FP64 (the drop-in path): per node, per
+// row, (G, Gd) = sum_n c[row,n] ef[l,n,node] {1/sqrt(ev), sqrt(ev)}.
+// FP32 (the mixed path), laid out for one 16-byte gather per row: a float4
+// array [numr][nrow] of (G[i], G[i+1], D1[j], D2[j]) with j = max(i, 1),
+// D1 = (H[j+1]-H[j-1])/2, D2 = H[j-1]-2H[j]+H[j+1], H = p0 G (all from FP64
+// sums), followed by a float2 array [numr][nrow] of (Gd[i], Gd[i+1]).
+template <typename R>
+struct SphFieldLayout {
+  static constexpr bool f32 = std::is_same<R, float>::value;
+  // elements of R per (node, row)
+  static constexpr int per_row = f32 ? 6 : 2;
 };
 
 template <typename R>
@@ -87,16 +105,23 @@ __device__ __forceinline__ SphBins<R> sph_bins(const SphTab<R>& T, R r, bool nee
   } else {
     B.wp[0] = B.lw0; B.wp[1] = B.lw1; B.wp[2] = R(0);
   }
+  B.fac = R(0);
+  B.x2 = x2;
+  B.wf[0] = B.wf[1] = B.wf[2] = R(0);
   if (need_force) {
-    R fac = d_xi_to_r(x, T.cmap, T.scale) * T.inv_dxi;
-    B.wf[0] = fac * (x2 - R(0.5)) * T.p0[j - 1];
-    B.wf[1] = fac * (R(-2) * x2) * T.p0[j];
-    B.wf[2] = fac * (x2 + R(0.5)) * T.p0[j + 1];
-  } else {
-    B.wf[0] = B.wf[1] = B.wf[2] = R(0);
+    const R fac = d_xi_to_r(x, T.cmap, T.scale) * T.inv_dxi;
+    B.fac = fac;
+    if constexpr (!std::is_same<R, float>::value) {
+      B.wf[0] = fac * (x2 - R(0.5)) * T.p0[j - 1];
+      B.wf[1] = fac * (R(-2) * x2) * T.p0[j];
+      B.wf[2] = fac * (x2 + R(0.5)) * T.p0[j + 1];
+    }
   }
+  B.dw0 = B.dw1 = R(0);
   if (need_dens) {
     R dlerp = x1 * T.d0[i] + x2 * T.d0[i + 1];
+    B.dw0 = x1 * dlerp;
+    B.dw1 = x2 * dlerp;
     if (i == j) {
       B.wd[0] = R(0); B.wd[1] = x1 * dlerp; B.wd[2] = x2 * dlerp;
     } else {
@@ -194,9 +219,7 @@ struct SphEvalOpts {
 };
 
 // One point of the spherical evaluation.  Field GH: per node, per row, the
-// coefficient-contracted radial functions (pot-kind, dens-kind):
-//   GH[(node*nrow + row)*2 + 0] = sum_n c[row,n] ef[l,n,node]/sqrt(ev[l,n])
-//   GH[(node*nrow + row)*2 + 1] = sum_n c[row,n] ef[l,n,node]*sqrt(ev[l,n])
+// coefficient-contracted radial functions in the SphFieldLayout of R.
 // out: den0 den1 pot0 pot1 potr pott potp (before the mode's output mapping).
 template <typename R, int LCAP>
 __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __restrict__ GH, R r, R costh, R c1,
@@ -218,14 +241,26 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
   const R* g2 = g1 + nrow * 2;
 
   auto rowvals = [&](int row, R& pot, R& frc, R& den) {
-    R a0 = g0[2 * row], a1 = g1[2 * row], a2 = g2[2 * row];
-    pot = B.wp[0] * a0 + B.wp[1] * a1 + B.wp[2] * a2;
-    frc = B.wf[0] * a0 + B.wf[1] * a1 + B.wf[2] * a2;
-    if (dens) {
-      R b0 = g0[2 * row + 1], b1 = g1[2 * row + 1], b2 = g2[2 * row + 1];
-      den = B.wd[0] * b0 + B.wd[1] * b1 + B.wd[2] * b2;
+    if constexpr (SphFieldLayout<R>::f32) {
+      const float4 q = reinterpret_cast<const float4*>(GH)[(size_t)B.i * nrow + row];
+      pot = B.lw0 * q.x + B.lw1 * q.y;
+      frc = B.fac * fmaf(B.x2, q.w, q.z);
+      if (dens) {
+        const float2 d = reinterpret_cast<const float2*>(GH + (size_t)T.numr * nrow * 4)[(size_t)B.i * nrow + row];
+        den = B.dw0 * d.x + B.dw1 * d.y;
+      } else {
+        den = R(0);
+      }
     } else {
-      den = R(0);
+      R a0 = g0[2 * row], a1 = g1[2 * row], a2 = g2[2 * row];
+      pot = B.wp[0] * a0 + B.wp[1] * a1 + B.wp[2] * a2;
+      frc = B.wf[0] * a0 + B.wf[1] * a1 + B.wf[2] * a2;
+      if (dens) {
+        R b0 = g0[2 * row + 1], b1 = g1[2 * row + 1], b2 = g2[2 * row + 1];
+        den = B.wd[0] * b0 + B.wd[1] * b1 + B.wd[2] * b2;
+      } else {
+        den = R(0);
+      }
     }
   };
 

@@ -241,8 +241,8 @@ int xt_learned_prepare(void *sph, void *mlp, int K, const double *expcoef, doubl
 /* Potential and gradient at n points (xyzw: float4 x y z -, device) in the
  * spheresl.all_eval formulation (cos/sin(m phi)); out: float4 per point =
  * (pot0 + pot1, dpot/dr, dpot/dcos(theta), dpot/dphi).  Radius band b of
- * nbands equal bands in ln r over the table range uses the networks when
- * band_use[b] != 0 (device int array) and FP32 table interpolation of
+ * nbands (<= 64) equal bands in ln r over the table range uses the networks
+ * when band_use[b] != 0 (host int array) and FP32 table interpolation of
  * field_f32 (xt_sph_prepare at XT_F32 with the same coefficients) otherwise. */
 size_t xt_learned_eval_workspace(void *sph, long long n);
 int xt_learned_eval(void *sph, const void *field_f32, void *mlp, const void *prep, int K, double a_prior, double c0,
