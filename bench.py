@@ -41,6 +41,8 @@ N1 = 1_000_000
 CFG0 = dict(lmax=4, nmax=10, numr=2000, rmin=1e-3, rmax=100.0, cmap=2, scale=1.0)
 N0 = 100_000
 L2_BYTES = 129 * 1024 * 1024
+# DRAM bytes of one k_cyl_binrec<double, df> launch at the headline workload (ncu --set full)
+BINREC_F64_TRAFFIC = 32_177_664 + 3_989_504
 
 
 def cache_dir():
@@ -551,7 +553,10 @@ def gpu_arm(args, rank, world):
                     "contraction, field, sorted evaluation (8 kernels)",
         "gpu_launches": 8 * K,
         "roofline": {"bound": "hbm", "kernel": st_names[dom], "achieved": round(ach, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": BINREC_F64_TRAFFIC,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_cyl_binrec<double, df> "
+                                       "at this workload (one launch)",
+                     "bound_note": "FP64-issue-bound: ncu shows the FP64 pipe 87 % active at 1.5 % of DRAM peak",
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg64[dom],
                      "launch_ms": round(float(stages64[dom]), 4)},
         "fused_stages": fused_stages,
@@ -738,6 +743,37 @@ def profile_batched(args):
     return 0
 
 
+def profile_learned(args):
+    """Learned radial basis on the lmax 6 / nmax 20 Hernquist basis: label
+    1e5 radii, warm-up + 3 training steps (batch 8192), then for 1e6
+    Hernquist points (seed 5) warm-up evaluations and one evaluation with the
+    networks in every band and one with the table in every band."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import learned, spheresl
+    from exptool_gb300.tables.samplers import hernquist_sample
+    cache, model = sl6_table_paths()
+    table = spheresl.table_from_files(cache, model)
+    lb = learned.LearnedRadialBasis(table, nbands=12, seed=0)
+    lb.fit_scales(n=16384)
+    t, T = lb.labels(dev.to_dev(lb.sample_radii(65536, 4)))
+    for _ in range(args.warmup + 3):
+        lb.train_step(t[:8192], T[:, :8192, :], 65536 * 64, 8192, 1e-3)
+    n = 1_000_000
+    x, y, z, m = hernquist_sample(n, seed=5)
+    ec = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)))
+    lb.prepare(ec)
+    xyzw = torch.zeros((n, 4), dtype=torch.float32)
+    for k, a in enumerate((x, y, z)):
+        xyzw[:, k] = torch.from_numpy(a.astype(np.float32))
+    xyzw = xyzw.to("cuda")
+    for bu in [np.ones(12, np.int32)] * args.warmup + [np.ones(12, np.int32), np.zeros(12, np.int32)]:
+        lb.eval(xyzw, band_use=bu)
+    torch.cuda.synchronize()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -748,6 +784,8 @@ def main():
     ap.add_argument("--profile-batched", action="store_true",
                     help="run the batched spherical accumulation on the first 16 snapshots (warm-up + one call) "
                          "and exit (for ncu captures)")
+    ap.add_argument("--profile-learned", action="store_true",
+                    help="learned radial basis: a few training steps and two evaluations of 1e6 points (for ncu)")
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
                          "(a short, fixed launch sequence for ncu captures)")
@@ -756,6 +794,8 @@ def main():
         return profile_run(args)
     if args.profile_batched:
         return profile_batched(args)
+    if args.profile_learned:
+        return profile_learned(args)
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
