@@ -324,3 +324,29 @@ def accumulated_eval(r, z, phi, accum_cos, accum_sin, potC, rforceC, zforceC, de
                              _lib.XT_COORD_CYL, no_odd=no_odd)
     res = [dev.to_host(t) for t in outs[:7]]
     return tuple(float(v[0]) for v in res) if scalar else tuple(res)
+
+
+# ---------------------------------------------------------------- coefficient files
+def eof_coefficients_to_file(f, EOF_Object):
+    """eof.eof_coefficients_to_file (eof.py:1646-1671)."""
+    from ..io import coefficients
+    coefficients.eof_coefficients_to_file(f, EOF_Object)
+
+
+def save_eof_coefficients(outfile, EOF_Object, verbose=0):
+    """eof.save_eof_coefficients (eof.py:1675-1709)."""
+    from ..io import coefficients
+    coefficients.save_eof_coefficients(outfile, EOF_Object, verbose)
+
+
+def restore_eof_coefficients(infile):
+    """eof.restore_eof_coefficients (eof.py:1712-1739): (last dump,
+    OrderedDict{time: EOF_Object})."""
+    from ..io import coefficients
+    return coefficients.restore_eof_coefficients(infile, EOF_Object)
+
+
+def extract_eof_coefficients(f):
+    """eof.extract_eof_coefficients (eof.py:1743-1760)."""
+    from ..io import coefficients
+    return coefficients.extract_eof_coefficients(f, EOF_Object)

@@ -57,6 +57,13 @@ class Fields:
     # ------------------------------------------------------------ tables
     def prep_tables(self):
         """Read and upload both bases (potential.py:257-294)."""
+        self._read_tables()
+        self._cyl = eof.table_from_file(self.EOF.eof_file)
+        self._upload_halo()
+
+    def _read_tables(self):
+        """The host half of prep_tables: table arrays and parameters as
+        instance attributes (what save_field writes)."""
         try:
             eof_file = self.EOF.eof_file
         except AttributeError:
@@ -76,11 +83,77 @@ class Fields:
             self.SL.model_file, self.numrhalo, self.rminhalo, self.rmaxhalo, cmap=self.cmaphalo, scale=self.scalehalo)
         self.halo_use_l = self.lmaxhalo
         self.halo_use_n = self.nmaxhalo
-        self._cyl = eof.table_from_file(eof_file)
+
+    def _upload_halo(self):
         self._sph = dev.SphTable(self.lmaxhalo, self.nmaxhalo, self.numrhalo, self.cmaphalo, self.rminhalo,
                                  self.rmaxhalo, self.scalehalo, self.xihalo, self.p0halo, self.d0halo,
                                  self.evtablehalo, self.eftablehalo)
         self._fcache = {}
+
+    def _upload_from_arrays(self):
+        """Device tables from the instance's own arrays (a restored field)."""
+        dens = bool(self.densdisk)
+        self._cyl = eof.table_from_arrays(self.mmax, self.norder, self.numx, self.numy, self.cmapdisk, self.XMIN,
+                                          self.dX, self.YMIN, self.dY, self.ascale, self.hscale, self.potC,
+                                          self.rforceC, self.zforceC, self.potS, self.rforceS, self.zforceS,
+                                          self.densC if dens else None, self.densS if dens else None)
+        self._upload_halo()
+
+    # ------------------------------------------------------------ persistence
+    def save_field(self, filename=''):
+        """potential.Fields.save_field (potential.py:738-963): the global, EOF
+        and SL blocks of a prepared instance in one binary record, readable by
+        ``restore_field``."""
+        from ..io import coefficients
+        if filename == '':
+            print('potential.Fields.save_field: No filename specified.')
+        if not hasattr(self, "potC"):
+            self._read_tables()
+        for k in ("xcen_disk", "ycen_disk", "zcen_disk", "xcen_halo", "ycen_halo", "zcen_halo"):
+            if not hasattr(self, k):
+                setattr(self, k, 0.0)
+        with open(filename, "wb") as f:
+            coefficients.field_record(self).tofile(f)
+
+    # ------------------------------------------------------------ curves
+    def rotation_curve(self, rvals=np.linspace(0.0001, 0.1, 100), mono=False, angle=0.):
+        """potential.Fields.rotation_curve (potential.py:500-565): v_c from the
+        radial forces at (x, y, z) = (r, angle, 0) -- the reference passes
+        `angle` as the y coordinate -- all points in one GPU call."""
+        if mono:
+            keep = (self.halo_use_l, self.disk_use_m)
+            self.halo_use_l, self.disk_use_m = 0, 0
+        rv = np.asarray(rvals, dtype=np.float64)
+        res = self.return_forces_cyl(rv, np.full_like(rv, angle), np.zeros_like(rv))
+        disk_force, halo_force = np.asarray(res[0]), np.asarray(res[1])
+        self.rvals = rvals
+        self.disk_dpdr = -1. * disk_force
+        self.halo_dpdr = -1. * halo_force
+        self.total_dpdr = -1. * disk_force + -1. * halo_force
+        self.disk_rotation = (rv * abs(disk_force)) ** 0.5
+        self.halo_rotation = (rv * abs(halo_force)) ** 0.5
+        self.total_rotation = (rv * (abs(halo_force) + abs(disk_force))) ** 0.5
+        if mono:
+            self.halo_use_l, self.disk_use_m = keep
+
+    def resonance_positions(self, rvals=np.linspace(0.0001, 0.1, 100), mono=False):
+        """potential.Fields.resonance_positions (potential.py:568-628): omega and
+        kappa = sqrt(3 omega^2 + d omega/dr) (the reference's expression) from
+        the radial forces along +x, derivative by an interpolating cubic spline."""
+        from scipy.interpolate import UnivariateSpline
+        if mono:
+            keep = (self.halo_use_l, self.disk_use_m)
+            self.halo_use_l, self.disk_use_m = 0, 0
+        rv = np.asarray(rvals, dtype=np.float64)
+        res = self.return_forces_cyl(rv, np.zeros_like(rv), np.zeros_like(rv))
+        disk_force, halo_force = np.asarray(res[0]), np.asarray(res[1])
+        self.rvals = rvals
+        self.omega = ((abs(halo_force) + abs(disk_force)) / rv) ** 0.5
+        spl = UnivariateSpline(rv, self.omega, k=3, s=0)
+        ddphi = spl.derivative()(rv)
+        self.kappa = (3. * self.omega ** 2. + ddphi) ** 0.5
+        if mono:
+            self.halo_use_l, self.disk_use_m = keep
 
     def set_field_parameters(self, no_odd=False, halo_l=-1, halo_n=-1, disk_m=-1, disk_n=-1):
         """potential.py:365-377."""
@@ -177,3 +250,40 @@ class Fields:
         fzhalo = -1.0 * (z * hfr - r2 * hft) / r3
         res = (dfr, frhalo, dfp, -1.0 * hfp, dfz, fzhalo, -1.0 * dp, hp + hp0)
         return tuple(float(v[0]) for v in res) if scalar else res
+
+
+def restore_field(filename=''):
+    """potential.restore_field (potential.py:968-1042): a Fields instance
+    from a ``save_field`` file, with its tables and coefficients, ready for
+    force evaluation without the original cache files."""
+    from ..io import coefficients
+    r = coefficients.read_field_record(filename)
+    infile, eof_file, sph_file, model_file = r["files"]
+    nhalo, transform, no_odd, centering, mutual_center, verbose = (int(v) for v in r["flags"])
+    F = Fields(infile, eof_file, sph_file, model_file, nhalo=nhalo, transform=transform, no_odd=no_odd,
+               centering=centering, mutual_center=mutual_center, verbose=verbose)
+    F.time = r["time"]
+    F.numx, F.numy, F.mmax, F.norder, F.cmapdisk, F.densdisk = (int(v) for v in r["eof_i"])
+    (F.rmindisk, F.rmaxdisk, F.ascale, F.hscale, F.XMIN, F.dX, F.YMIN, F.dY, F.xcen_disk, F.ycen_disk,
+     F.zcen_disk) = r["eof_f"]
+    shp = (F.mmax + 1, F.norder, F.numx + 1, F.numy + 1)
+    F.EOF = eof.EOF_Object()
+    F.EOF.cos = r["cos"].reshape(F.mmax + 1, F.norder)
+    F.EOF.sin = r["sin"].reshape(F.mmax + 1, F.norder)
+    for k in ("potC", "rforceC", "zforceC", "densC", "potS", "rforceS", "zforceS", "densS"):
+        setattr(F, k, r[k].reshape(shp))
+    F.halofac, F.rminhalo, F.rmaxhalo, F.scalehalo, F.xcen_halo, F.ycen_halo, F.zcen_halo = r["sl_f"]
+    F.numrhalo, F.cmaphalo, F.lmaxhalo, F.nmaxhalo = (int(v) for v in r["sl_i"])
+    F.xihalo, F.p0halo, F.d0halo = r["xi"], r["p0"], r["d0"]
+    F.ltable = F.ltablehalo = r["ltable"]
+    F.evtablehalo = r["ev"].reshape(F.lmaxhalo + 1, F.nmaxhalo)
+    F.eftablehalo = r["ef"].reshape(F.lmaxhalo + 1, F.nmaxhalo, F.numrhalo)
+    F.SL = spheresl.SL_Object()
+    F.SL.expcoef = r["expcoef"].reshape((F.lmaxhalo + 1) ** 2, F.nmaxhalo)
+    F.disk_use_m, F.disk_use_n = F.mmax, F.norder
+    F.halo_use_l, F.halo_use_n = F.lmaxhalo, F.nmaxhalo
+    F.SL.model_file, F.SL.sph_file = F.model_file, F.sph_file
+    F.EOF.eof_file, F.EOF.mmax = F.eof_file, F.mmax
+    F.halofac = float(F.halofac)
+    F._upload_from_arrays()
+    return F

@@ -231,3 +231,31 @@ def factorial_return(lmax):
             if m != 0:
                 f[l, m] *= np.sqrt(2.0)
     return f
+
+
+# ---------------------------------------------------------------- coefficient files
+def sl_coefficients_to_file(f, SL_Object):
+    """spheresl.sl_coefficients_to_file (spheresl.py:1390-1409): one dump at
+    the current position of the open file."""
+    from ..io import coefficients
+    coefficients.sl_coefficients_to_file(f, SL_Object)
+
+
+def save_sl_coefficients(outfile, SL_Object, verbose=0):
+    """spheresl.save_sl_coefficients (spheresl.py:1414-1441): append a dump and
+    bump the leading dump count."""
+    from ..io import coefficients
+    coefficients.save_sl_coefficients(outfile, SL_Object, verbose)
+
+
+def restore_sl_coefficients(infile):
+    """spheresl.restore_sl_coefficients (spheresl.py:1444-1467): (last dump,
+    {round(time, 3): SL_Object})."""
+    from ..io import coefficients
+    return coefficients.restore_sl_coefficients(infile, SL_Object)
+
+
+def extract_sl_coefficients(f):
+    """spheresl.extract_sl_coefficients (spheresl.py:1471-1488)."""
+    from ..io import coefficients
+    return coefficients.extract_sl_coefficients(f, SL_Object)

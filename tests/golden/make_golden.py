@@ -11,6 +11,10 @@ Outputs (all small):
   eof_c1.npz, eof_c0.npz      particles, EOF accumulate / evaluate outputs
   fields.npz                  Fields.return_forces_cart, leapfrog_integrate,
                               compute_timestep outputs
+  coef_files.npz              bytes of SL / EOF coefficient files written by the
+                              reference (two dumps each), the SHA-256 and size of
+                              a Fields.save_field file, rotation_curve and
+                              resonance_positions outputs
 The table files are built by this project's generators; every output array is
 produced by the reference code.
 """
@@ -241,6 +245,77 @@ def fields_case(ref, sph_cache, sph_model, expcoef, eof_path, a_cos, a_sin):
     print("fields done")
 
 
+def coef_files_case(ref, sl_ec, sl_ec2, eof_cos, eof_sin):
+    """Coefficient and field files written by the reference's own writers,
+    from fixed metadata (relative file names, so the bytes do not depend on
+    where the repository lives)."""
+    import hashlib
+    import tempfile
+    out = {}
+    tmp = tempfile.mkdtemp()
+    o = ref.spheresl.SL_Object()
+    o.filename, o.comp, o.nbodies, o.sph_file, o.model_file = "OUT.run0.00010", "dark", 207, "sl_c2.cache", "sl_c2.model"
+    o.lmax, o.nmax = 4, 6
+    sl_path = os.path.join(tmp, "sl.coef")
+    # spheresl.save_sl_coefficients fails under numpy 2 (it seeks with a
+    # 1-element memmap, spheresl.py:1435); frame the file as it does and let
+    # the reference's own sl_coefficients_to_file write each dump
+    with open(sl_path, "wb") as f:
+        np.array([2], dtype="i4").tofile(f)
+        for t, ec in ((0.5, sl_ec), (1.25, sl_ec2)):
+            o.time, o.expcoef = t, ec
+            ref.spheresl.sl_coefficients_to_file(f, o)
+    last, dumps = ref.spheresl.restore_sl_coefficients(sl_path)
+    out["sl_restored_times"] = np.array(sorted(dumps.keys()))
+    out["sl_bytes"] = np.frombuffer(open(sl_path, "rb").read(), dtype=np.uint8)
+    e = ref.eof.EOF_Object()
+    e.filename, e.comp, e.nbodies, e.eof_file, e.mmax, e.nmax = "OUT.run0.00010", "star", 3000, "eof_c1.cache", 3, 3
+    eof_path = os.path.join(tmp, "eof.coef")
+    for t, (c, s_) in ((0.5, (eof_cos, eof_sin)), (1.25, (2.0 * eof_cos, -eof_sin))):
+        e.time, e.cos, e.sin = t, c, s_
+        ref.eof.save_eof_coefficients(eof_path, e)
+    out["eof_bytes"] = np.frombuffer(open(eof_path, "rb").read(), dtype=np.uint8)
+    last, dumps = ref.eof.restore_eof_coefficients(eof_path)
+    out["eof_restored_times"] = np.array(list(dumps.keys()))
+    # a whole field, with cache file names relative to this directory
+    cwd = os.getcwd()
+    os.chdir(HERE)
+    try:
+        refshim.set_log_bounds(ref, 1e-3, 100.0)
+        F = ref.potential.Fields("OUT.run0.00010", "eof_c1.cache", "sl_c2.cache", "sl_c2.model", verbose=0)
+        F.EOF = ref.eof.EOF_Object()
+        F.EOF.eof_file, F.EOF.cos, F.EOF.sin = "eof_c1.cache", eof_cos, eof_sin
+        F.SL = ref.spheresl.SL_Object()
+        F.SL.sph_file, F.SL.model_file, F.SL.expcoef = "sl_c2.cache", "sl_c2.model", sl_ec
+        F.halofac = 0.75
+        F.time = 2.5
+        F.prep_tables()
+        F.xcen_disk = F.ycen_disk = F.zcen_disk = 0.0
+        F.xcen_halo = F.ycen_halo = F.zcen_halo = 0.0
+        fpath = os.path.join(tmp, "field.bin")
+        F.save_field(fpath)
+        raw = open(fpath, "rb").read()
+        out["field_sha256"] = np.frombuffer(hashlib.sha256(raw).digest(), dtype=np.uint8)
+        out["field_size"] = np.array(len(raw))
+        G = ref.potential.restore_field(fpath)
+        px = np.array([0.7, -1.3, 2.2])
+        py = np.array([0.4, 0.9, -0.6])
+        pz = np.array([0.05, -0.2, 0.3])
+        out["restored_forces_cart"] = np.array([G.return_forces_cart(px[i], py[i], pz[i]) for i in range(3)])
+        rv = np.linspace(0.05, 3.0, 12)
+        F.rotation_curve(rvals=rv)
+        for k in ("disk_rotation", "halo_rotation", "total_rotation", "disk_dpdr", "halo_dpdr", "total_dpdr"):
+            out["rc_" + k] = np.asarray(getattr(F, k))
+        F.rotation_curve(rvals=rv, mono=True, angle=0.3)
+        out["rc_mono_angle_total_rotation"] = np.asarray(F.total_rotation)
+        F.resonance_positions(rvals=rv)
+        out["rp_omega"], out["rp_kappa"] = np.asarray(F.omega), np.asarray(F.kappa)
+    finally:
+        os.chdir(cwd)
+    np.savez_compressed(P("coef_files.npz"), **out)
+    print("coefficient files done")
+
+
 def main():
     ref = refshim.load()
     sl_out = {}
@@ -250,6 +325,8 @@ def main():
     eof_case(ref, "c0", 0, False, 2, 3, 8, 600)
     cache, modelf, ec = sl_out[2]
     fields_case(ref, cache, modelf, ec, eof_path, a_cos, a_sin)
+    ec2 = np.load(P("sl_c2.npz"))["expcoef_noodd"]
+    coef_files_case(ref, ec, ec2, a_cos, a_sin)
 
 
 if __name__ == "__main__":
