@@ -342,6 +342,18 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ GPU arm
+def max_over_ranks(x, world, device="cuda"):
+    """Max of a host number over the ranks of the default process group: the
+    slowest replica sets the time of a step."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def gpu_arm(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -387,10 +399,7 @@ def gpu_arm(args, rank, world):
             tot += e0.elapsed_time(e1)
         if world > 1:
             dist.barrier()
-            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            tot = float(tt.item())
-        return tot
+        return max_over_ranks(tot, world)
 
     def timed(prec, steps, warmup, phases=False):
         for _ in range(warmup):
@@ -418,10 +427,7 @@ def gpu_arm(args, rank, world):
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
-            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            tot = float(tt.item())
-        return tot, ph / steps
+        return max_over_ranks(tot, world), ph / steps
 
     K, W = args.steps, args.warmup
     with Clocks(int(os.environ.get("LOCAL_RANK", 0))) as clk:
