@@ -79,7 +79,10 @@ _SIGS = {
     "xt_learned_prepare": (c_int, [c_vp, c_vp, c_int, c_vp, c_dbl, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "xt_learned_eval_workspace": (c_sz, [c_vp, c_ll]),
     "xt_learned_eval": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_int, c_vp, c_ll, c_int,
-                                c_vp, c_vp, c_sz, c_vp]),
+                                c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_learned_radial_pass": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_int, c_vp, c_ll, c_int,
+                                       c_vp, c_vp]),
+    "xt_learned_status": (c_int, []),
 }
 
 EXPORTED = tuple(_SIGS)

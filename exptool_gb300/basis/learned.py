@@ -134,6 +134,7 @@ class LearnedRadialBasis:
         _lib.check(self._lib.xt_mlp_create(self.L, 2 * self.K, p.ctypes.data, _lib.ctypes.byref(h)), "xt_mlp_create")
         self.handle = h.value
         self.band_use = np.zeros(self.nbands, dtype=np.int32)
+        self.engine = "tc"
         self.history = []
         self.report = None
         self._prep_key = None
@@ -274,7 +275,27 @@ class LearnedRadialBasis:
         self._field32 = self.table.prepare(ec, coef_scale, -1, -1, "f32")
         self._prep_key = key
 
-    def eval(self, xyzw, band_use=None, no_odd=False, out=None, workspace=None):
+    ENGINES = {"mma": 0, "tc": 1}
+
+    def radial_pass(self, xyzw, engine="tc", band_use=None):
+        """The network pass alone: (N, rstride) float32 folded network sums
+        (rows of points outside network bands are left unset)."""
+        bu = np.ascontiguousarray(np.ones(self.nbands) if band_use is None else band_use, dtype=np.int32)
+        n = int(xyzw.shape[0])
+        rs = (2 * self.L * self.L + 3) // 4 * 4
+        R = torch.zeros((n, rs), dtype=torch.float32, device=xyzw.device)
+        _lib.check(self._lib.xt_learned_radial_pass(self.table.handle, self.handle, dev.dptr(self._prep), self.K,
+                                                    self.a_prior, self.c0, self.c1, bu.ctypes.data, self.nbands,
+                                                    dev.dptr(xyzw), n,
+                                                    self.ENGINES[engine], dev.dptr(R), dev.stream_ptr()),
+                   "xt_learned_radial_pass")
+        return R
+
+    def status(self):
+        """Raise if a tensor-memory network pass gave up waiting for its MMAs."""
+        _lib.check(self._lib.xt_learned_status(), "learned network pass")
+
+    def eval(self, xyzw, band_use=None, no_odd=False, out=None, workspace=None, engine=None):
         """float4 (pot, dpot/dr, dpot/dcos(theta), dpot/dphi) per point of xyzw
         ((N, 4) float32 CUDA tensor), all_eval formulation.  band_use: per band
         1 = network, 0 = table (default: the calibrated choice)."""
@@ -293,7 +314,8 @@ class LearnedRadialBasis:
         _lib.check(self._lib.xt_learned_eval(self.table.handle, dev.dptr(self._field32.buf), self.handle,
                                              dev.dptr(self._prep), self.K, self.a_prior, self.c0, self.c1,
                                              bu.ctypes.data, self.nbands, dev.dptr(xyzw), n, int(bool(no_odd)),
-                                             dev.dptr(out), dev.dptr(ws), ws.numel(), dev.stream_ptr()),
+                                             self.ENGINES[engine or self.engine], dev.dptr(out), dev.dptr(ws),
+                                             ws.numel(), dev.stream_ptr()),
                    "xt_learned_eval")
         return out
 

@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "xt_internal.cuh"
 
@@ -52,24 +53,57 @@ struct MlpHandle {
   long long step = 0;
 };
 
-// SiLU through the hardware tanh: sigma(z) = (1 + tanh(z/2)) / 2.  Training
-// and inference use the same form, so the trained network is the evaluated one.
+constexpr int TC_MAX_BANDS = 64;
+
+// Arguments of the tensor-memory network pass (xt_mlp_tc.cu).
+struct TcArgs {
+  const float4* xyzw;
+  long long n;
+  const __nv_bfloat16* wb;
+  const float* params;
+  int psize, L;
+  const __nv_bfloat16* w4h;
+  const __nv_bfloat16* w4l;
+  const float* b4c;
+  float c0, c1, rmin, rmax;
+  float lnr0, inv_bw;
+  int nb;
+  float* R;
+  int rstride;
+  int* err;                   // set to 1 on an MMA wait timeout
+  const float* CS;            // [(lmax+1)^2][K] prior weights c * scale * s (adds the prior to R)
+  int K;
+  float a_inv;                // 1 / prior scale length
+  int band_use[TC_MAX_BANDS];
+};
+int launch_mlp_radial_tc(const TcArgs& a, int nsm, cudaStream_t st);
+int tc_error_flag(int** dptr);
+
+// SiLU through the hardware tanh: sigma(z) = (1 + tanh(z/2)) / 2.  Training,
+// the gradients and both inference engines use these same functions, so the
+// trained network is the evaluated one.  (Packed-half tanh halves the
+// transcendental instructions but costs more conversions than it saves here.)
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 __device__ __forceinline__ float sigm_fast(float z) { return fmaf(0.5f, tanh_fast(0.5f * z), 0.5f); }
-__device__ __forceinline__ float silu_fast(float z) { return z * sigm_fast(z); }
+// silu(z) = h + h tanh(h) with h = z/2.  Halving is exact, so callers may
+// form h directly as fma(x, w/2, b/2) = (x w + b)/2 with the same bits.
+__device__ __forceinline__ float silu_h(float h) { return fmaf(h, tanh_fast(h), h); }
+__device__ __forceinline__ float silu_fast(float z) { return silu_h(0.5f * z); }
 __device__ __forceinline__ float dsilu_fast(float z) {
   const float s = sigm_fast(z);
   return s * fmaf(z, 1.f - s, 1.f);
 }
+__device__ __forceinline__ float2 silu_fast2(float z0, float z1) { return make_float2(silu_fast(z0), silu_fast(z1)); }
 
 __device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<unsigned*>(&v);
 }
+__device__ __forceinline__ unsigned pack_bf16x2(float2 v) { return pack_bf16x2(v.x, v.y); }
 
 // D += A(16x16, row) * B(16x8, col), BF16 in, FP32 accumulate.
 __device__ __forceinline__ void mma_bf16_16816(float d[4], const unsigned a[4], unsigned b0, unsigned b1) {

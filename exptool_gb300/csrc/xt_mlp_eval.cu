@@ -12,9 +12,9 @@
 // 16-column slice), and only the weights live in shared memory (ldmatrix).
 //
 // Pass 2 (k_learned_eval, FP32 CUDA cores): per point, the analytic
-// Hernquist-Ostriker prior contracted with c*s, plus the pass-1 residuals,
-// assembled with the associated Legendre functions and cos/sin(m phi) as in
-// spheresl.all_eval (spheresl.py:987-1102).  Points in radius bands marked
+// Hernquist-Ostriker prior contracted with c*s (unless pass 1 added it),
+// plus the pass-1 sums, assembled with the associated Legendre functions and
+// cos/sin(m phi) as in spheresl.all_eval (spheresl.py:987-1102).  Points in radius bands marked
 // for the table fall back to FP32 table interpolation of the coefficient-
 // contracted field (the mixed-precision table path).
 #include <cmath>
@@ -134,10 +134,10 @@ __device__ __forceinline__ void hidden_layer(unsigned (&A)[8][4], const __nv_bfl
   for (int kk = 0; kk < 8; ++kk) {
     const int c0 = 16 * kk + 2 * tq, c1 = c0 + 8;
     const float p0 = bias[c0], p1 = bias[c0 + 1], p2 = bias[c1], p3 = bias[c1 + 1];
-    A[kk][0] = pack_bf16x2(silu_fast(acc[2 * kk][0] + p0), silu_fast(acc[2 * kk][1] + p1));
-    A[kk][1] = pack_bf16x2(silu_fast(acc[2 * kk][2] + p0), silu_fast(acc[2 * kk][3] + p1));
-    A[kk][2] = pack_bf16x2(silu_fast(acc[2 * kk + 1][0] + p2), silu_fast(acc[2 * kk + 1][1] + p3));
-    A[kk][3] = pack_bf16x2(silu_fast(acc[2 * kk + 1][2] + p2), silu_fast(acc[2 * kk + 1][3] + p3));
+    A[kk][0] = pack_bf16x2(silu_fast2(acc[2 * kk][0] + p0, acc[2 * kk][1] + p1));
+    A[kk][1] = pack_bf16x2(silu_fast2(acc[2 * kk][2] + p0, acc[2 * kk][3] + p1));
+    A[kk][2] = pack_bf16x2(silu_fast2(acc[2 * kk + 1][0] + p2, acc[2 * kk + 1][1] + p3));
+    A[kk][3] = pack_bf16x2(silu_fast2(acc[2 * kk + 1][2] + p2, acc[2 * kk + 1][3] + p3));
   }
 }
 
@@ -213,10 +213,10 @@ __global__ void __launch_bounds__(RAD_WARPS * 32, 2) k_mlp_radial(RadialArgs a) 
 #pragma unroll
     for (int kk = 0; kk < 8; ++kk) {
       const int c = 16 * kk + 2 * tq, d = c + 8;
-      A[kk][0] = pack_bf16x2(silu_fast(fmaf(t0, w1[c], b1[c])), silu_fast(fmaf(t0, w1[c + 1], b1[c + 1])));
-      A[kk][1] = pack_bf16x2(silu_fast(fmaf(t1, w1[c], b1[c])), silu_fast(fmaf(t1, w1[c + 1], b1[c + 1])));
-      A[kk][2] = pack_bf16x2(silu_fast(fmaf(t0, w1[d], b1[d])), silu_fast(fmaf(t0, w1[d + 1], b1[d + 1])));
-      A[kk][3] = pack_bf16x2(silu_fast(fmaf(t1, w1[d], b1[d])), silu_fast(fmaf(t1, w1[d + 1], b1[d + 1])));
+      A[kk][0] = pack_bf16x2(silu_fast2(fmaf(t0, w1[c], b1[c]), fmaf(t0, w1[c + 1], b1[c + 1])));
+      A[kk][1] = pack_bf16x2(silu_fast2(fmaf(t1, w1[c], b1[c]), fmaf(t1, w1[c + 1], b1[c + 1])));
+      A[kk][2] = pack_bf16x2(silu_fast2(fmaf(t0, w1[d], b1[d]), fmaf(t0, w1[d + 1], b1[d + 1])));
+      A[kk][3] = pack_bf16x2(silu_fast2(fmaf(t1, w1[d], b1[d]), fmaf(t1, w1[d + 1], b1[d + 1])));
     }
     hidden_layer(A, W2s, b2, lane);
     hidden_layer(A, W3s, b3, lane);
@@ -253,15 +253,16 @@ __global__ void __launch_bounds__(RAD_WARPS * 32, 2) k_mlp_radial(RadialArgs a) 
 
 struct LearnArgs {
   SphTab<float> T;
-  const float* GH;          // FP32 coefficient-contracted table field [numr][nrow][2]
+  const float* GH;          // FP32 coefficient-contracted table field (SphFieldLayout<float>)
   const float* CS;          // [nrow][K] c * scale * s
-  const float* R;           // pass-1 residual sums [n][rstride]
+  const float* R;           // pass-1 sums [n][rstride]
   int rstride, K, lmax, no_odd;
   float a_inv, rmin, rmax, lnr0, inv_bw;
   int nb;
   const float4* xyzw;
   long long n;
   float4* out;              // pot, dpot/dr, dpot/dcos(theta), dpot/dphi
+  int prior_in_R;           // pass 1 already added the prior (tensor-memory engine)
   int band_use[MAX_BANDS];
 };
 
@@ -313,15 +314,17 @@ __global__ void __launch_bounds__(256) k_learned_eval(LearnArgs a) {
           pv[rr] = w.x;
           dv[rr] = w.y;
         }
-        const float* cs = CS + loff * a.K;
-        ho_radial<float>(u, l, a.K, inv_n, [&](int n, float ho, float uho) {
+        if (!a.prior_in_R) {
+          const float* cs = CS + loff * a.K;
+          ho_radial<float>(u, l, a.K, inv_n, [&](int n, float ho, float uho) {
 #pragma unroll
-          for (int rr = 0; rr < 2 * l + 1; ++rr) {
-            const float c = cs[rr * a.K + n];
-            pv[rr] = fmaf(c, ho, pv[rr]);
-            dv[rr] = fmaf(c, uho, dv[rr]);
-          }
-        });
+            for (int rr = 0; rr < 2 * l + 1; ++rr) {
+              const float c = cs[rr * a.K + n];
+              pv[rr] = fmaf(c, ho, pv[rr]);
+              dv[rr] = fmaf(c, uho, dv[rr]);
+            }
+          });
+        }
 #pragma unroll
         for (int rr = 0; rr < 2 * l + 1; ++rr) dv[rr] *= inv_rc;
       } else {
@@ -369,6 +372,84 @@ static int launch_learned_eval(const LearnArgs& a, size_t shbytes, cudaStream_t 
   return XT_OK;
 }
 
+// Pass 1 for n points into R (rstride floats per point): engine 0 = mma.sync
+// warp tiles (k_mlp_radial), 1 = tcgen05 / tensor memory (k_mlp_radial_tc).
+static int radial_pass(const SphTab<double>& T, MlpHandle* h, const void* prep, int K, double a_prior, double c0,
+                       double c1, const int* band_use, int nbands, const float* xyzw, long long n, int engine,
+                       float* R, cudaStream_t st) {
+  const PrepLayout pl = prep_layout(h->L, K);
+  const char* pb = static_cast<const char*>(prep);
+  const float lnr0 = (float)T.lo, inv_bw = (float)(nbands / (T.hi - T.lo));
+  const float rmin = (float)exp((double)T.lo), rmax = (float)exp((double)T.hi);
+  bool any_net = false;
+  for (int b = 0; b < nbands; ++b) any_net = any_net || band_use[b] != 0;
+  if (!any_net || n == 0) return XT_OK;
+  int nsm = 152, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (engine == 1) {
+    TcArgs ta{};
+    ta.xyzw = reinterpret_cast<const float4*>(xyzw);
+    ta.n = n;
+    ta.wb = h->wb;
+    ta.params = h->params;
+    ta.psize = h->psize;
+    ta.L = h->L;
+    ta.w4h = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4h);
+    ta.w4l = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4l);
+    ta.b4c = reinterpret_cast<const float*>(pb + pl.b4c);
+    ta.c0 = (float)c0;
+    ta.c1 = (float)c1;
+    ta.rmin = rmin;
+    ta.rmax = rmax;
+    ta.lnr0 = lnr0;
+    ta.inv_bw = inv_bw;
+    ta.nb = nbands;
+    ta.R = R;
+    ta.rstride = r_stride(T.lmax);
+    for (int b = 0; b < nbands; ++b) ta.band_use[b] = band_use[b] != 0;
+    ta.CS = nullptr;          // prior in the second pass (faster than in this pass's epilogue)
+    ta.K = K;
+    ta.a_inv = (float)(1.0 / a_prior);
+    int rc = tc_error_flag(&ta.err);
+    if (rc) return rc;
+    return launch_mlp_radial_tc(ta, nsm, st);
+  }
+  RadialArgs ra{};
+  ra.xyzw = reinterpret_cast<const float4*>(xyzw);
+  ra.n = n;
+  ra.wb = h->wb;
+  ra.params = h->params;
+  ra.psize = h->psize;
+  ra.w4h = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4h);
+  ra.w4l = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4l);
+  ra.b4c = reinterpret_cast<const float*>(pb + pl.b4c);
+  ra.c0 = (float)c0;
+  ra.c1 = (float)c1;
+  ra.rmin = rmin;
+  ra.rmax = rmax;
+  for (int b = 0; b < nbands; ++b) ra.band_use[b] = band_use[b] != 0;
+  ra.lnr0 = lnr0;
+  ra.inv_bw = inv_bw;
+  ra.nb = nbands;
+  ra.R = R;
+  ra.rstride = r_stride(T.lmax);
+  const size_t rad_smem = (size_t)(2 * HID + 2 * NC) * WPAD * 2 + (4 * HID + NC) * 4;
+  static bool attr_set = false;
+  if (!attr_set) {
+    XT_CUDA(cudaFuncSetAttribute(k_mlp_radial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_smem));
+    attr_set = true;
+  }
+  const long long ntile = (n + 15) / 16;
+  long long gx = (2LL * nsm + h->L - 1) / h->L;
+  const long long gmax = (ntile + RAD_WARPS - 1) / RAD_WARPS;
+  if (gx > gmax) gx = gmax;
+  if (gx < 1) gx = 1;
+  k_mlp_radial<<<dim3((unsigned)gx, h->L), RAD_WARPS * 32, rad_smem, st>>>(ra);
+  XT_CHECK_LAUNCH("k_mlp_radial");
+  return XT_OK;
+}
+
 }  // namespace xt
 
 using namespace xt;
@@ -413,7 +494,7 @@ size_t xt_learned_eval_workspace(void* sph, long long n) {
 
 int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* prep, int K, double a_prior, double c0,
                     double c1, const int* band_use, int nbands, const float* xyzw, long long n, int no_odd,
-                    float* out, void* workspace, size_t workspace_bytes, void* stream) {
+                    int engine, float* out, void* workspace, size_t workspace_bytes, void* stream) {
   SphTab<double> T;
   SphTab<float> Tf;
   XT_REQUIRE(sph_tabs(sph, &T, &Tf), "NULL SL table handle");
@@ -438,55 +519,17 @@ int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* pre
   const char* pb = static_cast<const char*>(prep);
   const float lnr0 = (float)T.lo, inv_bw = (float)(nbands / (T.hi - T.lo));
   const float rmin = (float)exp((double)T.lo), rmax = (float)exp((double)T.hi);
-
-  RadialArgs ra{};
-  ra.xyzw = reinterpret_cast<const float4*>(xyzw);
-  ra.n = n;
-  ra.wb = h->wb;
-  ra.params = h->params;
-  ra.psize = h->psize;
-  ra.w4h = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4h);
-  ra.w4l = reinterpret_cast<const __nv_bfloat16*>(pb + pl.w4l);
-  ra.b4c = reinterpret_cast<const float*>(pb + pl.b4c);
-  ra.c0 = (float)c0;
-  ra.c1 = (float)c1;
-  ra.rmin = rmin;
-  ra.rmax = rmax;
-  bool any_net = false;
-  for (int b = 0; b < nbands; ++b) {
-    ra.band_use[b] = band_use[b] != 0;
-    any_net = any_net || ra.band_use[b];
-  }
-  ra.lnr0 = lnr0;
-  ra.inv_bw = inv_bw;
-  ra.nb = nbands;
-  ra.R = static_cast<float*>(workspace);
-  ra.rstride = r_stride(T.lmax);
-  const size_t rad_smem = (size_t)(2 * HID + 2 * NC) * WPAD * 2 + (4 * HID + NC) * 4;
-  static bool attr_set = false;
-  if (!attr_set) {
-    XT_CUDA(cudaFuncSetAttribute(k_mlp_radial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_smem));
-    attr_set = true;
-  }
-  int nsm = 152, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long long ntile = (n + 15) / 16;
-  long long gx = (2LL * nsm + h->L - 1) / h->L;
-  const long long gmax = (ntile + RAD_WARPS - 1) / RAD_WARPS;
-  if (gx > gmax) gx = gmax;
-  if (gx < 1) gx = 1;
-  if (any_net) {
-    k_mlp_radial<<<dim3((unsigned)gx, h->L), RAD_WARPS * 32, rad_smem, st>>>(ra);
-    XT_CHECK_LAUNCH("k_mlp_radial");
-  }
+  XT_REQUIRE(engine == 0 || engine == 1, "engine: 0 mma.sync, 1 tcgen05");
+  int rc = radial_pass(T, h, prep, K, a_prior, c0, c1, band_use, nbands, xyzw, n, engine,
+                       static_cast<float*>(workspace), st);
+  if (rc) return rc;
 
   LearnArgs la{};
   la.T = Tf;
   la.GH = static_cast<const float*>(field_f32);
   la.CS = reinterpret_cast<const float*>(pb + pl.cs);
-  la.R = ra.R;
-  la.rstride = ra.rstride;
+  la.R = static_cast<const float*>(workspace);
+  la.rstride = r_stride(T.lmax);
   la.K = K;
   la.lmax = T.lmax;
   la.no_odd = no_odd;
@@ -495,15 +538,48 @@ int xt_learned_eval(void* sph, const void* field_f32, void* mlp, const void* pre
   la.rmax = rmax;
   la.lnr0 = lnr0;
   la.inv_bw = inv_bw;
-  for (int b = 0; b < nbands; ++b) la.band_use[b] = ra.band_use[b];
+  for (int b = 0; b < nbands; ++b) la.band_use[b] = band_use[b] != 0;
   la.nb = nbands;
-  la.xyzw = ra.xyzw;
+  la.xyzw = reinterpret_cast<const float4*>(xyzw);
   la.n = n;
   la.out = reinterpret_cast<float4*>(out);
+  la.prior_in_R = 0;
   const size_t sh = ((size_t)(T.lmax + 1) * (T.lmax + 1) * K + MLP_KMAX) * 4;
   if (T.lmax <= 4) return launch_learned_eval<4>(la, sh, st);
   if (T.lmax <= 6) return launch_learned_eval<6>(la, sh, st);
   return launch_learned_eval<7>(la, sh, st);
+}
+
+int xt_learned_radial_pass(void* sph, void* mlp, const void* prep, int K, double a_prior, double c0, double c1,
+                           const int* band_use, int nbands, const float* xyzw, long long n, int engine, float* R,
+                           void* stream) {
+  SphTab<double> T;
+  XT_REQUIRE(sph_tabs(sph, &T, nullptr), "NULL SL table handle");
+  MlpHandle* h = nullptr;
+  XT_REQUIRE(mlp_view(mlp, &h), "NULL network handle");
+  XT_REQUIRE(T.cmap == 2 && h->L == T.lmax + 1 && h->nout == 2 * K && K <= T.nmax, "network / table / K mismatch");
+  XT_REQUIRE(prep && band_use && xyzw && R && n >= 0, "NULL argument");
+  XT_REQUIRE(nbands >= 1 && nbands <= MAX_BANDS, "need 1 <= nbands <= %d", MAX_BANDS);
+  XT_REQUIRE(engine == 0 || engine == 1, "engine: 0 mma.sync, 1 tcgen05");
+  XT_REQUIRE((reinterpret_cast<uintptr_t>(xyzw) & 15) == 0, "xyzw must be a 16-byte aligned float4 array");
+  XT_REQUIRE(a_prior > 0.0, "prior scale must be positive");
+  return radial_pass(T, h, prep, K, a_prior, c0, c1, band_use, nbands, xyzw, n, engine, R, as_stream(stream));
+}
+
+int xt_learned_status(void) {
+  int* d = nullptr;
+  int rc = tc_error_flag(&d);
+  if (rc) return rc;
+  int v = 0;
+  XT_CUDA(cudaDeviceSynchronize());
+  XT_CUDA(cudaMemcpy(&v, d, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    const int zero = 0;
+    XT_CUDA(cudaMemcpy(d, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    set_error("tensor-memory network pass: an MMA completion wait timed out");
+    return XT_ERR_DEVICE;
+  }
+  return XT_OK;
 }
 
 }  // extern "C"

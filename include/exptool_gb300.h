@@ -247,7 +247,18 @@ int xt_learned_prepare(void *sph, void *mlp, int K, const double *expcoef, doubl
 size_t xt_learned_eval_workspace(void *sph, long long n);
 int xt_learned_eval(void *sph, const void *field_f32, void *mlp, const void *prep, int K, double a_prior, double c0,
                     double c1, const int *band_use, int nbands, const float *xyzw, long long n, int no_odd,
-                    float *out, void *workspace, size_t workspace_bytes, void *stream);
+                    int engine, float *out, void *workspace, size_t workspace_bytes, void *stream);
+/* engine selects the network pass: 0 = mma.sync warp tiles, 1 = tcgen05 with
+ * accumulators in tensor memory.  The network pass alone (for comparisons):
+ * R[n][rstride] with rstride = 2 (lmax+1)^2 rounded up to a multiple of 4;
+ * row p holds, for every coefficient row, the folded network sums (potential,
+ * r d/dr) of points in network bands. */
+int xt_learned_radial_pass(void *sph, void *mlp, const void *prep, int K, double a_prior, double c0, double c1,
+                           const int *band_use, int nbands, const float *xyzw, long long n, int engine, float *R,
+                           void *stream);
+/* Synchronises, then reports (and clears) a tensor-memory pass that gave up
+ * waiting for its MMAs: XT_ERR_DEVICE, else XT_OK. */
+int xt_learned_status(void);
 
 #ifdef __cplusplus
 }

@@ -152,3 +152,37 @@ def test_learned_eval_matches_oracle_and_fallback_matches_table():
     for row in rep["bands"]:
         if row.get("count", 0) and row["use_net"]:
             assert row["net_median"] <= 1e-5
+
+
+def test_tensor_memory_pass_matches_mma_pass():
+    """The two network-pass engines (tcgen05 with the prior folded into its
+    epilogue; mma.sync with the prior in the second pass) give the same
+    potential and forces: same BF16 operands and rounding points, different
+    accumulation order inside the tensor cores."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.tables.samplers import hernquist_sample
+    from oracle.sl import compute_coefficients_solitary
+    lb = _basis(seed=4)
+    lb.fit_scales(n=4096)
+    lb.train(n_train=16384, seed=4, batch=2048, steps=50, lr=1e-3, lr_final=1e-4, log_every=0)
+    tab = _otable()
+    x, y, z, m = hernquist_sample(5000, seed=13)
+    lb.prepare(compute_coefficients_solitary(x, y, z, m, tab))
+    ones = np.ones(lb.nbands, np.int32)
+    for n in (300, 4096 + 77):
+        px, py, pz, _ = hernquist_sample(n, seed=14)
+        xyzw = torch.zeros((n, 4), dtype=torch.float32)
+        xyzw[:, 0], xyzw[:, 1], xyzw[:, 2] = (torch.from_numpy(a.astype(np.float32)) for a in (px, py, pz))
+        xyzw = xyzw.to(dev.device())
+        out_a = dev.to_host(lb.eval(xyzw, band_use=ones, engine="mma")).astype(np.float64)
+        out_b = dev.to_host(lb.eval(xyzw, band_use=ones, engine="tc")).astype(np.float64)
+        lb.status()
+        r = np.sqrt(px * px + py * py + pz * pz)
+        costh = pz / r
+        ga = lb.grad_components(out_a.T, r, costh)
+        gb = lb.grad_components(out_b.T, r, costh)
+        e = np.linalg.norm(ga - gb, axis=1) / np.linalg.norm(ga, axis=1)
+        assert np.median(e) <= 1e-5 and np.max(e) <= 1e-3, (np.median(e), np.max(e))
+        pe = np.abs(out_a[:, 0] - out_b[:, 0]) / np.abs(out_a[:, 0])
+        assert np.median(pe) <= 1e-6 and np.max(pe) <= 1e-4, (np.median(pe), np.max(pe))
