@@ -65,7 +65,7 @@ _SIGS = {
     "xt_fields_forces": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp,
                                  c_dbl, c_ll, c_dpp, c_vp]),
     "xt_leapfrog": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_dpp, c_ll, c_int, c_int,
-                            c_int, c_dbl, c_dbl, c_int, c_int, c_vp, c_vp]),
+                            c_int, c_dbl, c_dbl, c_int, c_int, c_vp, c_vp, c_vp]),
     "xt_mlp_param_size": (c_int, []),
     "xt_mlp_create": (c_int, [c_int, c_int, c_vp, ctypes.POINTER(c_vp)]),
     "xt_mlp_destroy": (c_int, [c_vp]),

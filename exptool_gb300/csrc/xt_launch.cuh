@@ -21,6 +21,7 @@ struct OrbitArgs {
   int step0, nsteps, nint, apse, ap_max;
   double dt, rotc;
   double* traj;
+  const double* dts;          // per-orbit step sizes (NULL: dt for all)
 };
 
 template <typename R, int LC>

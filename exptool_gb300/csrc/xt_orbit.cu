@@ -53,7 +53,8 @@ int xt_fields_forces(void* sph, const void* sph_field, void* cyl, const void* cy
 
 int xt_leapfrog(void* sph, const void* sph_field, void* cyl, const void* cyl_field, int precision, int halo_l,
                 int disk_m, int no_odd, int trig_l, double* const* state, long long n, int step0, int nsteps,
-                int nint, double dt, double rotc, int apse, int ap_max, double* traj, void* stream) {
+                int nint, double dt, double rotc, int apse, int ap_max, double* traj, const double* dts,
+                void* stream) {
   SphTab<double> sd; SphTab<float> sf; CylTab<double> cd; CylTab<float> cf;
   XT_REQUIRE(sph_tabs(sph, &sd, &sf) && cyl_tabs(cyl, &cd, &cf), "NULL table handle");
   XT_REQUIRE(sph_field && cyl_field && state, "NULL field or state");
@@ -67,7 +68,7 @@ int xt_leapfrog(void* sph, const void* sph_field, void* cyl, const void* cyl_fie
   OrbitArgs A;
   for (int k = 0; k < S_COUNT; ++k) A.s[k] = state[k];
   A.n = n; A.step0 = step0; A.nsteps = nsteps; A.nint = nint; A.apse = apse; A.ap_max = ap_max;
-  A.dt = dt; A.rotc = rotc; A.traj = traj;
+  A.dt = dt; A.rotc = rotc; A.traj = traj; A.dts = dts;
   cudaStream_t st = as_stream(stream);
   const int grid = grid_for(n, 128, 8);
   int rc = with_lcap(sd.lmax, [&](auto lc) {

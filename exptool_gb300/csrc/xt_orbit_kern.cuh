@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(128) k_leapfrog(SphTab<R> ST, const R* __restr
       r2m1 = A.s[S_R2M1][p]; r2m2 = A.s[S_R2M2][p]; aps = A.s[S_APS][p];
       nstep = (int)A.s[S_NSTEP][p]; e0 = A.s[S_E0][p]; edev = A.s[S_EDEV][p];
     }
-    const double dt = A.dt, dt2 = A.dt * A.dt;
+    const double dt = A.dts ? A.dts[p] : A.dt, dt2 = dt * dt;
     const int kbeg = A.step0 < 1 ? 1 : A.step0;
     int kend = A.step0 + A.nsteps;
     if (kend > A.nint) kend = A.nint;

@@ -326,12 +326,13 @@ STATE_SLOTS = ("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz", "pot", "r2m1",
 
 
 def leapfrog(sph_field, cyl_field, state, step0, nsteps, nint, dt, rotc=0.0, apse=False, ap_max=1000, traj=None,
-             halo_l=-1, disk_m=-1, no_odd=False, trig_l=True):
-    """Advance orbit ensemble ``state`` (16 x n float64 tensor) in place."""
+             halo_l=-1, disk_m=-1, no_odd=False, trig_l=True, dts=None):
+    """Advance orbit ensemble ``state`` (16 x n float64 tensor) in place;
+    ``dts`` (n float64 CUDA tensor) gives each orbit its own step."""
     lib = _lib.load()
     n = int(state.shape[1])
     pp, keep = _lib.ptr_array([state[k].data_ptr() for k in range(len(STATE_SLOTS))])
     _lib.check(lib.xt_leapfrog(sph_field.table.handle, dptr(sph_field.buf), cyl_field.table.handle,
                                dptr(cyl_field.buf), sph_field.precision, int(halo_l), int(disk_m), int(bool(no_odd)),
                                int(bool(trig_l)), pp, n, int(step0), int(nsteps), int(nint), float(dt), float(rotc),
-                               int(bool(apse)), int(ap_max), dptr(traj), stream_ptr()), "xt_leapfrog")
+                               int(bool(apse)), int(ap_max), dptr(traj), dptr(dts), stream_ptr()), "xt_leapfrog")

@@ -168,3 +168,221 @@ def leapfrog_ensemble(FieldInstance, nint, dt, initpos, initvel, rotfreq=0.0, pr
     ens = Ensemble(FieldInstance, initpos, initvel, nint, dt, rotfreq, precision, chunk, apse, ap_max)
     st = ens.run(graph=graph).cpu().numpy()
     return {k: st[i] for i, k in enumerate(dev.STATE_SLOTS)}
+
+
+# ---------------------------------------------------------------- orbit grids
+def compute_timesteps(FieldInstance, start_pos, start_vel, dyn_res=100.):
+    """compute_timestep for many starting points in one force call: (n,)
+    step sizes, elementwise the reference's criteria (integrate.py:217-272)."""
+    eps = 1.0e-10
+    pos = np.atleast_2d(np.asarray(start_pos, dtype=np.float64))
+    vel = np.atleast_2d(np.asarray(start_vel, dtype=np.float64))
+    vtot = np.sum(vel ** 2., axis=1) ** 0.5 + eps
+    dfx, hfx, dfy, hfy, dfz, hfz, dp, hp = (np.asarray(v) for v in
+                                            FieldInstance.return_forces_cart(pos[:, 0], pos[:, 1], pos[:, 2]))
+    acc = np.stack([dfx + hfx, dfy + hfy, dfz * hfz], axis=1)
+    dtr = np.sum(pos * acc, axis=1)
+    atot = np.sum(acc ** 2., axis=1) ** 0.5 + eps
+    ptot = np.abs(dp + hp)
+    crit = np.stack([1.0 / np.sqrt(vtot + eps), np.sqrt(vtot / (atot + eps)), ptot / (np.abs(dtr) + eps),
+                     np.sqrt(ptot / (atot * atot + eps))], axis=1)
+    return np.min(crit, axis=1) / dyn_res
+
+
+def _grid_orbits(F, pos, vel, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max):
+    """All orbits of a grid in one launch, each with the step
+    max(compute_timestep, dt): trajectories (n, nint, 10), steps taken (n,),
+    step sizes (n,)."""
+    # the reference computes each orbit's step before its leapfrog_integrate
+    # call sets the field parameters, so the first orbit's step uses the
+    # parameters the instance had on entry
+    dt0 = compute_timesteps(F, pos[:1], vel[:1], dyn_res=dyn_res)
+    F.set_field_parameters(no_odd=no_odd, halo_l=halo_l, disk_m=disk_m)
+    rest = compute_timesteps(F, pos[1:], vel[1:], dyn_res=dyn_res) if pos.shape[0] > 1 else np.zeros(0)
+    dts = np.maximum(np.concatenate([dt0, rest]), dt)
+    sf, cf = F.device_fields()
+    nint = int(nint)
+    state = _new_state(pos, vel)
+    n = state.shape[1]
+    traj = torch.zeros((n, nint, 10), dtype=torch.float64, device=state.device)
+    dev.leapfrog(sf, cf, state, 0, nint, nint, 0.0, rotc=2.0 * np.pi * rotfreq, apse=False, ap_max=ap_max,
+                 traj=traj, halo_l=F._halo_l(), disk_m=F._disk_m(), no_odd=F.no_odd, trig_l=not F.halo_correct_m,
+                 dts=dev.to_dev(dts))
+    return dev.to_host(traj), dev.to_host(state[13]).astype(np.int64), dts
+
+
+def _orbit_rows(tr, nstep, dtime, nint, rotfreq, keys):
+    """Rows of one orbit in the integrate_grid layout, zero-padded to nint:
+    the Orbits fields of leapfrog_integrate (integrate.py:163-188)."""
+    times = np.arange(0, nint, 1) * dtime
+    barpos = 2.0 * np.pi * rotfreq * times[:nstep]
+    X, Y = tr[:nstep, 0], tr[:nstep, 1]
+    VX, VY = tr[:nstep, 3], tr[:nstep, 4]
+    if np.min(barpos) < 0.0:
+        TX, TY = transform(X, Y, barpos)
+    else:
+        TX, TY = clock_transform(X, Y, barpos)
+    val = {"X": X, "Y": Y, "Z": tr[:nstep, 2], "TX": TX, "TY": TY, "VX": VX, "VY": VY, "VZ": tr[:nstep, 5],
+           "T": times[:nstep]}
+    out = np.zeros((len(keys), nint))
+    for i, k in enumerate(keys):
+        out[i, :nstep] = val[k]
+    return out
+
+
+_KEYS_2D = ("X", "Y", "TX", "TY", "VX", "VY", "T")
+_KEYS_3D = ("X", "Y", "Z", "TX", "TY", "VX", "VY", "VZ", "T")
+
+
+def integrate_grid(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, verbose):
+    """integrate.integrate_grid (integrate.py:848-884): orbits launched from
+    (rad, 0, 0) with velocity (0, vel, 0), step max(compute_timestep, dt);
+    array [rads, vels, 7 (X Y TX TY VX VY T), nint].  All orbits in one launch."""
+    rads, vels = np.asarray(rads, dtype=np.float64), np.asarray(vels, dtype=np.float64)
+    R, V = np.meshgrid(rads, vels, indexing="ij")
+    pos = np.stack([R.ravel(), np.zeros(R.size), np.zeros(R.size)], axis=1)
+    vel = np.stack([np.zeros(R.size), V.ravel(), np.zeros(R.size)], axis=1)
+    return _grid(F, pos, vel, (rads.size, vels.size), nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max,
+                 _KEYS_2D)
+
+
+def integrate_grid_launchy(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, verbose):
+    """integrate.integrate_grid_launchy (integrate.py:886-922): launched from
+    (0, rad, 0) with velocity (0, vel, 0)."""
+    rads, vels = np.asarray(rads, dtype=np.float64), np.asarray(vels, dtype=np.float64)
+    R, V = np.meshgrid(rads, vels, indexing="ij")
+    pos = np.stack([np.zeros(R.size), R.ravel(), np.zeros(R.size)], axis=1)
+    vel = np.stack([np.zeros(R.size), V.ravel(), np.zeros(R.size)], axis=1)
+    return _grid(F, pos, vel, (rads.size, vels.size), nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max,
+                 _KEYS_2D)
+
+
+def _grid3(rads, vels, zs, vzs, launch):
+    G = np.meshgrid(np.asarray(rads, dtype=np.float64), np.asarray(vels, dtype=np.float64),
+                    np.asarray(zs, dtype=np.float64), np.asarray(vzs, dtype=np.float64), indexing="ij")
+    R, V, Z, VZ = (g.ravel() for g in G)
+    zero = np.zeros(R.size)
+    pos = np.stack([R, zero, Z] if launch == "x" else [zero, R, Z], axis=1)
+    vel = np.stack([zero, V, VZ], axis=1)
+    return pos, vel, G[0].shape
+
+
+def integrate_grid_3D(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, zs, vzs, verbose):
+    """integrate.integrate_grid_3D (integrate.py:760-802): launched from
+    (rad, 0, z) with velocity (0, vel, vz); array [rads, vels, zs, vzs, 9
+    (X Y Z TX TY VX VY VZ T), nint]."""
+    if zs is None or vzs is None:
+        print('ERROR: 3D orbit specified, but no z or vz values passed!')
+        return None
+    pos, vel, shape = _grid3(rads, vels, zs, vzs, "x")
+    return _grid(F, pos, vel, shape, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, _KEYS_3D)
+
+
+def integrate_grid_3D_launchy(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, zs, vzs,
+                              verbose):
+    """integrate.integrate_grid_3D_launchy (integrate.py:804-846): launched
+    from (0, rad, z)."""
+    if zs is None or vzs is None:
+        print('ERROR: 3D orbit specified, but no z or vz values passed!')
+        return None
+    pos, vel, shape = _grid3(rads, vels, zs, vzs, "y")
+    return _grid(F, pos, vel, shape, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, _KEYS_3D)
+
+
+def _grid(F, pos, vel, shape, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, keys):
+    nint = int(nint)
+    tr, nstep, dts = _grid_orbits(F, pos, vel, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max)
+    out = np.zeros((pos.shape[0], len(keys), nint))
+    for i in range(pos.shape[0]):
+        out[i] = _orbit_rows(tr[i], int(nstep[i]), dts[i], nint, rotfreq, keys)
+    return out.reshape(tuple(shape) + (len(keys), nint))
+
+
+def redistribute_arrays(rads, divisions):
+    """integrate.redistribute_arrays (integrate.py:440-466): split rads into
+    `divisions` contiguous chunks."""
+    return np.array_split(np.asarray(rads), divisions)
+
+
+def re_form_orbit_arrays(array):
+    """integrate.re_form_orbit_arrays (integrate.py:469-487): concatenate
+    per-chunk grids along the radius axis as float32."""
+    return np.concatenate([np.asarray(a) for a in array], axis=0).astype("f4")
+
+
+def re_form_orbit_arrays_3D(array):
+    """integrate.re_form_orbit_arrays_3D (integrate.py:490-509)."""
+    return re_form_orbit_arrays(array)
+
+
+def do_integrate_multi(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, verbose=0,
+                       nprocs=-1, threedee=False, zs=None, vzs=None, launch='x'):
+    """integrate.do_integrate_multi (integrate.py:290-335): the whole grid in
+    one GPU launch (nprocs is accepted and unused); float32 orbit array as
+    the reference's re_form_orbit_arrays returns."""
+    if threedee:
+        if (zs is None) or (vzs is None):
+            print('ERROR: 3D orbit specified, but no z or vz values passed!')
+            return None
+        fn = integrate_grid_3D if launch == 'x' else integrate_grid_3D_launchy
+        arr = fn(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, zs, vzs, verbose)
+        return re_form_orbit_arrays_3D([arr])
+    fn = integrate_grid if launch == 'x' else integrate_grid_launchy
+    arr = fn(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, disk_m, dyn_res, ap_max, verbose)
+    return re_form_orbit_arrays([arr])
+
+
+# ---------------------------------------------------------------- orbit text files
+def _orbit_line(head, rows):
+    """One line as the reference's print calls write it: every token followed
+    by a space, then a newline (integrate.py:513-536)."""
+    toks = [str(v) for v in head]
+    for row in rows:
+        toks.extend(str(v) for v in row)
+    return "".join(t + " " for t in toks) + "\n"
+
+
+def print_orbit_array(f, OrbitArray):
+    """integrate.print_orbit_array (integrate.py:513-536): per orbit, nsteps,
+    R_0, V_0, dT, then the X, Y, TX, TY, VX, VY rows."""
+    nsteps = OrbitArray.shape[-1]
+    for rad in range(0, OrbitArray.shape[0]):
+        for vel in range(0, OrbitArray.shape[1]):
+            O = OrbitArray[rad, vel]
+            f.write(_orbit_line((nsteps, O[0, 0], O[5, 0], O[-1, 1]), [O[k] for k in range(6)]))
+
+
+def print_orbit_array_3D(f, OrbitArray):
+    """integrate.print_orbit_array_3D (integrate.py:539-568)."""
+    nsteps = OrbitArray.shape[-1]
+    for rad in range(0, OrbitArray.shape[0]):
+        for vel in range(0, OrbitArray.shape[1]):
+            for z in range(0, OrbitArray.shape[2]):
+                for vz in range(0, OrbitArray.shape[3]):
+                    O = OrbitArray[rad, vel, z, vz]
+                    f.write(_orbit_line((nsteps, O[0, 0], O[6, 0], O[2, 0], O[7, 0], O[-1, 1]),
+                                        [O[k] for k in range(8)]))
+
+
+def _read_lines(infile, head, keys):
+    D = {k: {} for k in head + keys}
+    with open(infile, "r") as f:
+        for linenum, line in enumerate(f):
+            d = [float(q) for q in line.split()]
+            npoints = int(d[0])
+            for i, k in enumerate(head):
+                D[k][linenum] = d[1 + i]
+            o = 1 + len(head)
+            for i, k in enumerate(keys):
+                D[k][linenum] = d[o + i * npoints:o + (i + 1) * npoints]
+    return D
+
+
+def read_integrations(infile):
+    """integrate.read_integrations (integrate.py:970-998)."""
+    return _read_lines(infile, ["R_0", "V_0", "dT"], ["X", "Y", "TX", "TY", "VX", "VY"])
+
+
+def read_integrations_3D(infile):
+    """integrate.read_integrations_3D (integrate.py:1001-1038)."""
+    return _read_lines(infile, ["R_0", "V_0", "Z_0", "VZ_0", "dT"], ["X", "Y", "Z", "TX", "TY", "VX", "VY", "VZ"])

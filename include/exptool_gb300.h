@@ -191,14 +191,16 @@ int xt_fields_forces(void *sph, const void *sph_field, void *cyl, const void *cy
  * for n independent orbits.  state: 16 device arrays of n float64
  * (x y z vx vy vz fx fy fz pot r2m1 r2m2 aps nstep e0 emaxdev) updated in
  * place; steps [step0, step0+nsteps) of a run of nint steps with rotation
- * angle rotc * (k*dt) at step k.  traj (optional, may be NULL): row-major
+ * angle rotc * (k*dt) at step k.  dt_per_orbit (device, may be NULL): a step
+ * size per orbit replacing dt (integrate.integrate_grid gives every orbit its
+ * own compute_timestep step, integrate.py:848-884).  traj (optional, may be NULL): row-major
  * (n, nint, 10) = x y z vx vy vz p fx fy fz of every step.  apse != 0 stops
  * an orbit after ap_max planar apocentres.  The force precision follows
  * `precision` (fields prepared at that precision); kick/drift are FP64. */
 int xt_leapfrog(void *sph, const void *sph_field, void *cyl, const void *cyl_field, int precision,
                 int halo_l, int disk_m, int no_odd, int trig_l, double *const *state, long long n,
                 int step0, int nsteps, int nint, double dt, double rotc, int apse, int ap_max, double *traj,
-                void *stream);
+                const double *dt_per_orbit, void *stream);
 
 /* ------------------------------------------------------------------ learned radial basis
  * No counterpart in the reference: a surrogate for the SL radial tables of

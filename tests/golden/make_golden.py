@@ -11,6 +11,8 @@ Outputs (all small):
   eof_c1.npz, eof_c0.npz      particles, EOF accumulate / evaluate outputs
   fields.npz                  Fields.return_forces_cart, leapfrog_integrate,
                               compute_timestep outputs
+  orbit_grids.npz             integrate_grid / _launchy / _3D arrays and the
+                              print_orbit_array(_3D) text of the reference
   coef_files.npz              bytes of SL / EOF coefficient files written by the
                               reference (two dumps each), the SHA-256 and size of
                               a Fields.save_field file, rotation_curve and
@@ -316,6 +318,38 @@ def coef_files_case(ref, sl_ec, sl_ec2, eof_cos, eof_sin):
     print("coefficient files done")
 
 
+def orbit_grid_case(ref, sph_cache, sph_model, expcoef, eof_path, a_cos, a_sin):
+    """Orbit grids of the reference integrator in the fields_case potential."""
+    import io
+    refshim.set_log_bounds(ref, 1e-3, 100.0)
+    F = ref.potential.Fields("none", eof_path, sph_cache, sph_model, verbose=0)
+    F.EOF = ref.eof.EOF_Object()
+    F.EOF.eof_file, F.EOF.cos, F.EOF.sin = eof_path, a_cos, a_sin
+    F.SL = ref.spheresl.SL_Object()
+    F.SL.sph_file, F.SL.model_file, F.SL.expcoef = sph_cache, sph_model, expcoef
+    F.halofac = 0.8
+    F.prep_tables()
+    out = {}
+    rads, vels = np.array([0.6, 1.4]), np.array([0.45, 0.7])
+    # dt = 1e-4 is below every compute_timestep step, so each orbit keeps its own
+    g = ref.integrate.integrate_grid(rads, vels, F, 30, 1e-4, 0.15, False, -1, -1, 100., 1000, 0)
+    out["grid"] = g
+    F.reset_field_parameters()
+    out["grid_launchy"] = ref.integrate.integrate_grid_launchy(rads, vels, F, 25, 0.01, -0.2, True, 2, 2, 50., 1000, 0)
+    F.reset_field_parameters()
+    out["grid_3d"] = ref.integrate.integrate_grid_3D(np.array([1.0]), np.array([0.5, 0.6]), F, 20, 1e-4, 0.0,
+                                                     False, -1, -1, 100., 1000, np.array([0.05, -0.1]),
+                                                     np.array([0.02]), 0)
+    buf = io.StringIO()
+    ref.integrate.print_orbit_array(buf, g)
+    out["grid_text"] = np.array(buf.getvalue())
+    buf = io.StringIO()
+    ref.integrate.print_orbit_array_3D(buf, out["grid_3d"])
+    out["grid_3d_text"] = np.array(buf.getvalue())
+    np.savez_compressed(P("orbit_grids.npz"), **out)
+    print("orbit grids done")
+
+
 def main():
     ref = refshim.load()
     sl_out = {}
@@ -327,6 +361,7 @@ def main():
     fields_case(ref, cache, modelf, ec, eof_path, a_cos, a_sin)
     ec2 = np.load(P("sl_c2.npz"))["expcoef_noodd"]
     coef_files_case(ref, ec, ec2, a_cos, a_sin)
+    orbit_grid_case(ref, cache, modelf, ec, eof_path, a_cos, a_sin)
 
 
 if __name__ == "__main__":
