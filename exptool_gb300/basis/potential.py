@@ -39,19 +39,58 @@ class Fields:
         self._fcache = {}
 
     # ------------------------------------------------------------ coefficients
-    def total_coefficients(self, disk_particles=None, halo_particles=None, halo_total=None):
-        """Accumulate disc (EOF) and halo (SL) coefficients from in-memory
-        particle containers (``.data`` dicts or holders); cf. potential.py:98-252.
-        halofac = len(halo_particles) / halo_total when halo_total is given."""
+    def total_coefficients(self, disk_particles=None, halo_particles=None, halo_total=None, ncenter=10000):
+        """potential.Fields.total_coefficients (potential.py:98-252) on
+        in-memory particle containers (``.data`` dicts or holders) instead of
+        a snapshot file.  halofac = len(halo_particles) / halo_total when
+        halo_total is given (the reference divides the halo count by itself,
+        :139-142, so 1).  With ``centering``: the mass-weighted centre of the
+        ``ncenter`` disc particles nearest the origin (argsort of r) is taken
+        off the disc, and off the halo either the same centre
+        (``mutual_center``) or the centre of the halo particles at those same
+        indices (the reference ranks the disc radii for the halo too,
+        :196-205); then both bases are accumulated on the GPU."""
         if disk_particles is None or halo_particles is None:
             raise ValueError("total_coefficients needs disk_particles and halo_particles (no snapshot reader here)")
+        if self.transform:
+            raise NotImplementedError("transform=True needs the bar transform of exptool.analysis.pattern")
+        from ..io.particle import holder, positions
         self.time = getattr(disk_particles, "time", None)
-        nh = np.asarray(halo_particles.data["m"] if hasattr(halo_particles, "data") else halo_particles.mass).size
-        self.halofac = float(nh) / float(halo_total) if halo_total else 1.0
-        self.xcen_disk = self.ycen_disk = self.zcen_disk = 0.0
-        self.xcen_halo = self.ycen_halo = self.zcen_halo = 0.0
-        self.EOF = eof.compute_coefficients(disk_particles, self.eof_file, verbose=self.verbose, no_odd=self.no_odd)
-        self.SL = spheresl.compute_coefficients(halo_particles, self.sph_file, self.model_file, verbose=self.verbose,
+        dx, dy, dz, dm = positions(disk_particles)
+        hx, hy, hz, hm = positions(halo_particles)
+        self.halofac = float(hm.size) / float(halo_total) if halo_total else 1.0
+        if self.centering:
+            print('potential.Fields.total_coefficients: Computing centering (centering=True)')
+            cp = ((dx * dx + dy * dy + dz * dz) ** 0.5).argsort()[0:ncenter]
+            wd = np.sum(dm[cp])
+            self.xcen_disk = np.sum(dx[cp] * dm[cp]) / wd
+            self.ycen_disk = np.sum(dy[cp] * dm[cp]) / wd
+            self.zcen_disk = np.sum(dz[cp] * dm[cp]) / wd
+            if self.mutual_center:
+                print('potential.Fields.total_coefficients: Using computed disk center for halo (mutual_center=True)')
+                self.xcen_halo, self.ycen_halo, self.zcen_halo = self.xcen_disk, self.ycen_disk, self.zcen_disk
+            else:
+                wh = np.sum(hm[cp])
+                self.xcen_halo = np.sum(hx[cp] * hm[cp]) / wh
+                self.ycen_halo = np.sum(hy[cp] * hm[cp]) / wh
+                self.zcen_halo = np.sum(hz[cp] * hm[cp]) / wh
+            print('potential.Fields.total_coefficients: (x,y,z) = {0:6.5f},{1:6.5f},{2:6.5f}'
+                  .format(float(self.xcen_disk), float(self.ycen_disk), float(self.zcen_disk)))
+        else:
+            self.xcen_disk = self.ycen_disk = self.zcen_disk = 0.
+            self.xcen_halo = self.ycen_halo = self.zcen_halo = 0.
+
+        def shifted(x, y, z, m, cx, cy, cz, src):
+            h = holder()
+            h.xpos, h.ypos, h.zpos, h.mass = x - cx, y - cy, z - cz, m
+            h.time = getattr(src, "time", None)
+            return h
+
+        disk = shifted(dx, dy, dz, dm, self.xcen_disk, self.ycen_disk, self.zcen_disk, disk_particles)
+        halo = shifted(hx, hy, hz, hm, self.xcen_halo, self.ycen_halo, self.zcen_halo, halo_particles)
+        self.centered_particles = (disk, halo)
+        self.EOF = eof.compute_coefficients(disk, self.eof_file, verbose=self.verbose, no_odd=self.no_odd)
+        self.SL = spheresl.compute_coefficients(halo, self.sph_file, self.model_file, verbose=self.verbose,
                                                 no_odd=self.no_odd)
 
     # ------------------------------------------------------------ tables

@@ -13,6 +13,8 @@ Outputs (all small):
                               compute_timestep outputs
   orbit_grids.npz             integrate_grid / _launchy / _3D arrays and the
                               print_orbit_array(_3D) text of the reference
+  centering.npz               Fields.total_coefficients centring (centres and the
+                              centred particles handed to the accumulators)
   coef_files.npz              bytes of SL / EOF coefficient files written by the
                               reference (two dumps each), the SHA-256 and size of
                               a Fields.save_field file, rotation_curve and
@@ -350,6 +352,59 @@ def orbit_grid_case(ref, sph_cache, sph_model, expcoef, eof_path, a_cos, a_sin):
     print("orbit grids done")
 
 
+def centering_case(ref):
+    """Fields.total_coefficients with centring, the snapshot reader replaced
+    by in-memory particles and the two accumulators by recorders of the
+    particles they receive (the coefficient paths are pinned elsewhere)."""
+    rng = np.random.default_rng(41)
+    dx, dy, dz, dm = disc_sample(12000, seed=42)
+    dm = dm * rng.uniform(0.5, 1.5, dm.size)
+    dx, dy, dz = dx + 0.03, dy - 0.02, dz + 0.01          # an off-centre disc
+    hx, hy, hz, hm = hernquist_sample(15000, seed=43)
+    hx = hx - 0.05
+    comps = {"star": Data(dx, dy, dz, dm), "dark": Data(hx, hy, hz, hm)}
+    comps["star"].time = 1.5
+
+    class FakeInput:
+        def __init__(self, filename, comp="star", verbose=0):
+            src = comps[comp]
+            self.data = {k: np.array(v) for k, v in src.data.items()}
+            self.time = src.time
+
+    seen = {}
+
+    def rec_eof(P, eof_file, verbose=0, no_odd=False, **kw):
+        seen["disk"] = np.stack([P.data["x"], P.data["y"], P.data["z"], P.data["m"]])
+        return ref.eof.EOF_Object()
+
+    def rec_sl(P, sph_file, mod_file, verbose=0, no_odd=False):
+        seen["halo"] = np.stack([P.data["x"], P.data["y"], P.data["z"], P.data["m"]])
+        return ref.spheresl.SL_Object()
+
+    pot = ref.potential
+    keep = (pot.particle.Input, pot.eof.compute_coefficients, pot.spheresl.compute_coefficients)
+    out = {}
+    try:
+        pot.particle.Input = FakeInput
+        pot.eof.compute_coefficients = rec_eof
+        pot.spheresl.compute_coefficients = rec_sl
+        for mutual in (False, True):
+            F = pot.Fields("fake", "eof", "sph", "mod", centering=True, mutual_center=mutual, verbose=0)
+            F.total_coefficients()
+            tag = "mutual" if mutual else "separate"
+            out[tag + "_centers"] = np.array([F.xcen_disk, F.ycen_disk, F.zcen_disk, F.xcen_halo, F.ycen_halo,
+                                              F.zcen_halo, F.halofac, F.time])
+            # checksums of the centred particles handed to the accumulators
+            out[tag + "_disk_sums"] = np.array([seen["disk"].sum(axis=1), (seen["disk"] ** 2).sum(axis=1)])
+            out[tag + "_halo_sums"] = np.array([seen["halo"].sum(axis=1), (seen["halo"] ** 2).sum(axis=1)])
+            out[tag + "_disk_first"] = seen["disk"][:, :16]
+            out[tag + "_halo_first"] = seen["halo"][:, :16]
+    finally:
+        pot.particle.Input, pot.eof.compute_coefficients, pot.spheresl.compute_coefficients = keep
+    np.savez_compressed(P("centering.npz"), **out)
+    print("centering done")
+
+
 def main():
     ref = refshim.load()
     sl_out = {}
@@ -362,6 +417,7 @@ def main():
     ec2 = np.load(P("sl_c2.npz"))["expcoef_noodd"]
     coef_files_case(ref, ec, ec2, a_cos, a_sin)
     orbit_grid_case(ref, cache, modelf, ec, eof_path, a_cos, a_sin)
+    centering_case(ref)
 
 
 if __name__ == "__main__":
