@@ -218,9 +218,13 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     are placed at the origin (unless nanblock) for both passes."""
     x, y, z, m = positions(PSPInput)
     table = table_from_file(eof_file)
-    # particles with a NaN coordinate are placed at the origin on the device
-    c, s, outs = table.accumulate_eval(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision, m1=m1, m2=m2,
-                                       nan_to_origin=not nanblock)
+    # inputs and results cross host <-> device as copies enqueued on the
+    # compute stream (asynchronous from pinned arrays) with one final
+    # synchronisation; particles with a NaN coordinate are placed at the
+    # origin on the device
+    c, s, outs = table.accumulate_eval(*(dev.to_dev_async(a) for a in (x, y, z, m)), precision=precision, m1=m1,
+                                       m2=m2, nan_to_origin=not nanblock)
+    host = dev.to_host_many([c, s] + list(outs))
     out = EOF_Object()
     out.time = getattr(PSPInput, "time", None)
     out.filename = getattr(PSPInput, "filename", None)
@@ -229,9 +233,8 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     out.eof_file = eof_file
     out.mmax = table.mmax
     out.nmax = table.norder
-    out.cos = dev.to_host(c)
-    out.sin = dev.to_host(s)
-    return out, tuple(dev.to_host(t) for t in outs)
+    out.cos, out.sin = host[0], host[1]
+    return out, tuple(host[2:])
 
 
 # ---------------------------------------------------------------- evaluation

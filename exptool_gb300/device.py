@@ -46,6 +46,25 @@ def to_dev(a, dtype=torch.float64) -> torch.Tensor:
     return t.contiguous()
 
 
+def to_dev_async(a) -> torch.Tensor:
+    """numpy float64 -> CUDA float64 tensor, enqueued on the current stream
+    without waiting when the source is in pinned memory (the caller keeps the
+    source alive until the stream has passed the copy); pageable sources are
+    copied synchronously by torch."""
+    t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64)))
+    return t.to(device(), non_blocking=True)
+
+
+def to_host_many(ts) -> list:
+    """Several device tensors -> NumPy arrays in pinned host memory: all
+    copies enqueued on the current stream, one synchronisation."""
+    hs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in ts]
+    for h, t in zip(hs, ts):
+        h.copy_(t, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return [h.numpy() for h in hs]
+
+
 def to_host(t: torch.Tensor) -> np.ndarray:
     """Device tensor -> NumPy array in pinned host memory (torch's caching
     host allocator), so the device-to-host copy is a direct DMA; the array
