@@ -309,6 +309,96 @@ __global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* _
   }
 }
 
+// FP64-path record kernel.  The set-up of every particle (R, rho = |(x, y)|,
+// cos/sin phi, the cmap = 1 map, the z map's sign factor, the cell and the
+// in-cell offsets) runs in double-float arithmetic on the FP32 pipe: inputs
+// are split into float pairs with integer operations, and only asinh (and
+// cmap = 2's log) and the returned R use the FP64 pipe.  Results equal the
+// FP64 arithmetic to ~2^-46 relative.  Points outside the range where FP32
+// exponents are safe (|x|, |y|, |z| < 1e15, rho^2 > 1e-30, coordinates 0 or
+// >= 2^-74 in magnitude) take the FP64 arithmetic.
+__device__ __forceinline__ void df_cell(df X, int nmax_cells, float& f, df& off) {
+  float t = floorf(X.h);
+  if (t == X.h && X.l < 0.f) t -= 1.f;                      // X just below an integer
+  if (!(t >= 0.f)) t = 0.f;                                 // negative or NaN
+  if (X.h < 0.f || (X.h == 0.f && X.l < 0.f)) X = {0.f, 0.f};
+  if (t >= (float)nmax_cells) t = (float)(nmax_cells - 1);  // X itself is left unclamped (extrapolation)
+  f = t;
+  off = df_sub(X, {t, 0.f});
+}
+
+__global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, const double* __restrict__ x,
+                                                       const double* __restrict__ y, const double* __restrict__ z,
+                                                       const double* __restrict__ mass, long long n,
+                                                       int* __restrict__ hist, int* __restrict__ cell,
+                                                       int* __restrict__ slot, df* __restrict__ rec,
+                                                       double* __restrict__ Rout, int nan_to_origin) {
+  const df xmin = df_from(T.XMIN), idx = df_from(T.inv_dX), ymin = df_from(T.YMIN), idy = df_from(T.inv_dY);
+  const df ias = df_from(T.inv_ascale), one = {1.f, 0.f}, soft = df_from(1.0e-10), zeps = df_from(1.0e-8);
+  const df m4pi = df_from(-FOUR_PI_C);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    double xx = x[p], yy = y[p], zz = z[p];
+    if (nan_to_origin && (isnan(xx) || isnan(yy) || isnan(zz))) xx = yy = zz = 0.0;
+    bool okx, oky, okz;
+    const df xd = df_split(xx, okx), yd = df_split(yy, oky), zd = df_split(zz, okz);
+    const df s2 = df_add(df_mul(xd, xd), df_mul(yd, yd));
+    const bool safe = okx && oky && okz && fabsf(xd.h) < 1.0e15f && fabsf(yd.h) < 1.0e15f &&
+                      fabsf(zd.h) < 1.0e15f && s2.h > 1.0e-30f;
+    df dx, dy, c1, s1;
+    float fx, fy;
+    if (safe) {
+      const df Rc = df_sqrt(df_add(s2, soft));
+      const df rho = df_sqrt(s2);
+      c1 = df_div(xd, rho);
+      s1 = df_div(yd, rho);
+      df xi;
+      if (T.cmap == 1) {
+        const df u = df_mul(Rc, ias);
+        xi = df_div(df_sub(u, one), df_add(u, one));
+      } else if (T.cmap == 2) {
+        xi = df_from(log(df_to(Rc)));
+      } else {
+        xi = Rc;
+      }
+      df_cell(df_mul(df_sub(xi, xmin), idx), T.numx, fx, dx);
+      const df sg = df_div(zd, df_add(df_abs(zd), zeps));
+      const df yv = df_mul(sg, df_from(asinh(fabs(zz * T.inv_hscale))));
+      df_cell(df_mul(df_sub(yv, ymin), idy), T.numy, fy, dy);
+      if (Rout) Rout[p] = df_to(Rc);
+    } else {
+      const double Rd = sqrt(xx * xx + yy * yy + 1.0e-10);
+      double c, s;
+      unit_phi(xx, yy, c, s);
+      c1 = df_from(c);
+      s1 = df_from(s);
+      double X = (r_to_xi_inv(Rd, T.cmap, T.inv_ascale) - T.XMIN) * T.inv_dX;
+      double Y = (z_to_y_inv(zz, T.inv_hscale) - T.YMIN) * T.inv_dY;
+      double tx = trunc(X), ty = trunc(Y);
+      if (!(tx >= 0.0)) tx = 0.0;
+      if (!(ty >= 0.0)) ty = 0.0;
+      if (X < 0.0) X = 0.0;
+      if (Y < 0.0) Y = 0.0;
+      if (tx >= (double)T.numx) tx = (double)(T.numx - 1);
+      if (ty >= (double)T.numy) ty = (double)(T.numy - 1);
+      fx = (float)tx;
+      fy = (float)ty;
+      dx = df_from(X - tx);
+      dy = df_from(Y - ty);
+      if (Rout) Rout[p] = Rd;
+    }
+    const int ix = (int)fx, iy = (int)fy;
+    const int c = ix * T.numy + iy;
+    cell[p] = c;
+    slot[p] = atomicAdd(hist + c, 1);
+    rec[0 * n + p] = dx;
+    rec[1 * n + p] = dy;
+    rec[2 * n + p] = c1;
+    rec[3 * n + p] = s1;
+    rec[4 * n + p] = df_mul(df_split_or_from(mass[p]), m4pi);
+  }
+}
+
 // Exclusive prefix sum of hist[0..ncell) into off[] in two levels: tiles of
 // 1024 cells scanned by one block each (warp shuffles), then the tile totals.
 constexpr int kScanTile = 1024;
@@ -1018,7 +1108,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     int rc;
     if ((rc = timing_mark(0, st))) return rc;
     if (n > 0) {
-      k_cyl_binrec<R, RT><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+      if constexpr (F64)
+        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+      else
+        k_cyl_binrec<R, RT><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
       XT_CHECK_LAUNCH("k_cyl_binrec");
       if ((rc = timing_mark(1, st))) return rc;
       {

@@ -92,6 +92,12 @@ def test_eof_golden(tag):
     assert not np.any(s[0])
     E = eof.compute_coefficients(P, path, verbose=0)
     assert max(rel(E.cos[m], g["cos"][m]) for m in range(mmax + 1)) <= TOL
+    # the fused pipeline (double-float set-up and inner products) on the same particles
+    E2, res2 = eof.compute_coefficients_and_forces(P, path, verbose=0)
+    assert max(rel(E2.cos[m], g["cos"][m]) for m in range(mmax + 1)) <= TOL
+    assert max(rel(E2.sin[m], g["sin"][m]) for m in range(1, mmax + 1)) <= TOL
+    for k in range(6):
+        assert rel(res2[k], g["aep"][k]) <= TOL, k
     E.cos, E.sin = g["cos"], g["sin"]
     res = eof.compute_forces(P, E, verbose=0)
     for k in range(6):

@@ -151,10 +151,12 @@ def test_disc_fused_matches_separate_calls(disc):
     E = eof.compute_coefficients(P, path, verbose=0)
     ref = eof.compute_forces(P, E, verbose=0)
     E2, got = eof.compute_coefficients_and_forces(P, path, verbose=0)
+    # the fused set-up is double-float (~2^-46): coefficients within 1e-11
+    # of the FP64 separate calls (both within 1e-10 of the reference)
     for mm in range(t["mmax"] + 1):
-        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-12
+        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-11
         if mm:
-            assert rel(E2.sin[mm], E.sin[mm]) <= 1e-12
+            assert rel(E2.sin[mm], E.sin[mm]) <= 1e-11
     for k in range(6):
         assert rel(got[k], ref[k]) <= 1e-10, k
     E3, got32 = eof.compute_coefficients_and_forces(P, path, verbose=0, precision="f32")
@@ -182,4 +184,4 @@ def test_disc_fused_nan_particles(disc):
     E2, _ = eof.compute_coefficients_and_forces(P, path, verbose=0)
     assert np.all(np.isfinite(E2.cos))
     for mm in range(t["mmax"] + 1):
-        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-12
+        assert rel(E2.cos[mm], E.cos[mm]) <= 1e-11
