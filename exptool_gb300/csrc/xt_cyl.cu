@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* _
 }
 
 // FP64-path record kernel.  The set-up of every particle (R, rho = |(x, y)|,
-// cos/sin phi, the cmap = 1 map, the z map's sign factor, the cell and the
-// in-cell offsets) runs in double-float arithmetic on the FP32 pipe: inputs
-// are split into float pairs with integer operations, and only asinh (and
-// cmap = 2's log) and the returned R use the FP64 pipe.  Results equal the
+// cos/sin phi, the radial map including cmap = 2's log, the z map's sign
+// factor and asinh, the cell and the in-cell offsets) runs in double-float
+// arithmetic on the FP32 pipe: inputs are split into float pairs with
+// integer operations and the returned R is assembled with one FP64 add.  Results equal the
 // FP64 arithmetic to ~2^-46 relative.  Points outside the range where FP32
 // exponents are safe (|x|, |y|, |z| < 1e15, rho^2 > 1e-30, coordinates 0 or
 // >= 2^-74 in magnitude) take the FP64 arithmetic.
@@ -327,15 +327,24 @@ __device__ __forceinline__ void df_cell(df X, int nmax_cells, float& f, df& off)
   off = df_sub(X, {t, 0.f});
 }
 
-__global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, const double* __restrict__ x,
+// Table constants as float pairs, split on the host.
+struct BinrecDf {
+  df xmin, idx, ymin, idy, ias, ih, soft, zeps, m4pi;
+};
+
+static df host_df(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
+__global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecDf K, const double* __restrict__ x,
                                                        const double* __restrict__ y, const double* __restrict__ z,
                                                        const double* __restrict__ mass, long long n,
                                                        int* __restrict__ hist, int* __restrict__ cell,
                                                        int* __restrict__ slot, df* __restrict__ rec,
                                                        double* __restrict__ Rout, int nan_to_origin) {
-  const df xmin = df_from(T.XMIN), idx = df_from(T.inv_dX), ymin = df_from(T.YMIN), idy = df_from(T.inv_dY);
-  const df ias = df_from(T.inv_ascale), one = {1.f, 0.f}, soft = df_from(1.0e-10), zeps = df_from(1.0e-8);
-  const df m4pi = df_from(-FOUR_PI_C);
+  const df xmin = K.xmin, idx = K.idx, ymin = K.ymin, idy = K.idy, ias = K.ias, one = {1.f, 0.f};
+  const df soft = K.soft, zeps = K.zeps, m4pi = K.m4pi;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     double xx = x[p], yy = y[p], zz = z[p];
@@ -357,15 +366,15 @@ __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, const d
         const df u = df_mul(Rc, ias);
         xi = df_div(df_sub(u, one), df_add(u, one));
       } else if (T.cmap == 2) {
-        xi = df_from(log(df_to(Rc)));
+        xi = df_log(Rc);
       } else {
         xi = Rc;
       }
       df_cell(df_mul(df_sub(xi, xmin), idx), T.numx, fx, dx);
       const df sg = df_div(zd, df_add(df_abs(zd), zeps));
-      const df yv = df_mul(sg, df_from(asinh(fabs(zz * T.inv_hscale))));
+      const df yv = df_mul(sg, df_asinh(df_mul(df_abs(zd), K.ih)));
       df_cell(df_mul(df_sub(yv, ymin), idy), T.numy, fy, dy);
-      if (Rout) Rout[p] = df_to(Rc);
+      if (Rout) Rout[p] = df_to_int(Rc);
     } else {
       const double Rd = sqrt(xx * xx + yy * yy + 1.0e-10);
       double c, s;
@@ -1108,8 +1117,12 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     int rc;
     if ((rc = timing_mark(0, st))) return rc;
     if (n > 0) {
-      if constexpr (F64)
-        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+      if constexpr (F64) {
+        const BinrecDf K{host_df(T.XMIN), host_df(T.inv_dX), host_df(T.YMIN), host_df(T.inv_dY),
+                         host_df(T.inv_ascale), host_df(T.inv_hscale), host_df(1.0e-10), host_df(1.0e-8),
+                         host_df(-FOUR_PI_C)};
+        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, K, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+      }
       else
         k_cyl_binrec<R, RT><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
       XT_CHECK_LAUNCH("k_cyl_binrec");
