@@ -25,6 +25,10 @@ XT_SPH_FORCE_EVAL = 2
 XT_CYL_ACCUMULATED_EVAL_PARTICLES = 0
 XT_CYL_FORCE_EVAL = 1
 XT_CYL_ACCUMULATED_EVAL = 2
+XT_PTR_DEVICE = 0
+XT_PTR_PINNED = 1
+XT_PTR_PAGEABLE = 2
+XT_PTR_INACCESSIBLE = 3
 
 _lock = threading.Lock()
 _lib = None
@@ -36,6 +40,7 @@ c_dpp = ctypes.POINTER(ctypes.c_void_p)
 _SIGS = {
     "xt_abi_version": (c_int, []),
     "xt_last_error": (ctypes.c_char_p, []),
+    "xt_pointer_access": (c_int, [c_vp]),
     "xt_sph_table_create": (c_int, [c_int, c_int, c_int, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_vp, c_vp, c_vp, c_vp,
                                     ctypes.POINTER(c_vp)]),
     "xt_sph_table_destroy": (c_int, [c_vp]),

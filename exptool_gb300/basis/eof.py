@@ -218,11 +218,13 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     are placed at the origin (unless nanblock) for both passes."""
     x, y, z, m = positions(PSPInput)
     table = table_from_file(eof_file)
-    # inputs and results cross host <-> device as copies enqueued on the
-    # compute stream (asynchronous from pinned arrays) with one final
-    # synchronisation; particles with a NaN coordinate are placed at the
-    # origin on the device
-    c, s, outs = table.accumulate_eval(*(dev.to_dev_async(a) for a in (x, y, z, m)), precision=precision, m1=m1,
+    # Particle arrays in page-locked host memory are read by the binning
+    # kernel in place (the host -> device traffic overlaps its work); other
+    # inputs are copied to the device first.  Results are computed into device
+    # memory and copied back to page-locked host arrays, with one
+    # synchronisation at the end.  Particles with a NaN coordinate are placed
+    # at the origin on the device.
+    c, s, outs = table.accumulate_eval(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision, m1=m1,
                                        m2=m2, nan_to_origin=not nanblock)
     host = dev.to_host_many([c, s] + list(outs))
     out = EOF_Object()

@@ -42,6 +42,12 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // (152 on GB300) times the resident blocks per SM, capped by the work.
 int grid_for(long long n, int block, int blocks_per_sm = 8);
 
+// Where a pointer lives, as far as kernels are concerned (XT_PTR_* values of
+// the public header): device (or managed) memory, pinned host memory, other
+// host memory the device can address (pageable access), or host memory it
+// cannot address.
+int pointer_access(const void* p);
+
 // ------------------------------------------------------------------ device math
 constexpr double PI = 3.14159265358979323846;
 

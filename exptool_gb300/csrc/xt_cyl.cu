@@ -169,7 +169,15 @@ __global__ void __launch_bounds__(256) k_cyl_field(const TT* __restrict__ tab, c
       const int ti = tmap[f];
       const double* coef = (ti >= 4) ? sinc : cosc;
       const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
-      for (int k = 0; k < nuse; ++k) acc += coef[m * norder + k] * (double)t[(size_t)k * nnode];
+      int k = 0;
+      for (; k + 8 <= nuse; k += 8) {     // eight table rows in flight, then the FMAs in order
+        TT v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = t[(size_t)(k + u) * nnode];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += coef[m * norder + k + u] * (double)v[u];
+      }
+      for (; k < nuse; ++k) acc += coef[m * norder + k] * (double)t[(size_t)k * nnode];
     }
     tile[nl * mf_total + mf] = (R)acc;
   }
@@ -480,83 +488,12 @@ __global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __r
   }
 }
 
-// Deposit of sorted records: each thread takes RUN consecutive particles and
-// sums their contributions per (m, cos/sin, corner) in registers while the
-// cell stays the same, issuing the FP64 atomics once per run and cell.
-template <typename R, int MCAP, int RUN>
-__global__ void __launch_bounds__(128) k_cyl_deposit_sorted(CylTab<R> T, long long n, const R* __restrict__ srec,
-                                                            const int* __restrict__ scell, double* __restrict__ D,
-                                                            size_t nnode) {
-  const int ny1 = T.numy + 1;
-  const int mmax = T.mmax;
-  const long long nrun = (n + RUN - 1) / RUN;
-  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nrun;
-       r += (long long)gridDim.x * blockDim.x) {
-    R acc[2 * MCAP + 1][4];
-#pragma unroll
-    for (int j = 0; j < 2 * MCAP + 1; ++j)
-#pragma unroll
-      for (int k = 0; k < 4; ++k) acc[j][k] = R(0);
-    int cur = -1;
-    auto flush = [&](int c) {
-      const int ix = c / T.numy, iy = c - ix * T.numy;
-      const size_t n00 = (size_t)ix * ny1 + iy, n10 = n00 + ny1, n01 = n00 + 1, n11 = n10 + 1;
-#pragma unroll
-      for (int j = 0; j < 2 * MCAP + 1; ++j) {
-        if (j > 2 * mmax) break;
-        const int m = (j + 1) / 2;             // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
-        const int cs = (j == 0) ? 0 : ((j & 1) ? 0 : 1);
-        double* d = D + (size_t)(2 * m + cs) * nnode;
-        atomicAdd(d + n00, (double)acc[j][0]);
-        atomicAdd(d + n10, (double)acc[j][1]);
-        atomicAdd(d + n01, (double)acc[j][2]);
-        atomicAdd(d + n11, (double)acc[j][3]);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[j][k] = R(0);
-      }
-    };
-    const long long q0 = r * RUN;
-#pragma unroll 1
-    for (int u = 0; u < RUN; ++u) {
-      const long long q = q0 + u;
-      if (q >= n) break;
-      const int c = scell[q];
-      if (c != cur) {
-        if (cur >= 0) flush(cur);
-        cur = c;
-      }
-      R w[4];
-      weights_from_frac(srec[0 * n + q], srec[1 * n + q], w);
-      const R c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
-      R cprev = R(1), sprev = R(0), ccur = c1, scur = s1;
-#pragma unroll
-      for (int m = 0; m <= MCAP; ++m) {
-        if (m > mmax) break;
-        R cm, sm;
-        if (m == 0) { cm = R(1); sm = R(0); }
-        else if (m == 1) { cm = c1; sm = s1; }
-        else {
-          cm = R(2) * c1 * ccur - cprev;
-          sm = R(2) * c1 * scur - sprev;
-          cprev = ccur; sprev = scur; ccur = cm; scur = sm;
-        }
-        const R wc = base * cm;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[m == 0 ? 0 : 2 * m - 1][k] += wc * w[k];
-        if (m > 0) {
-          const R ws = base * sm;
-#pragma unroll
-          for (int k = 0; k < 4; ++k) acc[2 * m][k] += ws * w[k];
-        }
-      }
-    }
-    if (cur >= 0) flush(cur);
-  }
-}
-
-// Evaluation of sorted records (accumulated_eval_particles outputs p0 p fr fp fz),
-// written back to the particles' original slots.
-template <typename R>
+// Evaluation of the binned records (accumulated_eval_particles outputs p0 p
+// fr fp fz).  SORTED: records in cell order (srec, scell) with each result
+// written back to the particle's original slot sorig[q]; otherwise the records
+// in original order (rec, cell) and coalesced result writes, which is the form
+// for results written straight into host memory.
+template <typename R, bool SORTED>
 __global__ void __launch_bounds__(128) k_cyl_eval_sorted(CylTab<R> T, const R* __restrict__ F, long long n,
                                                          const R* __restrict__ srec, const int* __restrict__ scell,
                                                          const int* __restrict__ sorig, CylEvalOpts o, double* o0,
@@ -575,7 +512,7 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted(CylTab<R> T, const R* _
     B.c11 = w[3];
     R v[9];
     cyl_eval_bins(T, F, B, srec[2 * n + q], srec[3 * n + q], o, v);
-    const int p = sorig[q];
+    const long long p = SORTED ? (long long)sorig[q] : q;
     if (o0) o0[p] = v[0];
     if (o1) o1[p] = v[1];
     if (o2) o2[p] = v[2];
@@ -594,78 +531,139 @@ __device__ __forceinline__ void df_weights(df dx, df dy, df w[4]) {
   w[3] = df_mul(dx, dy);
 }
 
-// Double-float deposit of sorted records (FP64 path): as k_cyl_deposit_sorted,
-// with the per-run sums kept as df and converted to FP64 for the atomics.
-template <int MCAP, int RUN>
-__global__ void __launch_bounds__(128) k_cyl_deposit_sorted_df(CylTab<double> T, long long n,
-                                                               const df* __restrict__ srec,
-                                                               const int* __restrict__ scell, double* __restrict__ D,
-                                                               size_t nnode) {
-  const int ny1 = T.numy + 1;
-  const int mmax = T.mmax;
+// Arithmetic of the sorted deposit: FP32 sums (mixed path) or double-float
+// sums (FP64 path), both widened to FP64 for the atomics.
+struct DepF32 {
+  using T = float;
+  static __device__ __forceinline__ T zero() { return 0.f; }
+  static __device__ __forceinline__ T one() { return 1.f; }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return a * b + c; }
+  static __device__ __forceinline__ T cheb(T c1, T cur, T prev) { return 2.f * c1 * cur - prev; }
+  static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
+  static __device__ __forceinline__ double wide(T a) { return (double)a; }
+};
+struct DepDF {
+  using T = df;
+  static __device__ __forceinline__ T zero() { return df{0.f, 0.f}; }
+  static __device__ __forceinline__ T one() { return df{1.f, 0.f}; }
+  static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return df_fma(a, b, c); }
+  static __device__ __forceinline__ T cheb(T c1, T cur, T prev) {
+    return df_sub(df_scale(df_mul(c1, cur), 2.f), prev);
+  }
+  static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { df_weights(dx, dy, w); }
+  static __device__ __forceinline__ double wide(T a) { return df_to(a); }
+};
+
+constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
+
+// Deposit of sorted records.  Each lane takes RUN consecutive particles and
+// sums their contributions per (m, cos/sin, corner) in registers while the
+// cell stays the same.  A lane whose cell changes (and every lane at the end
+// of its run) parks its sums in shared memory; the whole warp then widens
+// them to FP64 and issues the atomics, 32 entries per instruction.  (A
+// divergent per-lane flush would occupy the FP64 unit for a full warp
+// instruction per value however few lanes are active.)  Loops are
+// warp-uniform so that the ballots see every lane.
+template <typename M, int MCAP, int RUN>
+__global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, long long n,
+                                                            const typename M::T* __restrict__ srec,
+                                                            const int* __restrict__ scell, double* __restrict__ D,
+                                                            size_t nnode) {
+  using T = typename M::T;
+  constexpr int NJ = 2 * MCAP + 1;
+  constexpr int NE = NJ * 4;
+  constexpr int PITCH = NE + 1;                 // conflict-free parking of up to 8 lanes
+  __shared__ T park[4][kDepSlots][PITCH];
+  __shared__ int park_node[4][kDepSlots];     // lower-left node of the parked lane's cell
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int ny1 = numy + 1;
+  const int nju = 2 * mmax + 1;                 // accumulators in use
   const long long nrun = (n + RUN - 1) / RUN;
-  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nrun;
-       r += (long long)gridDim.x * blockDim.x) {
-    df acc[2 * MCAP + 1][4];
+  T acc[NJ][4];
 #pragma unroll
-    for (int j = 0; j < 2 * MCAP + 1; ++j)
+  for (int j = 0; j < NJ; ++j)
 #pragma unroll
-      for (int k = 0; k < 4; ++k) acc[j][k] = df{0.f, 0.f};
-    int cur = -1;
-    auto flush = [&](int c) {
-      const int ix = c / T.numy, iy = c - ix * T.numy;
-      const size_t n00 = (size_t)ix * ny1 + iy, n10 = n00 + ny1, n01 = n00 + 1, n11 = n10 + 1;
-#pragma unroll
-      for (int j = 0; j < 2 * MCAP + 1; ++j) {
-        if (j > 2 * mmax) break;
-        const int m = (j + 1) / 2;
-        const int cs = (j == 0) ? 0 : ((j & 1) ? 0 : 1);
-        double* d = D + (size_t)(2 * m + cs) * nnode;
-        atomicAdd(d + n00, df_to(acc[j][0]));
-        atomicAdd(d + n10, df_to(acc[j][1]));
-        atomicAdd(d + n01, df_to(acc[j][2]));
-        atomicAdd(d + n11, df_to(acc[j][3]));
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[j][k] = df{0.f, 0.f};
+    for (int k = 0; k < 4; ++k) acc[j][k] = M::zero();
+
+  // park the sums of the lanes in `want`, batch by batch, and deposit them
+  auto flush = [&](bool want, int cell) {
+    unsigned pend = __ballot_sync(0xffffffffu, want);
+    while (pend) {
+      unsigned batch = 0, rest = pend;
+      for (int i = 0; i < kDepSlots && rest; ++i) {
+        batch |= rest & (0u - rest);
+        rest &= rest - 1;
       }
-    };
-    const long long q0 = r * RUN;
+      const int nb = __popc(batch);
+      if (batch & (1u << lane)) {
+        const int sidx = __popc(batch & ((1u << lane) - 1));
+        const int ix = cell / numy, iy = cell - ix * numy;
+        park_node[wib][sidx] = ix * ny1 + iy;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            park[wib][sidx][j * 4 + k] = acc[j][k];
+            acc[j][k] = M::zero();
+          }
+      }
+      __syncwarp();
+      for (int i = lane; i < nb * NE; i += 32) {
+        const int sidx = i / NE, e = i - sidx * NE;
+        const int j = e >> 2, k = e & 3;
+        if (j < nju) {
+          const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
+          const int m = (j + 1) >> 1;          // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
+          const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
+          atomicAdd(D + (size_t)(2 * m + cs) * nnode + node, M::wide(park[wib][sidx][e]));
+        }
+      }
+      __syncwarp();
+      pend &= ~batch;
+    }
+  };
+
+  for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); r0 < nrun;
+       r0 += (long long)gridDim.x * blockDim.x) {
+    const long long q0 = (r0 + lane) * RUN;
+    int cur = -1;
 #pragma unroll 1
     for (int u = 0; u < RUN; ++u) {
       const long long q = q0 + u;
-      if (q >= n) break;
-      const int c = scell[q];
-      if (c != cur) {
-        if (cur >= 0) flush(cur);
-        cur = c;
-      }
-      df w[4];
-      df_weights(srec[0 * n + q], srec[1 * n + q], w);
-      const df c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
-      df cprev{1.f, 0.f}, sprev{0.f, 0.f}, ccur = c1, scur = s1;
+      const bool valid = q < n;                 // also false for lanes past the last run
+      const int c = valid ? scell[q] : cur;
+      flush(cur >= 0 && c != cur, cur);
+      cur = c;
+      if (!valid) continue;
+      T w[4];
+      M::weights(srec[0 * n + q], srec[1 * n + q], w);
+      const T c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
+      T cprev = M::one(), sprev = M::zero(), ccur = c1, scur = s1;
 #pragma unroll
       for (int m = 0; m <= MCAP; ++m) {
         if (m > mmax) break;
-        df cm, sm;
-        if (m == 0) { cm = df{1.f, 0.f}; sm = df{0.f, 0.f}; }
+        T cm, sm;
+        if (m == 0) { cm = M::one(); sm = M::zero(); }
         else if (m == 1) { cm = c1; sm = s1; }
         else {
-          cm = df_sub(df_scale(df_mul(c1, ccur), 2.f), cprev);
-          sm = df_sub(df_scale(df_mul(c1, scur), 2.f), sprev);
+          cm = M::cheb(c1, ccur, cprev);
+          sm = M::cheb(c1, scur, sprev);
           cprev = ccur; sprev = scur; ccur = cm; scur = sm;
         }
-        const df wc = df_mul(base, cm);
+        const T wc = M::mul(base, cm);
         const int jc = (m == 0) ? 0 : 2 * m - 1;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) acc[jc][k] = df_fma(wc, w[k], acc[jc][k]);
+        for (int k = 0; k < 4; ++k) acc[jc][k] = M::fma(wc, w[k], acc[jc][k]);
         if (m > 0) {
-          const df ws = df_mul(base, sm);
+          const T ws = M::mul(base, sm);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) acc[2 * m][k] = df_fma(ws, w[k], acc[2 * m][k]);
+          for (int k = 0; k < 4; ++k) acc[2 * m][k] = M::fma(ws, w[k], acc[2 * m][k]);
         }
       }
     }
-    if (cur >= 0) flush(cur);
+    flush(cur >= 0, cur);
   }
 }
 
@@ -715,7 +713,15 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, 
       const int ti = tmap[f];
       const df* coef = cf + ((ti >= 4) ? ncoef : 0) + m * norder;
       const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
-      for (int k = 0; k < norder; ++k) acc = df_fma(coef[k], load_df(t + (size_t)k * nnode), acc);
+      int k = 0;
+      for (; k + 8 <= norder; k += 8) {   // eight table rows in flight, then the FMAs in order
+        TT v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = t[(size_t)(k + u) * nnode];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc = df_fma(coef[k + u], load_df(&v[u]), acc);
+      }
+      for (; k < norder; ++k) acc = df_fma(coef[k], load_df(t + (size_t)k * nnode), acc);
     }
     tile[nl * mf_total + mf] = from_df<OT>(acc);
   }
@@ -725,7 +731,9 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, 
   for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) dst[idx] = tile[idx];
 }
 
-// Double-float evaluation of sorted records (FP64 path, accumulated_eval_particles).
+// Double-float evaluation of the binned records (FP64 path,
+// accumulated_eval_particles); SORTED as for k_cyl_eval_sorted.
+template <bool SORTED>
 __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
                                                             const df* __restrict__ srec,
                                                             const int* __restrict__ scell,
@@ -775,7 +783,7 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, co
       fz = df_add(fz, fzm);
       fp = df_add(fp, fpm);
     }
-    const int pidx = sorig[q];
+    const long long pidx = SORTED ? (long long)sorig[q] : q;
     if (o0) o0[pidx] = df_to(p0);
     if (o1) o1[pidx] = df_to(p);
     if (o2) o2[pidx] = df_to(fr);
@@ -1084,6 +1092,20 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
              h->mmax, h->norder);
   XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
              "the fused path supports numx*numy <= %d cells", kScanTile * kScanTile);
+  // particle arrays and results may live in host memory the device can
+  // address (pinned, or any host memory where the device has pageable access)
+  bool host_out = false;
+  if (n > 0) {
+    for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
+      XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
+                 p);
+    for (int i = 0; i < 6; ++i) {
+      if (!outs[i]) continue;
+      const int k = pointer_access(outs[i]);
+      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
+      host_out |= k != XT_PTR_DEVICE;
+    }
+  }
   const FusedLayout L = fused_layout(h, n, precision);
   if (!workspace || workspace_bytes < L.total) {
     set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
@@ -1146,10 +1168,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         constexpr int MC = decltype(mc)::value;
         constexpr int RUN = decltype(rl)::value;
         const int gr = grid_for((n + RUN - 1) / RUN, 128, 8);
-        if constexpr (F64)
-          k_cyl_deposit_sorted_df<MC, RUN><<<gr, 128, 0, st>>>(T, n, srec, scell, D, h->nnode);
-        else
-          k_cyl_deposit_sorted<R, MC, RUN><<<gr, 128, 0, st>>>(T, n, srec, scell, D, h->nnode);
+        using Mth = std::conditional_t<F64, DepDF, DepF32>;
+        k_cyl_deposit_sorted<Mth, MC, RUN><<<gr, 128, 0, st>>>(h->numy, h->mmax, n,
+                                                               reinterpret_cast<const typename Mth::T*>(srec),
+                                                               scell, D, h->nnode);
       };
       auto dep_m = [&](auto rl) {
         if (h->mmax <= 2) dep(std::integral_constant<int, 2>{}, rl);
@@ -1203,15 +1225,32 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     }
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {
+      // Device results are evaluated from the cell-sorted records (neighbouring
+      // threads share field rows in L1: 0.18 ms against 0.39 ms in particle
+      // order for 1e6 disc particles).  Results in host memory are evaluated in
+      // particle order instead, so that each warp's writes over the host link
+      // are coalesced rather than 8-byte scatters.
+      const bool sorted = !host_out;
+      const RT* er = sorted ? srec : rec;
+      const int* ec = sorted ? scell : cell;
       if constexpr (F64) {
-        k_cyl_eval_sorted_df<<<g128, 128, 0, st>>>(T, reinterpret_cast<const df*>(field), n, srec, scell, sorig, m1,
-                                                   m2, outs[0], outs[1], outs[2], outs[3], outs[4]);
+        auto ev = [&](auto srt) {
+          k_cyl_eval_sorted_df<decltype(srt)::value><<<g128, 128, 0, st>>>(
+              T, reinterpret_cast<const df*>(field), n, er, ec, sorig, m1, m2, outs[0], outs[1], outs[2], outs[3],
+              outs[4]);
+        };
+        if (sorted) ev(std::true_type{});
+        else ev(std::false_type{});
       } else {
         CylEvalOpts o;
         o.mode = XT_CYL_ACCUMULATED_EVAL_PARTICLES; o.m1 = m1; o.m2 = m2; o.mmax_use = h->mmax; o.no_odd = 0;
         o.perturb = 0; o.density = 0; o.nf = 6;
-        k_cyl_eval_sorted<R><<<g128, 128, 0, st>>>(T, field, n, srec, scell, sorig, o, outs[0], outs[1], outs[2],
-                                                   outs[3], outs[4]);
+        if (sorted)
+          k_cyl_eval_sorted<R, true><<<g128, 128, 0, st>>>(T, field, n, er, ec, sorig, o, outs[0], outs[1], outs[2],
+                                                           outs[3], outs[4]);
+        else
+          k_cyl_eval_sorted<R, false><<<g128, 128, 0, st>>>(T, field, n, er, ec, sorig, o, outs[0], outs[1],
+                                                            outs[2], outs[3], outs[4]);
       }
       XT_CHECK_LAUNCH("k_cyl_eval_sorted");
     }

@@ -54,6 +54,23 @@ int grid_for(long long n, int block, int blocks_per_sm) {
   return (int)(need < cap ? need : cap);
 }
 
+int pointer_access(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    a.type = cudaMemoryTypeUnregistered;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return XT_PTR_DEVICE;
+  if (a.type == cudaMemoryTypeHost) return XT_PTR_PINNED;
+  static int pageable = -1;
+  if (pageable < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    pageable = (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v) ? 1 : 0;
+  }
+  return pageable ? XT_PTR_PAGEABLE : XT_PTR_INACCESSIBLE;
+}
+
 // ------------------------------------------------------------------ handle
 struct SphHandle {
   int lmax, nmax, numr, cmap;
@@ -240,6 +257,7 @@ extern "C" {
 
 int xt_abi_version(void) { return 1; }
 const char* xt_last_error(void) { return xt::g_err.c_str(); }
+int xt_pointer_access(const void* p) { return xt::pointer_access(p); }
 
 int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, double rmax, double scale,
                         const double* xi, const double* p0, const double* d0, const double* ev, const double* ef,

@@ -8,6 +8,7 @@ reference-style APIs that pass tables on every call upload them once.
 """
 from __future__ import annotations
 
+import ctypes
 import hashlib
 import os
 import threading
@@ -53,6 +54,28 @@ def to_dev_async(a) -> torch.Tensor:
     copied synchronously by torch."""
     t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64)))
     return t.to(device(), non_blocking=True)
+
+
+def host_access(a: np.ndarray) -> int:
+    """How kernels can reach a NumPy array's buffer (``_lib.XT_PTR_*``)."""
+    return int(_lib.load().xt_pointer_access(ctypes.c_void_p(a.ctypes.data)))
+
+
+def kernel_input(a):
+    """A float64 particle array in the form the kernels read: a contiguous
+    array in page-locked host memory is passed in place (the kernels read it
+    over the host link, so the transfer overlaps their work); anything else is
+    copied to the device on the current stream first."""
+    a = np.asarray(a, dtype=np.float64)
+    if a.size and a.flags.c_contiguous and host_access(a) == _lib.XT_PTR_PINNED:
+        return a
+    return to_dev_async(a)
+
+
+def pinned_empty(n: int, count: int) -> list:
+    """``count`` float64 arrays of length n in page-locked host memory (torch's
+    caching host allocator), as torch tensors the kernels can write directly."""
+    return [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(count)]
 
 
 def to_host_many(ts) -> list:
@@ -265,19 +288,28 @@ class CylTable:
                                                stream_ptr()), "xt_cyl_accumulate")
         return cos, sin
 
-    def accumulate_eval(self, x, y, z, m, precision="f64", m1=0, m2=1000, workspace=None, nan_to_origin=True):
+    def accumulate_eval(self, x, y, z, m, precision="f64", m1=0, m2=1000, workspace=None, nan_to_origin=True,
+                        outs=None):
         """Fused accumulate + accumulated_eval_particles at the same particles:
-        returns cos, sin, [p0, p, fr, fp, fz, R]."""
-        n = int(x.numel())
+        returns cos, sin, [p0, p, fr, fp, fz, R].  x, y, z, m are CUDA tensors
+        or contiguous float64 NumPy arrays the device addresses (see
+        ``kernel_input``); ``outs`` optionally gives the six result arrays
+        (CUDA tensors or page-locked host tensors, written in place)."""
+        n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
-        cos = torch.empty((self.mmax + 1, self.norder), dtype=torch.float64, device=x.device)
+        cos = torch.empty((self.mmax + 1, self.norder), dtype=torch.float64, device=device())
         sin = torch.empty_like(cos)
-        outs = [torch.empty(n, dtype=torch.float64, device=x.device) for _ in range(6)]
+        if outs is None:
+            outs = [torch.empty(n, dtype=torch.float64, device=device()) for _ in range(6)]
         need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
         ws = workspace if (workspace is not None and workspace.numel() >= need) else \
-            torch.empty(need, dtype=torch.uint8, device=x.device)
-        pp, keep = _lib.ptr_array([dptr(t) for t in outs])
-        _lib.check(self._lib.xt_cyl_accumulate_eval(self.handle, dptr(x), dptr(y), dptr(z), dptr(m), n, pc, int(m1),
+            torch.empty(need, dtype=torch.uint8, device=device())
+
+        def ptr(a):
+            return a.data_ptr() if isinstance(a, torch.Tensor) else a.ctypes.data
+
+        pp, keep = _lib.ptr_array([ptr(t) for t in outs])
+        _lib.check(self._lib.xt_cyl_accumulate_eval(self.handle, ptr(x), ptr(y), ptr(z), ptr(m), n, pc, int(m1),
                                                     int(m2), int(bool(nan_to_origin)), dptr(cos), dptr(sin), pp,
                                                     dptr(ws), ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return cos, sin, outs

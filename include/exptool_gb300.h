@@ -47,9 +47,18 @@ extern "C" {
 #define XT_CYL_FORCE_EVAL 1                 /* eof.force_eval                 (eof.py:756) */
 #define XT_CYL_ACCUMULATED_EVAL 2           /* eof.accumulated_eval           (eof.py:874) */
 
+/* where a pointer lives, for kernels (xt_pointer_access) */
+#define XT_PTR_DEVICE 0       /* device or managed memory                              */
+#define XT_PTR_PINNED 1       /* page-locked host memory, addressed by kernels directly */
+#define XT_PTR_PAGEABLE 2     /* other host memory the device addresses (pageable access) */
+#define XT_PTR_INACCESSIBLE 3 /* host memory the device cannot address                 */
+
 /* --------------------------------------------------------------- misc */
 int xt_abi_version(void);
 const char *xt_last_error(void);
+/* XT_PTR_* class of p on the current device.  No counterpart in the reference
+ * (it has no device); used to pass host arrays straight to the kernels. */
+int xt_pointer_access(const void *p);
 
 /* --------------------------------------------------------------- spherical (SL) */
 /* Upload an SL basis: replaces the per-call table reads of
@@ -161,7 +170,11 @@ int xt_cyl_eval_points(void *handle, const void *field, int precision, int densi
  * inside the workspace (size from xt_cyl_accumulate_eval_workspace).
  * nan_to_origin != 0 places particles with a NaN coordinate at the origin
  * for both accumulation and evaluation (eof.py:1189-1204).  mmax <= 8,
- * norder <= 24. */
+ * norder <= 24.  Unlike the other entry points, x, y, z, m and outs may also
+ * be host memory the device addresses (xt_pointer_access XT_PTR_PINNED or
+ * XT_PTR_PAGEABLE): the kernels then read the particles in place over the
+ * host link, and host results are evaluated in particle order so that their
+ * writes are coalesced; XT_PTR_INACCESSIBLE pointers return XT_ERR_ARG. */
 size_t xt_cyl_accumulate_eval_workspace(void *handle, long long n, int precision);
 int xt_cyl_accumulate_eval(void *handle, const double *x, const double *y, const double *z, const double *m,
                            long long n, int precision, int m1, int m2, int nan_to_origin, double *cos_out,
