@@ -220,13 +220,14 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     table = table_from_file(eof_file)
     # Particle arrays in page-locked host memory are read by the binning
     # kernel in place (the host -> device traffic overlaps its work); other
-    # inputs are copied to the device first.  Results are computed into device
-    # memory and copied back to page-locked host arrays, with one
-    # synchronisation at the end.  Particles with a NaN coordinate are placed
-    # at the origin on the device.
-    c, s, outs = table.accumulate_eval(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision, m1=m1,
-                                       m2=m2, nan_to_origin=not nanblock)
-    host = dev.to_host_many([c, s] + list(outs))
+    # inputs are copied to the device first.  Coefficients and results are
+    # computed into reused device blocks and leave in two copies to
+    # page-locked host memory, with one synchronisation at the end.  Particles
+    # with a NaN coordinate are placed at the origin on the device.
+    coef, res = table.accumulate_eval_blocks(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision,
+                                             m1=m1, m2=m2, nan_to_origin=not nanblock)
+    cs_h, res_h = dev.to_host_many([coef, res])
+    host = [cs_h[0], cs_h[1]] + list(res_h)
     out = EOF_Object()
     out.time = getattr(PSPInput, "time", None)
     out.filename = getattr(PSPInput, "filename", None)

@@ -269,6 +269,7 @@ class CylTable:
         self.handle = h.value
         self._lib = lib
         self.field_cache = _Cache(limit=8)
+        self._fused_bufs = threading.local()
 
     def __del__(self):
         try:
@@ -289,16 +290,18 @@ class CylTable:
         return cos, sin
 
     def accumulate_eval(self, x, y, z, m, precision="f64", m1=0, m2=1000, workspace=None, nan_to_origin=True,
-                        outs=None):
+                        outs=None, coef=None):
         """Fused accumulate + accumulated_eval_particles at the same particles:
         returns cos, sin, [p0, p, fr, fp, fz, R].  x, y, z, m are CUDA tensors
         or contiguous float64 NumPy arrays the device addresses (see
         ``kernel_input``); ``outs`` optionally gives the six result arrays
-        (CUDA tensors or page-locked host tensors, written in place)."""
+        (CUDA tensors or page-locked host tensors, written in place) and
+        ``coef`` a (2, mmax+1, norder) device tensor for cos and sin."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
-        cos = torch.empty((self.mmax + 1, self.norder), dtype=torch.float64, device=device())
-        sin = torch.empty_like(cos)
+        if coef is None:
+            coef = torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device())
+        cos, sin = coef[0], coef[1]
         if outs is None:
             outs = [torch.empty(n, dtype=torch.float64, device=device()) for _ in range(6)]
         need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
@@ -313,6 +316,25 @@ class CylTable:
                                                     int(m2), int(bool(nan_to_origin)), dptr(cos), dptr(sin), pp,
                                                     dptr(ws), ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return cos, sin, outs
+
+    def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True):
+        """accumulate_eval into per-thread buffers kept for the last particle
+        count and precision: returns the (2, mmax+1, norder) coefficient block
+        (cos, sin) and the (6, n) result block.  The next call on this thread
+        with the same size overwrites both, so callers copy them out first."""
+        n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
+        pc = precision_code(precision)
+        b = getattr(self._fused_bufs, "v", None)
+        if b is None or b[0] != (n, pc):
+            need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
+            b = ((n, pc), torch.empty(need, dtype=torch.uint8, device=device()),
+                 torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device()),
+                 torch.empty((6, n), dtype=torch.float64, device=device()))
+            self._fused_bufs.v = b
+        _, ws, coef, res = b
+        self.accumulate_eval(x, y, z, m, precision=precision, m1=m1, m2=m2, workspace=ws,
+                             nan_to_origin=nan_to_origin, outs=list(res), coef=coef)
+        return coef, res
 
     def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):
         pc = precision_code(precision)
