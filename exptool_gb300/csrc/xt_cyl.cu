@@ -254,10 +254,25 @@ __global__ void __launch_bounds__(128) k_cyl_eval(CylTab<R> T, const R* __restri
 // cos/sin phi) is computed once; particles are counting-sorted by table cell
 // so that warps deposit into and gather from the same few nodes.
 
-// Records, structure of arrays with n entries each: the fractional cell
-// coordinates dx = X - ix, dy = Y - iy (the bilinear weights are products of
-// dx, dy and their complements), cos phi, sin phi, -4 pi m.
-constexpr int kRec = 5;
+// One binned particle, stored whole (48 bytes as double-float, 32 as FP32) so
+// that binning, sorting and both consumers move it with 16-byte accesses: the
+// fractional cell coordinates dx = X - ix, dy = Y - iy (the bilinear weights
+// are products of dx, dy and their complements), cos phi, sin phi, -4 pi m,
+// the cell, and an index (the particle's slot within its cell as binned, its
+// original index once sorted).
+template <typename RT>
+struct BinRec;
+template <>
+struct alignas(16) BinRec<df> {
+  df dx, dy, c1, s1, base;
+  int cell, idx;
+};
+template <>
+struct alignas(16) BinRec<float> {
+  float dx, dy, c1, s1, base;
+  int cell, idx, pad;
+};
+static_assert(sizeof(BinRec<df>) == 48 && sizeof(BinRec<float>) == 32, "record sizes");
 
 template <typename R>
 __device__ __forceinline__ void weights_from_frac(R dx, R dy, R w[4]) {
@@ -268,23 +283,12 @@ __device__ __forceinline__ void weights_from_frac(R dx, R dy, R w[4]) {
   w[3] = dx * dy;   // c11
 }
 
-template <typename RT, typename R>
-__device__ __forceinline__ RT to_rec(R v);
-template <>
-__device__ __forceinline__ float to_rec<float, float>(float v) { return v; }
-template <>
-__device__ __forceinline__ double to_rec<double, double>(double v) { return v; }
-template <>
-__device__ __forceinline__ df to_rec<df, double>(double v) { return df_from(v); }
-
-// RT = record type: float (mixed path), df (FP64 path: values computed in FP64,
-// stored as hi/lo FP32 pairs for the double-float deposit and evaluation).
-template <typename R, typename RT>
+// FP32-path record kernel (mixed precision).
+template <typename R>
 __global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* __restrict__ x,
                                                     const double* __restrict__ y, const double* __restrict__ z,
                                                     const double* __restrict__ mass, long long n,
-                                                    int* __restrict__ hist, int* __restrict__ cell,
-                                                    int* __restrict__ slot, RT* __restrict__ rec,
+                                                    int* __restrict__ hist, BinRec<R>* __restrict__ rec,
                                                     double* __restrict__ Rout, int nan_to_origin) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
@@ -305,14 +309,15 @@ __global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* _
     if (fx >= R(T.numx)) fx = R(T.numx - 1);
     if (fy >= R(T.numy)) fy = R(T.numy - 1);
     const int ix = (int)fx, iy = (int)fy;
-    const int c = ix * T.numy + iy;
-    cell[p] = c;
-    slot[p] = atomicAdd(hist + c, 1);
-    rec[0 * n + p] = to_rec<RT, R>(X - fx);
-    rec[1 * n + p] = to_rec<RT, R>(Y - fy);
-    rec[2 * n + p] = to_rec<RT, R>(c1);
-    rec[3 * n + p] = to_rec<RT, R>(s1);
-    rec[4 * n + p] = to_rec<RT, R>(R(-FOUR_PI_C) * (R)mass[p]);
+    BinRec<R> r;
+    r.dx = X - fx;
+    r.dy = Y - fy;
+    r.c1 = c1;
+    r.s1 = s1;
+    r.base = R(-FOUR_PI_C) * (R)mass[p];
+    r.cell = ix * T.numy + iy;
+    r.idx = atomicAdd(hist + r.cell, 1);
+    rec[p] = r;
     if (Rout) Rout[p] = (double)Rc;
   }
 }
@@ -348,8 +353,7 @@ static df host_df(double v) {
 __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecDf K, const double* __restrict__ x,
                                                        const double* __restrict__ y, const double* __restrict__ z,
                                                        const double* __restrict__ mass, long long n,
-                                                       int* __restrict__ hist, int* __restrict__ cell,
-                                                       int* __restrict__ slot, df* __restrict__ rec,
+                                                       int* __restrict__ hist, BinRec<df>* __restrict__ rec,
                                                        double* __restrict__ Rout, int nan_to_origin) {
   const df xmin = K.xmin, idx = K.idx, ymin = K.ymin, idy = K.idy, ias = K.ias, one = {1.f, 0.f};
   const df soft = K.soft, zeps = K.zeps, m4pi = K.m4pi;
@@ -405,14 +409,15 @@ __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecD
       if (Rout) Rout[p] = Rd;
     }
     const int ix = (int)fx, iy = (int)fy;
-    const int c = ix * T.numy + iy;
-    cell[p] = c;
-    slot[p] = atomicAdd(hist + c, 1);
-    rec[0 * n + p] = dx;
-    rec[1 * n + p] = dy;
-    rec[2 * n + p] = c1;
-    rec[3 * n + p] = s1;
-    rec[4 * n + p] = df_mul(df_split_or_from(mass[p]), m4pi);
+    BinRec<df> r;
+    r.dx = dx;
+    r.dy = dy;
+    r.c1 = c1;
+    r.s1 = s1;
+    r.base = df_mul(df_split_or_from(mass[p]), m4pi);
+    r.cell = ix * T.numy + iy;
+    r.idx = atomicAdd(hist + r.cell, 1);
+    rec[p] = r;
   }
 }
 
@@ -472,19 +477,17 @@ __global__ void __launch_bounds__(kScanTile) k_scan_add(int* __restrict__ off, c
   if (i < ncell) off[i] += pref;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __restrict__ cell,
-                                                     const int* __restrict__ slot, const int* __restrict__ off,
-                                                     const R* __restrict__ rec, R* __restrict__ srec,
-                                                     int* __restrict__ scell, int* __restrict__ sorig) {
+// Counting-sort scatter: record p moves to off[cell] + its slot, carrying p.
+template <typename RT>
+__global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __restrict__ off,
+                                                     const BinRec<RT>* __restrict__ rec,
+                                                     BinRec<RT>* __restrict__ srec) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
-    const int c = cell[p];
-    const long long q = (long long)off[c] + slot[p];
-#pragma unroll
-    for (int k = 0; k < kRec; ++k) srec[k * n + q] = rec[k * n + p];
-    scell[q] = c;
-    sorig[q] = (int)p;
+    BinRec<RT> r = rec[p];
+    const long long q = (long long)off[r.cell] + r.idx;
+    r.idx = (int)p;
+    srec[q] = r;
   }
 }
 
@@ -495,24 +498,24 @@ __global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __r
 // for results written straight into host memory.
 template <typename R, bool SORTED>
 __global__ void __launch_bounds__(128) k_cyl_eval_sorted(CylTab<R> T, const R* __restrict__ F, long long n,
-                                                         const R* __restrict__ srec, const int* __restrict__ scell,
-                                                         const int* __restrict__ sorig, CylEvalOpts o, double* o0,
-                                                         double* o1, double* o2, double* o3, double* o4) {
+                                                         const BinRec<R>* __restrict__ recs, CylEvalOpts o,
+                                                         double* o0, double* o1, double* o2, double* o3,
+                                                         double* o4) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
-    const int c = scell[q];
-    const int ix = c / T.numy, iy = c - ix * T.numy;
+    const BinRec<R> r = recs[q];
+    const int ix = r.cell / T.numy, iy = r.cell - ix * T.numy;
     CylBins<R> B;
     B.node = ix * (T.numy + 1) + iy;
     R w[4];
-    weights_from_frac(srec[0 * n + q], srec[1 * n + q], w);
+    weights_from_frac(r.dx, r.dy, w);
     B.c00 = w[0];
     B.c10 = w[1];
     B.c01 = w[2];
     B.c11 = w[3];
     R v[9];
-    cyl_eval_bins(T, F, B, srec[2 * n + q], srec[3 * n + q], o, v);
-    const long long p = SORTED ? (long long)sorig[q] : q;
+    cyl_eval_bins(T, F, B, r.c1, r.s1, o, v);
+    const long long p = SORTED ? (long long)r.idx : q;
     if (o0) o0[p] = v[0];
     if (o1) o1[p] = v[1];
     if (o2) o2[p] = v[2];
@@ -568,9 +571,8 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 // warp-uniform so that the ballots see every lane.
 template <typename M, int MCAP, int RUN>
 __global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, long long n,
-                                                            const typename M::T* __restrict__ srec,
-                                                            const int* __restrict__ scell, double* __restrict__ D,
-                                                            size_t nnode) {
+                                                            const BinRec<typename M::T>* __restrict__ srec,
+                                                            double* __restrict__ D, size_t nnode) {
   using T = typename M::T;
   constexpr int NJ = 2 * MCAP + 1;
   constexpr int NE = NJ * 4;
@@ -633,13 +635,15 @@ __global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, 
     for (int u = 0; u < RUN; ++u) {
       const long long q = q0 + u;
       const bool valid = q < n;                 // also false for lanes past the last run
-      const int c = valid ? scell[q] : cur;
+      BinRec<T> r;
+      if (valid) r = srec[q];
+      const int c = valid ? r.cell : cur;
       flush(cur >= 0 && c != cur, cur);
       cur = c;
       if (!valid) continue;
       T w[4];
-      M::weights(srec[0 * n + q], srec[1 * n + q], w);
-      const T c1 = srec[2 * n + q], s1 = srec[3 * n + q], base = srec[4 * n + q];
+      M::weights(r.dx, r.dy, w);
+      const T c1 = r.c1, s1 = r.s1, base = r.base;
       T cprev = M::one(), sprev = M::zero(), ccur = c1, scur = s1;
 #pragma unroll
       for (int m = 0; m <= MCAP; ++m) {
@@ -735,25 +739,23 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, 
 // accumulated_eval_particles); SORTED as for k_cyl_eval_sorted.
 template <bool SORTED>
 __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
-                                                            const df* __restrict__ srec,
-                                                            const int* __restrict__ scell,
-                                                            const int* __restrict__ sorig, int m1, int m2,
+                                                            const BinRec<df>* __restrict__ recs, int m1, int m2,
                                                             double* o0, double* o1, double* o2, double* o3,
                                                             double* o4) {
   const int ny1 = T.numy + 1;
   const int stride = (T.mmax + 1) * 6;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
-    const int c = scell[q];
-    const int ix = c / T.numy, iy = c - ix * T.numy;
+    const BinRec<df> r = recs[q];
+    const int ix = r.cell / T.numy, iy = r.cell - ix * T.numy;
     const df* f00 = F + (size_t)(ix * ny1 + iy) * stride;
     const df* f01 = f00 + stride;
     const df* f10 = f00 + (size_t)ny1 * stride;
     const df* f11 = f10 + stride;
     df w[4];
-    df_weights(srec[0 * n + q], srec[1 * n + q], w);
+    df_weights(r.dx, r.dy, w);
     const df w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
-    const df c1 = srec[2 * n + q], s1 = srec[3 * n + q];
+    const df c1 = r.c1, s1 = r.s1;
     const df zero{0.f, 0.f};
     df p0 = zero, p = zero, fr = zero, fp = zero, fz = zero;
     df cprev{1.f, 0.f}, sprev = zero, ccur = c1, scur = s1;
@@ -783,7 +785,7 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, co
       fz = df_add(fz, fzm);
       fp = df_add(fp, fpm);
     }
-    const long long pidx = SORTED ? (long long)sorig[q] : q;
+    const long long pidx = SORTED ? (long long)r.idx : q;
     if (o0) o0[pidx] = df_to(p0);
     if (o1) o1[pidx] = df_to(p);
     if (o2) o2[pidx] = df_to(fr);
@@ -1027,7 +1029,7 @@ static int timing_mark(int k, cudaStream_t st) {
 }
 
 struct FusedLayout {
-  size_t grid, part, hist, off, tsum, cell, slot, rec, srec, scell, sorig, field, total;
+  size_t grid, part, hist, off, tsum, rec, srec, field, total;
 };
 
 static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) {
@@ -1041,12 +1043,9 @@ static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) 
   L.hist = take(ncell * sizeof(int));
   L.off = take(ncell * sizeof(int));
   L.tsum = take(kScanTile * sizeof(int));
-  L.cell = take((size_t)n * sizeof(int));
-  L.slot = take((size_t)n * sizeof(int));
-  L.rec = take((size_t)n * kRec * rs);
-  L.srec = take((size_t)n * kRec * rs);
-  L.scell = take((size_t)n * sizeof(int));
-  L.sorig = take((size_t)n * sizeof(int));
+  const size_t recb = precision == XT_F32 ? sizeof(BinRec<float>) : sizeof(BinRec<df>);
+  L.rec = take((size_t)n * recb);
+  L.srec = take((size_t)n * recb);
   L.field = take(h->nnode * (h->mmax + 1) * 6 * rs);
   L.total = o;
   return L;
@@ -1118,10 +1117,6 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   int* hist = reinterpret_cast<int*>(ws + L.hist);
   int* off = reinterpret_cast<int*>(ws + L.off);
   int* tsum = reinterpret_cast<int*>(ws + L.tsum);
-  int* cell = reinterpret_cast<int*>(ws + L.cell);
-  int* slot = reinterpret_cast<int*>(ws + L.slot);
-  int* scell = reinterpret_cast<int*>(ws + L.scell);
-  int* sorig = reinterpret_cast<int*>(ws + L.sorig);
   const int ncell = h->numx * h->numy;
   XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->nnode * sizeof(double), st));
   XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
@@ -1130,11 +1125,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   auto run = [&](auto tag) -> int {
     using R = decltype(tag);
     constexpr bool F64 = std::is_same<R, double>::value;
-    using RT = typename std::conditional<F64, df, float>::type;   // record type
-    using RM = typename std::conditional<F64, double, float>::type; // same-size type for moving records
+    using RT = typename std::conditional<F64, df, float>::type;   // record arithmetic
     const CylTab<R>& T = *reinterpret_cast<const CylTab<R>*>(F64 ? (const void*)&h->tab_d : (const void*)&h->tab_f);
-    RT* rec = reinterpret_cast<RT*>(ws + L.rec);
-    RT* srec = reinterpret_cast<RT*>(ws + L.srec);
+    BinRec<RT>* rec = reinterpret_cast<BinRec<RT>*>(ws + L.rec);
+    BinRec<RT>* srec = reinterpret_cast<BinRec<RT>*>(ws + L.srec);
     R* field = reinterpret_cast<R*>(ws + L.field);
     int rc;
     if ((rc = timing_mark(0, st))) return rc;
@@ -1143,10 +1137,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         const BinrecDf K{host_df(T.XMIN), host_df(T.inv_dX), host_df(T.YMIN), host_df(T.inv_dY),
                          host_df(T.inv_ascale), host_df(T.inv_hscale), host_df(1.0e-10), host_df(1.0e-8),
                          host_df(-FOUR_PI_C)};
-        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, K, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
+        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, K, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
+      } else {
+        k_cyl_binrec<float><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
       }
-      else
-        k_cyl_binrec<R, RT><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, cell, slot, rec, outs[5], nan_to_origin);
       XT_CHECK_LAUNCH("k_cyl_binrec");
       if ((rc = timing_mark(1, st))) return rc;
       {
@@ -1157,8 +1151,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         XT_CHECK_LAUNCH("k_scan_add");
       }
       if ((rc = timing_mark(2, st))) return rc;
-      k_cyl_scatter<RM><<<g256, 256, 0, st>>>(n, cell, slot, off, reinterpret_cast<const RM*>(rec),
-                                              reinterpret_cast<RM*>(srec), scell, sorig);
+      k_cyl_scatter<RT><<<g256, 256, 0, st>>>(n, off, rec, srec);
       XT_CHECK_LAUNCH("k_cyl_scatter");
       if ((rc = timing_mark(3, st))) return rc;
       // run length (particles summed in registers per thread before the FP64
@@ -1169,9 +1162,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         constexpr int RUN = decltype(rl)::value;
         const int gr = grid_for((n + RUN - 1) / RUN, 128, 8);
         using Mth = std::conditional_t<F64, DepDF, DepF32>;
-        k_cyl_deposit_sorted<Mth, MC, RUN><<<gr, 128, 0, st>>>(h->numy, h->mmax, n,
-                                                               reinterpret_cast<const typename Mth::T*>(srec),
-                                                               scell, D, h->nnode);
+        k_cyl_deposit_sorted<Mth, MC, RUN><<<gr, 128, 0, st>>>(h->numy, h->mmax, n, srec, D, h->nnode);
       };
       auto dep_m = [&](auto rl) {
         if (h->mmax <= 2) dep(std::integral_constant<int, 2>{}, rl);
@@ -1231,13 +1222,11 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       // particle order instead, so that each warp's writes over the host link
       // are coalesced rather than 8-byte scatters.
       const bool sorted = !host_out;
-      const RT* er = sorted ? srec : rec;
-      const int* ec = sorted ? scell : cell;
+      const BinRec<RT>* er = sorted ? srec : rec;
       if constexpr (F64) {
         auto ev = [&](auto srt) {
           k_cyl_eval_sorted_df<decltype(srt)::value><<<g128, 128, 0, st>>>(
-              T, reinterpret_cast<const df*>(field), n, er, ec, sorig, m1, m2, outs[0], outs[1], outs[2], outs[3],
-              outs[4]);
+              T, reinterpret_cast<const df*>(field), n, er, m1, m2, outs[0], outs[1], outs[2], outs[3], outs[4]);
         };
         if (sorted) ev(std::true_type{});
         else ev(std::false_type{});
@@ -1246,11 +1235,11 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         o.mode = XT_CYL_ACCUMULATED_EVAL_PARTICLES; o.m1 = m1; o.m2 = m2; o.mmax_use = h->mmax; o.no_odd = 0;
         o.perturb = 0; o.density = 0; o.nf = 6;
         if (sorted)
-          k_cyl_eval_sorted<R, true><<<g128, 128, 0, st>>>(T, field, n, er, ec, sorig, o, outs[0], outs[1], outs[2],
-                                                           outs[3], outs[4]);
+          k_cyl_eval_sorted<R, true><<<g128, 128, 0, st>>>(T, field, n, er, o, outs[0], outs[1], outs[2], outs[3],
+                                                           outs[4]);
         else
-          k_cyl_eval_sorted<R, false><<<g128, 128, 0, st>>>(T, field, n, er, ec, sorig, o, outs[0], outs[1],
-                                                            outs[2], outs[3], outs[4]);
+          k_cyl_eval_sorted<R, false><<<g128, 128, 0, st>>>(T, field, n, er, o, outs[0], outs[1], outs[2], outs[3],
+                                                            outs[4]);
       }
       XT_CHECK_LAUNCH("k_cyl_eval_sorted");
     }
