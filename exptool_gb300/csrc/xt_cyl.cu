@@ -27,6 +27,7 @@ struct CylHandle {
   size_t nnode;
   double* tab = nullptr;   // [8][mmax+1][norder][nnode]: potC rforceC zforceC densC potS rforceS zforceS densS
   float* tab_f32 = nullptr;  // the same tables rounded to FP32 (mixed path)
+  float* tab_lo = nullptr;   // FP32 remainders: tab_f32 + tab_lo is a double-float copy of tab
   CylTab<double> tab_d;
   CylTab<float> tab_f;
 };
@@ -39,9 +40,13 @@ static inline const float* tab_ptr_f32(const CylHandle* h, int which) {
   return h->tab_f32 + (size_t)which * (h->mmax + 1) * h->norder * h->nnode;
 }
 
-__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+// hi = FP32 rounding of a, lo = FP32 rounding of a - hi (table set-up, once).
+__global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float h = (float)a[i];
+    hi[i] = h;
+    lo[i] = (float)(a[i] - (double)h);
+  }
 }
 
 constexpr double FOUR_PI_C = 4.0 * PI;
@@ -671,17 +676,6 @@ __global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, 
   }
 }
 
-// In-place FP64 -> df conversion of a field (8 bytes either way).
-__global__ void k_split_df(double* __restrict__ f, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double v = f[i];
-    reinterpret_cast<df*>(f)[i] = df_from(v);
-  }
-}
-
-__device__ __forceinline__ df load_df(const df* p) { return *p; }
-__device__ __forceinline__ df load_df(const float* p) { return df{*p, 0.f}; }
-
 template <typename OT>
 __device__ __forceinline__ OT from_df(df v);
 template <>
@@ -689,13 +683,15 @@ __device__ __forceinline__ df from_df<df>(df v) { return v; }
 template <>
 __device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
 
-// Field for the mixed fused path: coefficients staged in shared memory as df,
-// accumulation in df over the FP32 table rows, FP32 output (no FP64 pipe
-// work at all).  Layout as k_cyl_field with nf = 6.
-template <typename TT, typename OT, int TN>
-__global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, const double* __restrict__ cosc,
-                                                    const double* __restrict__ sinc, int mmax, int norder,
-                                                    size_t nnode, OT* __restrict__ F) {
+// Field of the fused paths: coefficients staged in shared memory as df,
+// accumulation in df on the FP32 pipe (no FP64 pipe work at all).  SPLIT:
+// double-float tables hi + lo and a df field (FP64 path); otherwise the FP32
+// tables alone and an FP32 field (mixed path).  Layout as k_cyl_field with
+// nf = 6.
+template <typename OT, int TN, bool SPLIT>
+__global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi, const float* __restrict__ lo,
+                                                    const double* __restrict__ cosc, const double* __restrict__ sinc,
+                                                    int mmax, int norder, size_t nnode, OT* __restrict__ F) {
   extern __shared__ unsigned char smem_raw[];
   df* cf = reinterpret_cast<df*>(smem_raw);                       // [2][(mmax+1)*norder]
   OT* tile = reinterpret_cast<OT*>(cf + 2 * (mmax + 1) * norder);
@@ -716,16 +712,17 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const TT* __restrict__ tab, 
     if (node < nnode && !(m == 0 && f >= 3)) {
       const int ti = tmap[f];
       const df* coef = cf + ((ti >= 4) ? ncoef : 0) + m * norder;
-      const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
+      const size_t t0 = (size_t)ti * tsize + (size_t)m * norder * nnode + node;
+      auto row = [&](int k) { return df{hi[t0 + (size_t)k * nnode], SPLIT ? lo[t0 + (size_t)k * nnode] : 0.f}; };
       int k = 0;
       for (; k + 8 <= norder; k += 8) {   // eight table rows in flight, then the FMAs in order
-        TT v[8];
+        df v[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = t[(size_t)(k + u) * nnode];
+        for (int u = 0; u < 8; ++u) v[u] = row(k + u);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) acc = df_fma(coef[k + u], load_df(&v[u]), acc);
+        for (int u = 0; u < 8; ++u) acc = df_fma(coef[k + u], v[u], acc);
       }
-      for (; k < norder; ++k) acc = df_fma(coef[k], load_df(t + (size_t)k * nnode), acc);
+      for (; k < norder; ++k) acc = df_fma(coef[k], row(k), acc);
     }
     tile[nl * mf_total + mf] = from_df<OT>(acc);
   }
@@ -849,11 +846,14 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
   h->tab_f = CylTab<float>{mmax, norder, numx, numy, cmap, (float)XMIN, (float)dX, (float)YMIN, (float)dY,
                            (float)ascale, (float)hscale, (float)(1.0 / dX), (float)(1.0 / dY),
                            (float)(1.0 / ascale), (float)(1.0 / hscale)};
-  // FP32 copy of the tables for the mixed path (halves the table traffic of
-  // its contraction and field kernels)
-  e = cudaMalloc((void**)&h->tab_f32, 8 * tsize * sizeof(float));
+  // FP32 copy of the tables (the mixed path reads it alone: half the table
+  // traffic of its field kernel) and the FP32 remainders, which with it form
+  // the double-float tables of the FP64 fused field (FP32-pipe arithmetic,
+  // same 8 bytes per entry as FP64)
+  e = cudaMalloc((void**)&h->tab_f32, 16 * tsize * sizeof(float));
   if (e == cudaSuccess) {
-    k_to_f32<<<grid_for((long long)(8 * tsize), 256, 8), 256>>>(h->tab, h->tab_f32, 8 * tsize);
+    h->tab_lo = h->tab_f32 + 8 * tsize;
+    k_split_tab<<<grid_for((long long)(8 * tsize), 256, 8), 256>>>(h->tab, h->tab_f32, h->tab_lo, 8 * tsize);
     e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaGetLastError();
   }
@@ -1191,29 +1191,15 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     if ((rc = timing_mark(5, st))) return rc;
     constexpr int TN = 32;
     const int fblocks = (int)((h->nnode + TN - 1) / TN);
-    if constexpr (F64) {
-      // FP64 field, then split in place into double-float pairs for the evaluation
-      const size_t sm = TN * (size_t)(h->mmax + 1) * 6 * sizeof(double);
-      if (sm > 48 * 1024)
-        XT_CUDA(cudaFuncSetAttribute(k_cyl_field<double, TN, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sm));
-      k_cyl_field<double, TN, double><<<fblocks, 256, sm, st>>>(h->tab, cos_out, sin_out, h->mmax, h->norder,
-                                                               h->nnode, h->mmax, h->norder, 6,
-                                                               reinterpret_cast<double*>(field));
-      XT_CHECK_LAUNCH("k_cyl_field");
-      const size_t nf = h->nnode * (h->mmax + 1) * 6;
-      k_split_df<<<grid_for((long long)nf, 256, 8), 256, 0, st>>>(reinterpret_cast<double*>(field), nf);
-      XT_CHECK_LAUNCH("k_split_df");
-    } else {
-      // FP32 field from the FP32 tables, coefficients staged as double-float
-      const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) + TN * (size_t)(h->mmax + 1) * 6 * sizeof(float);
-      if (sm > 48 * 1024)
-        XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<float, float, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sm));
-      k_cyl_field2<float, float, TN><<<fblocks, 256, sm, st>>>(h->tab_f32, cos_out, sin_out, h->mmax, h->norder,
-                                                              h->nnode, reinterpret_cast<float*>(field));
-      XT_CHECK_LAUNCH("k_cyl_field2");
-    }
+    // FP64 path: double-float field from the double-float tables; mixed path:
+    // FP32 field from the FP32 tables (coefficients staged as df in both)
+    using FT = std::conditional_t<F64, df, float>;
+    const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) + TN * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
+    if (sm > 48 * 1024)
+      XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TN, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_cyl_field2<FT, TN, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, cos_out, sin_out, h->mmax, h->norder,
+                                                         h->nnode, reinterpret_cast<FT*>(field));
+    XT_CHECK_LAUNCH("k_cyl_field2");
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {
       // Device results are evaluated from the cell-sorted records (neighbouring
