@@ -26,8 +26,9 @@ struct CylHandle {
   double XMIN, dX, YMIN, dY, ascale, hscale;
   size_t nnode;
   double* tab = nullptr;   // [8][mmax+1][norder][nnode]: potC rforceC zforceC densC potS rforceS zforceS densS
-  float* tab_f32 = nullptr;  // the same tables rounded to FP32 (mixed path)
+  float* tab_f32 = nullptr;  // the same tables rounded to FP32 (mixed path), rows of pitch_f nodes
   float* tab_lo = nullptr;   // FP32 remainders: tab_f32 + tab_lo is a double-float copy of tab
+  size_t pitch_f = 0;        // row pitch of tab_f32 / tab_lo: nnode rounded up to 4 (16-byte node quads)
   CylTab<double> tab_d;
   CylTab<float> tab_f;
 };
@@ -37,15 +38,25 @@ static inline const double* tab_ptr(const CylHandle* h, int which) {
 }
 
 static inline const float* tab_ptr_f32(const CylHandle* h, int which) {
-  return h->tab_f32 + (size_t)which * (h->mmax + 1) * h->norder * h->nnode;
+  return h->tab_f32 + (size_t)which * (h->mmax + 1) * h->norder * h->pitch_f;
 }
 
-// hi = FP32 rounding of a, lo = FP32 rounding of a - hi (table set-up, once).
-__global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo, size_t n) {
+// hi = FP32 rounding of a, lo = FP32 rounding of a - hi, rows of nnode
+// entries re-laid with a pitch of `pitch` entries (padding zeroed); table
+// set-up, once.
+__global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo,
+                            size_t rows, size_t nnode, size_t pitch) {
+  const size_t n = rows * pitch;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float h = (float)a[i];
+    const size_t row = i / pitch, node = i - row * pitch;
+    float h = 0.f, l = 0.f;
+    if (node < nnode) {
+      const double v = a[row * nnode + node];
+      h = (float)v;
+      l = (float)(v - (double)h);
+    }
     hi[i] = h;
-    lo[i] = (float)(a[i] - (double)h);
+    lo[i] = l;
   }
 }
 
@@ -96,11 +107,13 @@ __global__ void __launch_bounds__(256) k_cyl_deposit(CylTab<R> T, const double* 
 }
 
 // Partial dot products: block (chunk, out) with out = (m*norder + k)*2 + cs.
+// (tables' rows are tpitch entries apart)
 template <typename TT>
 __global__ void __launch_bounds__(256) k_cyl_contract_partial(const TT* __restrict__ potC,
                                                               const TT* __restrict__ potS,
                                                               const double* __restrict__ D, int mmax, int norder,
-                                                              size_t nnode, int nchunk, double* __restrict__ part) {
+                                                              size_t nnode, size_t tpitch, int nchunk,
+                                                              double* __restrict__ part) {
   const int chunk = blockIdx.x;
   const int out = blockIdx.y;
   const int cs = out & 1;
@@ -108,7 +121,7 @@ __global__ void __launch_bounds__(256) k_cyl_contract_partial(const TT* __restri
   const int m = mk / norder;
   double acc = 0.0;
   if (!(cs == 1 && m == 0)) {
-    const TT* t = (cs ? potS : potC) + (size_t)mk * nnode;
+    const TT* t = (cs ? potS : potC) + (size_t)mk * tpitch;
     const double* d = D + (size_t)(2 * m + cs) * nnode;
     const size_t per = (nnode + nchunk - 1) / nchunk;
     const size_t lo = (size_t)chunk * per;
@@ -153,15 +166,17 @@ __global__ void k_cyl_contract_final(const double* __restrict__ part, int nout, 
 // Fields F[(node*(mmax+1) + m)*nf + f] for m <= muse (m > muse left 0).
 // A block owns TN consecutive nodes; thread t reads table rows coalesced
 // along nodes and the tile is written back contiguously through shared memory.
+// (table rows tpitch entries apart)
 template <typename R, int TN, typename TT>
 __global__ void __launch_bounds__(256) k_cyl_field(const TT* __restrict__ tab, const double* __restrict__ cosc,
                                                    const double* __restrict__ sinc, int mmax, int norder,
-                                                   size_t nnode, int muse, int nuse, int nf, R* __restrict__ F) {
+                                                   size_t nnode, size_t tpitch, int muse, int nuse, int nf,
+                                                   R* __restrict__ F) {
   extern __shared__ unsigned char smem_raw[];
   R* tile = reinterpret_cast<R*>(smem_raw);
   const int mf_total = (mmax + 1) * nf;
   const size_t node0 = (size_t)blockIdx.x * TN;
-  const size_t tsize = (size_t)(mmax + 1) * norder * nnode;
+  const size_t tsize = (size_t)(mmax + 1) * norder * tpitch;
   // table index of field f: PC RC ZC PS RS ZS DC DS -> 0 1 2 4 5 6 3 7
   const int tmap[8] = {0, 1, 2, 4, 5, 6, 3, 7};
   for (int idx = threadIdx.x; idx < TN * mf_total; idx += blockDim.x) {
@@ -173,16 +188,16 @@ __global__ void __launch_bounds__(256) k_cyl_field(const TT* __restrict__ tab, c
     if (node < nnode && m <= muse && !(m == 0 && (f == 3 || f == 4 || f == 5 || f == 7))) {
       const int ti = tmap[f];
       const double* coef = (ti >= 4) ? sinc : cosc;
-      const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * nnode + node;
+      const TT* t = tab + (size_t)ti * tsize + (size_t)m * norder * tpitch + node;
       int k = 0;
       for (; k + 8 <= nuse; k += 8) {     // eight table rows in flight, then the FMAs in order
         TT v[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = t[(size_t)(k + u) * nnode];
+        for (int u = 0; u < 8; ++u) v[u] = t[(size_t)(k + u) * tpitch];
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc += coef[m * norder + k + u] * (double)v[u];
       }
-      for (; k < nuse; ++k) acc += coef[m * norder + k] * (double)t[(size_t)k * nnode];
+      for (; k < nuse; ++k) acc += coef[m * norder + k] * (double)t[(size_t)k * tpitch];
     }
     tile[nl * mf_total + mf] = (R)acc;
   }
@@ -541,27 +556,32 @@ __device__ __forceinline__ void df_weights(df dx, df dy, df w[4]) {
 
 // Arithmetic of the sorted deposit: FP32 sums (mixed path) or double-float
 // sums (FP64 path), both widened to FP64 for the atomics.
+// T is the record arithmetic, A the per-run sum (lazily renormalised for df).
 struct DepF32 {
   using T = float;
+  using A = float;
   static __device__ __forceinline__ T zero() { return 0.f; }
   static __device__ __forceinline__ T one() { return 1.f; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return a * b + c; }
+  static __device__ __forceinline__ A acc0() { return 0.f; }
+  static __device__ __forceinline__ void acc(A& a, T x, T y) { a = x * y + a; }
   static __device__ __forceinline__ T cheb(T c1, T cur, T prev) { return 2.f * c1 * cur - prev; }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
-  static __device__ __forceinline__ double wide(T a) { return (double)a; }
+  static __device__ __forceinline__ double wide(A a) { return (double)a; }
 };
 struct DepDF {
   using T = df;
+  using A = dacc;
   static __device__ __forceinline__ T zero() { return df{0.f, 0.f}; }
   static __device__ __forceinline__ T one() { return df{1.f, 0.f}; }
   static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return df_fma(a, b, c); }
+  static __device__ __forceinline__ A acc0() { return dacc{}; }
+  static __device__ __forceinline__ void acc(A& a, T x, T y) { a.fma(x, y); }
   static __device__ __forceinline__ T cheb(T c1, T cur, T prev) {
     return df_sub(df_scale(df_mul(c1, cur), 2.f), prev);
   }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { df_weights(dx, dy, w); }
-  static __device__ __forceinline__ double wide(T a) { return df_to(a); }
+  static __device__ __forceinline__ double wide(A a) { return df_to(a.raw()); }
 };
 
 constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
@@ -575,24 +595,25 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 // instruction per value however few lanes are active.)  Loops are
 // warp-uniform so that the ballots see every lane.
 template <typename M, int MCAP, int RUN>
-__global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, long long n,
+__global__ void __launch_bounds__(128, MCAP <= 6 ? 3 : 2) k_cyl_deposit_sorted(int numy, int mmax, long long n,
                                                             const BinRec<typename M::T>* __restrict__ srec,
                                                             double* __restrict__ D, size_t nnode) {
   using T = typename M::T;
+  using A = typename M::A;
   constexpr int NJ = 2 * MCAP + 1;
   constexpr int NE = NJ * 4;
   constexpr int PITCH = NE + 1;                 // conflict-free parking of up to 8 lanes
-  __shared__ T park[4][kDepSlots][PITCH];
+  __shared__ A park[4][kDepSlots][PITCH];
   __shared__ int park_node[4][kDepSlots];     // lower-left node of the parked lane's cell
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int ny1 = numy + 1;
   const int nju = 2 * mmax + 1;                 // accumulators in use
   const long long nrun = (n + RUN - 1) / RUN;
-  T acc[NJ][4];
+  A acc[NJ][4];
 #pragma unroll
   for (int j = 0; j < NJ; ++j)
 #pragma unroll
-    for (int k = 0; k < 4; ++k) acc[j][k] = M::zero();
+    for (int k = 0; k < 4; ++k) acc[j][k] = M::acc0();
 
   // park the sums of the lanes in `want`, batch by batch, and deposit them
   auto flush = [&](bool want, int cell) {
@@ -613,7 +634,7 @@ __global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, 
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             park[wib][sidx][j * 4 + k] = acc[j][k];
-            acc[j][k] = M::zero();
+            acc[j][k] = M::acc0();
           }
       }
       __syncwarp();
@@ -664,11 +685,11 @@ __global__ void __launch_bounds__(128) k_cyl_deposit_sorted(int numy, int mmax, 
         const T wc = M::mul(base, cm);
         const int jc = (m == 0) ? 0 : 2 * m - 1;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) acc[jc][k] = M::fma(wc, w[k], acc[jc][k]);
+        for (int k = 0; k < 4; ++k) M::acc(acc[jc][k], wc, w[k]);
         if (m > 0) {
           const T ws = M::mul(base, sm);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) acc[2 * m][k] = M::fma(ws, w[k], acc[2 * m][k]);
+          for (int k = 0; k < 4; ++k) M::acc(acc[2 * m][k], ws, w[k]);
         }
       }
     }
@@ -684,14 +705,20 @@ template <>
 __device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
 
 // Field of the fused paths: coefficients staged in shared memory as df,
-// accumulation in df on the FP32 pipe (no FP64 pipe work at all).  SPLIT:
+// lazily renormalised df sums on the FP32 pipe (no FP64 pipe work at all).  SPLIT:
 // double-float tables hi + lo and a df field (FP64 path); otherwise the FP32
-// tables alone and an FP32 field (mixed path).  Layout as k_cyl_field with
-// nf = 6.
-template <typename OT, int TN, bool SPLIT>
+// tables alone and an FP32 field (mixed path).  Each thread computes one
+// (m, field) entry for a quad of consecutive nodes from 16-byte loads of the
+// tables (rows of `pitch` entries, a multiple of 4), with four table rows in
+// flight and four independent sums; a warp covers 128 nodes.  The block's
+// QN = 4 * TQ nodes are written back contiguously through shared memory in the
+// layout of k_cyl_field with nf = 6.
+template <typename OT, int TQ, bool SPLIT>
 __global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                    const double* __restrict__ cosc, const double* __restrict__ sinc,
-                                                    int mmax, int norder, size_t nnode, OT* __restrict__ F) {
+                                                    size_t pitch, const double* __restrict__ cosc,
+                                                    const double* __restrict__ sinc, int mmax, int norder,
+                                                    size_t nnode, OT* __restrict__ F) {
+  constexpr int QN = 4 * TQ;
   extern __shared__ unsigned char smem_raw[];
   df* cf = reinterpret_cast<df*>(smem_raw);                       // [2][(mmax+1)*norder]
   OT* tile = reinterpret_cast<OT*>(cf + 2 * (mmax + 1) * norder);
@@ -700,34 +727,53 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi
   __syncthreads();
   const int nf = 6;
   const int mf_total = (mmax + 1) * nf;
-  const size_t node0 = (size_t)blockIdx.x * TN;
-  const size_t tsize = (size_t)(mmax + 1) * norder * nnode;
+  const size_t node0 = (size_t)blockIdx.x * QN;
+  const size_t tsize = (size_t)(mmax + 1) * norder * pitch;
   const int tmap[6] = {0, 1, 2, 4, 5, 6};
-  for (int idx = threadIdx.x; idx < TN * mf_total; idx += blockDim.x) {
-    const int nl = idx % TN;
-    const int mf = idx / TN;
+  for (int task = threadIdx.x; task < TQ * mf_total; task += blockDim.x) {
+    const int ql = task % TQ;
+    const int mf = task / TQ;
     const int m = mf / nf, f = mf % nf;
-    const size_t node = node0 + nl;
-    df acc{0.f, 0.f};
+    const size_t node = node0 + 4 * ql;
+    dacc acc[4];
     if (node < nnode && !(m == 0 && f >= 3)) {
       const int ti = tmap[f];
       const df* coef = cf + ((ti >= 4) ? ncoef : 0) + m * norder;
-      const size_t t0 = (size_t)ti * tsize + (size_t)m * norder * nnode + node;
-      auto row = [&](int k) { return df{hi[t0 + (size_t)k * nnode], SPLIT ? lo[t0 + (size_t)k * nnode] : 0.f}; };
+      const size_t t0 = (size_t)ti * tsize + (size_t)m * norder * pitch + node;
       int k = 0;
-      for (; k + 8 <= norder; k += 8) {   // eight table rows in flight, then the FMAs in order
-        df v[8];
+      for (; k + 4 <= norder; k += 4) {
+        float4 vh[4], vl[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = row(k + u);
+        for (int u = 0; u < 4; ++u) {
+          vh[u] = *reinterpret_cast<const float4*>(hi + t0 + (size_t)(k + u) * pitch);
+          vl[u] = SPLIT ? *reinterpret_cast<const float4*>(lo + t0 + (size_t)(k + u) * pitch)
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) acc = df_fma(coef[k + u], v[u], acc);
+        for (int u = 0; u < 4; ++u) {
+          const df c = coef[k + u];
+          acc[0].fma(c, df{vh[u].x, vl[u].x});
+          acc[1].fma(c, df{vh[u].y, vl[u].y});
+          acc[2].fma(c, df{vh[u].z, vl[u].z});
+          acc[3].fma(c, df{vh[u].w, vl[u].w});
+        }
       }
-      for (; k < norder; ++k) acc = df_fma(coef[k], row(k), acc);
+      for (; k < norder; ++k) {
+        const float4 vh = *reinterpret_cast<const float4*>(hi + t0 + (size_t)k * pitch);
+        const float4 vl = SPLIT ? *reinterpret_cast<const float4*>(lo + t0 + (size_t)k * pitch)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+        const df c = coef[k];
+        acc[0].fma(c, df{vh.x, vl.x});
+        acc[1].fma(c, df{vh.y, vl.y});
+        acc[2].fma(c, df{vh.z, vl.z});
+        acc[3].fma(c, df{vh.w, vl.w});
+      }
     }
-    tile[nl * mf_total + mf] = from_df<OT>(acc);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tile[(4 * ql + j) * mf_total + mf] = from_df<OT>(acc[j].value());
   }
   __syncthreads();
-  const size_t nvalid = (node0 + TN <= nnode) ? TN : (nnode - node0);
+  const size_t nvalid = (node0 + QN <= nnode) ? QN : (nnode - node0);
   OT* dst = F + node0 * mf_total;
   for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) dst[idx] = tile[idx];
 }
@@ -753,41 +799,57 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, co
     df_weights(r.dx, r.dy, w);
     const df w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
     const df c1 = r.c1, s1 = r.s1;
-    const df zero{0.f, 0.f};
-    df p0 = zero, p = zero, fr = zero, fp = zero, fz = zero;
-    df cprev{1.f, 0.f}, sprev = zero, ccur = c1, scur = s1;
+    // bilinear interpolation of the six fields of order m (lazy df sums, read
+    // unnormalised by the products that follow)
+    auto interp = [&](int m, df v[6]) {
+      const int b = m * 6;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        dacc a;
+        a.fma(f00[b + k], w0);
+        a.fma(f10[b + k], w1);
+        a.fma(f01[b + k], w2);
+        a.fma(f11[b + k], w3);
+        v[k] = a.raw();
+      }
+    };
+    df p0{0.f, 0.f};
+    dacc p, fr, fp, fz;
+    if (m1 <= 0 && m2 >= 0) {                   // m = 0: cos 0 = 1, sin 0 = 0
+      df v[6];
+      interp(0, v);
+      p0 = v[0];
+      fr.s = v[1].h; fr.e = v[1].l;
+      fz.s = v[2].h; fz.e = v[2].l;
+    }
+    df cprev{1.f, 0.f}, sprev{0.f, 0.f}, ccur = c1, scur = s1;
 #pragma unroll 1
-    for (int m = 0; m <= T.mmax; ++m) {
+    for (int m = 1; m <= T.mmax; ++m) {
       df cm, sm;
-      if (m == 0) { cm = df{1.f, 0.f}; sm = zero; }
-      else if (m == 1) { cm = c1; sm = s1; }
+      if (m == 1) { cm = c1; sm = s1; }
       else {
         cm = df_sub(df_scale(df_mul(c1, ccur), 2.f), cprev);
         sm = df_sub(df_scale(df_mul(c1, scur), 2.f), sprev);
         cprev = ccur; sprev = scur; ccur = cm; scur = sm;
       }
       if (m < m1 || m > m2) continue;
-      const int b = m * 6;
       df v[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k)
-        v[k] = df_fma(f11[b + k], w3, df_fma(f01[b + k], w2, df_fma(f10[b + k], w1, df_mul(f00[b + k], w0))));
-      const df pm = df_fma(cm, v[0], df_mul(sm, v[3]));
-      const df frm = df_fma(cm, v[1], df_mul(sm, v[4]));
-      const df fzm = df_fma(cm, v[2], df_mul(sm, v[5]));
-      const df fpm = df_scale(df_sub(df_mul(sm, v[0]), df_mul(cm, v[3])), (float)m);
-      if (m == 0) p0 = pm;
-      else p = df_add(p, pm);
-      fr = df_add(fr, frm);
-      fz = df_add(fz, fzm);
-      fp = df_add(fp, fpm);
+      interp(m, v);
+      p.fma(cm, v[0]);
+      p.fma(sm, v[3]);
+      fr.fma(cm, v[1]);
+      fr.fma(sm, v[4]);
+      fz.fma(cm, v[2]);
+      fz.fma(sm, v[5]);
+      fp.fma(df_scale(sm, (float)m), v[0]);     // m (sin(m phi) v0 - cos(m phi) v3)
+      fp.fma(df_neg(df_scale(cm, (float)m)), v[3]);
     }
     const long long pidx = SORTED ? (long long)r.idx : q;
     if (o0) o0[pidx] = df_to(p0);
-    if (o1) o1[pidx] = df_to(p);
-    if (o2) o2[pidx] = df_to(fr);
-    if (o3) o3[pidx] = df_to(fp);
-    if (o4) o4[pidx] = df_to(fz);
+    if (o1) o1[pidx] = df_to(p.raw());
+    if (o2) o2[pidx] = df_to(fr.raw());
+    if (o3) o3[pidx] = df_to(fp.raw());
+    if (o4) o4[pidx] = df_to(fz.raw());
   }
 }
 
@@ -850,10 +912,13 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
   // traffic of its field kernel) and the FP32 remainders, which with it form
   // the double-float tables of the FP64 fused field (FP32-pipe arithmetic,
   // same 8 bytes per entry as FP64)
-  e = cudaMalloc((void**)&h->tab_f32, 16 * tsize * sizeof(float));
+  h->pitch_f = (h->nnode + 3) & ~(size_t)3;
+  const size_t rows = 8 * (size_t)(mmax + 1) * norder;
+  e = cudaMalloc((void**)&h->tab_f32, 2 * rows * h->pitch_f * sizeof(float));
   if (e == cudaSuccess) {
-    h->tab_lo = h->tab_f32 + 8 * tsize;
-    k_split_tab<<<grid_for((long long)(8 * tsize), 256, 8), 256>>>(h->tab, h->tab_f32, h->tab_lo, 8 * tsize);
+    h->tab_lo = h->tab_f32 + rows * h->pitch_f;
+    k_split_tab<<<grid_for((long long)(rows * h->pitch_f), 256, 8), 256>>>(h->tab, h->tab_f32, h->tab_lo, rows,
+                                                                           h->nnode, h->pitch_f);
     e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaGetLastError();
   }
@@ -917,10 +982,10 @@ int xt_cyl_accumulate(void* handle, const double* x, const double* y, const doub
   dim3 g(kContractChunks, nout);
   if (precision == XT_F64)
     k_cyl_contract_partial<double><<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder, h->nnode,
-                                                      kContractChunks, part);
+                                                      h->nnode, kContractChunks, part);
   else
     k_cyl_contract_partial<float><<<g, 256, 0, st>>>(tab_ptr_f32(h, 0), tab_ptr_f32(h, 4), D, h->mmax, h->norder,
-                                                     h->nnode, kContractChunks, part);
+                                                     h->nnode, h->pitch_f, kContractChunks, part);
   XT_CHECK_LAUNCH("k_cyl_contract_partial");
   k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
   XT_CHECK_LAUNCH("k_cyl_contract_final");
@@ -956,14 +1021,16 @@ int xt_cyl_prepare(void* handle, const double* cos_c, const double* sin_c, int m
     const size_t sm = TN * mf * sizeof(double);
     if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<double, TN, double>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field<double, TN, double><<<blocks, 256, sm, st>>>(h->tab, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
-                                                    nmax_use, nf, static_cast<double*>(field));
+    k_cyl_field<double, TN, double><<<blocks, 256, sm, st>>>(h->tab, cos_c, sin_c, h->mmax, h->norder, h->nnode,
+                                                             h->nnode, mmax_use, nmax_use, nf,
+                                                             static_cast<double*>(field));
   } else {
     const size_t sm = TN * mf * sizeof(float);
     if (sm > 48 * 1024) XT_CUDA(cudaFuncSetAttribute(k_cyl_field<float, TN, float>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field<float, TN, float><<<blocks, 256, sm, st>>>(h->tab_f32, cos_c, sin_c, h->mmax, h->norder, h->nnode, mmax_use,
-                                                   nmax_use, nf, static_cast<float*>(field));
+    k_cyl_field<float, TN, float><<<blocks, 256, sm, st>>>(h->tab_f32, cos_c, sin_c, h->mmax, h->norder, h->nnode,
+                                                           h->pitch_f, mmax_use, nmax_use, nf,
+                                                           static_cast<float*>(field));
   }
   XT_CHECK_LAUNCH("k_cyl_field");
   return XT_OK;
@@ -1184,21 +1251,22 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     // coefficient contraction from the FP64 tables in both precisions: it is a
     // reduction of the accumulated sums and stays FP64
     k_cyl_contract_partial<double><<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder,
-                                                      h->nnode, kContractChunks, part);
+                                                      h->nnode, h->nnode, kContractChunks, part);
     XT_CHECK_LAUNCH("k_cyl_contract_partial");
     k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
     if ((rc = timing_mark(5, st))) return rc;
-    constexpr int TN = 32;
-    const int fblocks = (int)((h->nnode + TN - 1) / TN);
     // FP64 path: double-float field from the double-float tables; mixed path:
     // FP32 field from the FP32 tables (coefficients staged as df in both)
+    constexpr int TQ = 32;   // node quads per block
+    const int fblocks = (int)((h->nnode + 4 * TQ - 1) / (4 * TQ));
     using FT = std::conditional_t<F64, df, float>;
-    const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) + TN * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
+    const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) +
+                      4 * TQ * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
     if (sm > 48 * 1024)
-      XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TN, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field2<FT, TN, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, cos_out, sin_out, h->mmax, h->norder,
-                                                         h->nnode, reinterpret_cast<FT*>(field));
+      XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TQ, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_cyl_field2<FT, TQ, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, cos_out, sin_out, h->mmax,
+                                                         h->norder, h->nnode, reinterpret_cast<FT*>(field));
     XT_CHECK_LAUNCH("k_cyl_field2");
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {

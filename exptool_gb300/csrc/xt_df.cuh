@@ -56,6 +56,29 @@ __device__ __forceinline__ df df_mul(df a, df b) {
 // a * b + c with one renormalisation.
 __device__ __forceinline__ df df_fma(df a, df b, df c) { return df_add(df_mul(a, b), c); }
 
+// Lazily renormalised sum of df products (12 FP32 operations a term instead
+// of df_fma's 18): s collects the leading product parts through TwoSum, e the
+// TwoSum and TwoProd errors and the FP32 cross terms.  (s, e) is not kept
+// normalised, |e| stays ~2^-23 |s|, so it may be read directly as a df operand
+// of further products (the dropped lo*lo term is ~2^-46 relative); after n
+// terms the error is ~n 2^-47 of the sum of |terms|.
+struct dacc {
+  float s = 0.f, e = 0.f;
+  __device__ __forceinline__ void fma(df x, df y) {
+    const float p = __fmul_rn(x.h, y.h);
+    float pe = __fmaf_rn(x.h, y.h, -p);
+    pe = __fmaf_rn(x.h, y.l, pe);
+    pe = __fmaf_rn(x.l, y.h, pe);
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v));
+    s = t;
+    e = __fadd_rn(e, __fadd_rn(err, pe));
+  }
+  __device__ __forceinline__ df raw() const { return {s, e}; }
+  __device__ __forceinline__ df value() const { return fast_two_sum(s, e); }
+};
+
 // multiply by a small exact float (an integer m or 2)
 __device__ __forceinline__ df df_scale(df a, float s) {
   const float p = __fmul_rn(a.h, s);
