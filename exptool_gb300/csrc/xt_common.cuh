@@ -41,6 +41,7 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // Grid size for a grid-stride loop over n items: a multiple of the SM count
 // (152 on GB300) times the resident blocks per SM, capped by the work.
 int grid_for(long long n, int block, int blocks_per_sm = 8);
+int sm_count();   // multiprocessors of the current device (cached)
 
 // Where a pointer lives, as far as kernels are concerned (XT_PTR_* values of
 // the public header): device (or managed) memory, pinned host memory, other

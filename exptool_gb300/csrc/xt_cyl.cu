@@ -11,6 +11,7 @@
 // contracts the coefficients with the tables into per-node fields first
 // (cos/sin-weighted pot, rforce, zforce[, dens] per m), so each particle
 // reads 4 corners x (mmax+1) x 6 values instead of 4 x 6 x (mmax+1) x norder.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
@@ -567,7 +568,7 @@ struct DepF32 {
   static __device__ __forceinline__ void acc(A& a, T x, T y) { a = x * y + a; }
   static __device__ __forceinline__ T cheb(T c1, T cur, T prev) { return 2.f * c1 * cur - prev; }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
-  static __device__ __forceinline__ double wide(A a) { return (double)a; }
+  static __device__ __forceinline__ void deposit(double* d, A a) { atomicAdd(d, (double)a); }
 };
 struct DepDF {
   using T = df;
@@ -581,7 +582,7 @@ struct DepDF {
     return df_sub(df_scale(df_mul(c1, cur), 2.f), prev);
   }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { df_weights(dx, dy, w); }
-  static __device__ __forceinline__ double wide(A a) { return df_to(a.raw()); }
+  static __device__ __forceinline__ void deposit(double* d, A a) { atomicAdd(d, df_to(a.raw())); }
 };
 
 constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
@@ -593,69 +594,76 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 // them to FP64 and issues the atomics, 32 entries per instruction.  (A
 // divergent per-lane flush would occupy the FP64 unit for a full warp
 // instruction per value however few lanes are active.)  Loops are
-// warp-uniform so that the ballots see every lane.
-template <typename M, int MCAP, int RUN>
-__global__ void __launch_bounds__(128, MCAP <= 6 ? 3 : 2) k_cyl_deposit_sorted(int numy, int mmax, long long n,
-                                                            const BinRec<typename M::T>* __restrict__ srec,
-                                                            double* __restrict__ D, size_t nnode) {
+// warp-uniform so that the ballots see every lane.  With NPASS = 2 a run is
+// deposited in two passes over its records, orders m <= MCAP/2 and then the
+// rest, so that half the sums are live at a time (double-float sums: 104 ->
+// 56 registers of accumulators, for more resident warps; the second pass
+// re-reads the run's records from L1).
+template <typename M, int MCAP, int RUN, int NPASS>
+__global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
+    k_cyl_deposit_sorted(int numy, int mmax, long long n, const BinRec<typename M::T>* __restrict__ srec,
+                         double* __restrict__ D, size_t plane) {
   using T = typename M::T;
   using A = typename M::A;
-  constexpr int NJ = 2 * MCAP + 1;
-  constexpr int NE = NJ * 4;
-  constexpr int PITCH = NE + 1;                 // conflict-free parking of up to 8 lanes
+  constexpr int MH = NPASS == 2 ? MCAP / 2 : MCAP;      // last order of the first pass
+  constexpr int NJ0 = 2 * MH + 1, NJ1 = 2 * (MCAP - MH);
+  constexpr int NEMAX = 4 * (NJ0 > NJ1 ? NJ0 : NJ1);
+  constexpr int PITCH = NEMAX + 1;              // conflict-free parking of up to 8 lanes
   __shared__ A park[4][kDepSlots][PITCH];
   __shared__ int park_node[4][kDepSlots];     // lower-left node of the parked lane's cell
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int ny1 = numy + 1;
-  const int nju = 2 * mmax + 1;                 // accumulators in use
+  const int nju = 2 * mmax + 1;                 // sums in use (global index j)
   const long long nrun = (n + RUN - 1) / RUN;
-  A acc[NJ][4];
-#pragma unroll
-  for (int j = 0; j < NJ; ++j)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[j][k] = M::acc0();
 
-  // park the sums of the lanes in `want`, batch by batch, and deposit them
-  auto flush = [&](bool want, int cell) {
-    unsigned pend = __ballot_sync(0xffffffffu, want);
-    while (pend) {
-      unsigned batch = 0, rest = pend;
-      for (int i = 0; i < kDepSlots && rest; ++i) {
-        batch |= rest & (0u - rest);
-        rest &= rest - 1;
-      }
-      const int nb = __popc(batch);
-      if (batch & (1u << lane)) {
-        const int sidx = __popc(batch & ((1u << lane) - 1));
-        const int ix = cell / numy, iy = cell - ix * numy;
-        park_node[wib][sidx] = ix * ny1 + iy;
+  auto run_pass = [&](long long q0, auto pass_tag) {
+    constexpr int PASS = decltype(pass_tag)::value;
+    constexpr int MLO = PASS == 0 ? 0 : MH + 1, MHI = PASS == 0 ? MH : MCAP;
+    constexpr int J0 = PASS == 0 ? 0 : 2 * MH + 1;
+    constexpr int NJP = PASS == 0 ? NJ0 : NJ1;
+    constexpr int NE = 4 * NJP;
+    A acc[NJP][4];
 #pragma unroll
-        for (int j = 0; j < NJ; ++j)
+    for (int j = 0; j < NJP; ++j)
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            park[wib][sidx][j * 4 + k] = acc[j][k];
-            acc[j][k] = M::acc0();
-          }
-      }
-      __syncwarp();
-      for (int i = lane; i < nb * NE; i += 32) {
-        const int sidx = i / NE, e = i - sidx * NE;
-        const int j = e >> 2, k = e & 3;
-        if (j < nju) {
-          const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
-          const int m = (j + 1) >> 1;          // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
-          const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
-          atomicAdd(D + (size_t)(2 * m + cs) * nnode + node, M::wide(park[wib][sidx][e]));
+      for (int k = 0; k < 4; ++k) acc[j][k] = M::acc0();
+    // park the sums of the lanes in `want`, batch by batch, and deposit them
+    auto flush = [&](bool want, int cell) {
+      unsigned pend = __ballot_sync(0xffffffffu, want);
+      while (pend) {
+        unsigned batch = 0, rest = pend;
+        for (int i = 0; i < kDepSlots && rest; ++i) {
+          batch |= rest & (0u - rest);
+          rest &= rest - 1;
         }
+        const int nb = __popc(batch);
+        if (batch & (1u << lane)) {
+          const int sidx = __popc(batch & ((1u << lane) - 1));
+          const int ix = cell / numy, iy = cell - ix * numy;
+          park_node[wib][sidx] = ix * ny1 + iy;
+#pragma unroll
+          for (int j = 0; j < NJP; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              park[wib][sidx][j * 4 + k] = acc[j][k];
+              acc[j][k] = M::acc0();
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < nb * NE; i += 32) {
+          const int sidx = i / NE, e = i - sidx * NE;
+          const int j = J0 + (e >> 2), k = e & 3;
+          if (j < nju) {
+            const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
+            const int m = (j + 1) >> 1;        // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
+            const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
+            M::deposit(D + (size_t)(2 * m + cs) * plane + node, park[wib][sidx][e]);
+          }
+        }
+        __syncwarp();
+        pend &= ~batch;
       }
-      __syncwarp();
-      pend &= ~batch;
-    }
-  };
-
-  for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); r0 < nrun;
-       r0 += (long long)gridDim.x * blockDim.x) {
-    const long long q0 = (r0 + lane) * RUN;
+    };
     int cur = -1;
 #pragma unroll 1
     for (int u = 0; u < RUN; ++u) {
@@ -672,7 +680,7 @@ __global__ void __launch_bounds__(128, MCAP <= 6 ? 3 : 2) k_cyl_deposit_sorted(i
       const T c1 = r.c1, s1 = r.s1, base = r.base;
       T cprev = M::one(), sprev = M::zero(), ccur = c1, scur = s1;
 #pragma unroll
-      for (int m = 0; m <= MCAP; ++m) {
+      for (int m = 0; m <= MHI; ++m) {
         if (m > mmax) break;
         T cm, sm;
         if (m == 0) { cm = M::one(); sm = M::zero(); }
@@ -682,18 +690,28 @@ __global__ void __launch_bounds__(128, MCAP <= 6 ? 3 : 2) k_cyl_deposit_sorted(i
           sm = M::cheb(c1, scur, sprev);
           cprev = ccur; sprev = scur; ccur = cm; scur = sm;
         }
+        if (m < MLO) continue;
         const T wc = M::mul(base, cm);
-        const int jc = (m == 0) ? 0 : 2 * m - 1;
+        const int jc = ((m == 0) ? 0 : 2 * m - 1) - J0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) M::acc(acc[jc][k], wc, w[k]);
         if (m > 0) {
           const T ws = M::mul(base, sm);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) M::acc(acc[2 * m][k], ws, w[k]);
+          for (int k = 0; k < 4; ++k) M::acc(acc[2 * m - J0][k], ws, w[k]);
         }
       }
     }
     flush(cur >= 0, cur);
+  };
+
+  for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); r0 < nrun;
+       r0 += (long long)gridDim.x * blockDim.x) {
+    const long long q0 = (r0 + lane) * RUN;
+    run_pass(q0, std::integral_constant<int, 0>{});
+    if constexpr (NPASS == 2) {
+      if (mmax > MH) run_pass(q0, std::integral_constant<int, 1>{});
+    }
   }
 }
 
@@ -854,6 +872,83 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, co
 }
 
 static const int kContractChunks = 8;
+static const int kContractChunksDf = 64;   // most node chunks of k_cyl_contract_df
+
+// Coefficient contraction of the fused paths:
+//   cos/sin[m][k] = sum over nodes of D[2m+cs][node] * pot{C,S}[m][k][node].
+// Block (chunk, m, cs) takes a range of node quads; each thread multiplies
+// the quads' FP64 sums (split into float pairs by integer operations) by the
+// double-float tables (16-byte loads of hi and lo, rows of `pitch` entries,
+// six rows in flight) for all k <= KMAX at once, in lazily renormalised df
+// sums.  The block's sums are reduced in df (warp shuffles, then shared
+// memory) and stored per chunk as FP64 for k_cyl_contract_final.  D planes and
+// table rows share the pitch; padding entries are zero in both.
+template <int KMAX>
+__global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict__ hi, const float* __restrict__ lo,
+                                                         size_t pitch, const double* __restrict__ D, int mmax,
+                                                         int norder, size_t nnode, int nchunk,
+                                                         double* __restrict__ part) {
+  constexpr int RB = 6;                         // rows in flight
+  static_assert(KMAX % RB == 0, "KMAX must be a multiple of the row batch");
+  const int chunk = blockIdx.x, m = blockIdx.y, cs = blockIdx.z;
+  dacc acc[KMAX];
+  if (!(cs == 1 && m == 0)) {
+    const int nq = (int)((nnode + 3) / 4);
+    const int per = (nq + nchunk - 1) / nchunk;
+    const int q0 = chunk * per, q1 = min(q0 + per, nq);
+    const size_t tsz = (size_t)(mmax + 1) * norder * pitch;
+    const size_t rowbase = (size_t)(cs ? 4 : 0) * tsz + (size_t)m * norder * pitch;
+    const double* d = D + (size_t)(2 * m + cs) * pitch;
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+      const size_t node = 4 * (size_t)q;
+      const double2 da = *reinterpret_cast<const double2*>(d + node);
+      const double2 db = *reinterpret_cast<const double2*>(d + node + 2);
+      const df dv[4] = {df_split_or_from(da.x), df_split_or_from(da.y), df_split_or_from(db.x),
+                        df_split_or_from(db.y)};
+#pragma unroll
+      for (int k0 = 0; k0 < KMAX; k0 += RB) {
+        if (k0 >= norder) break;
+        float4 vh[RB], vl[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+          if (k0 + u < norder) {
+            const size_t o = rowbase + (size_t)(k0 + u) * pitch + node;
+            vh[u] = *reinterpret_cast<const float4*>(hi + o);
+            vl[u] = *reinterpret_cast<const float4*>(lo + o);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+          if (k0 + u < norder) {
+            acc[k0 + u].fma(dv[0], df{vh[u].x, vl[u].x});
+            acc[k0 + u].fma(dv[1], df{vh[u].y, vl[u].y});
+            acc[k0 + u].fma(dv[2], df{vh[u].z, vl[u].z});
+            acc[k0 + u].fma(dv[3], df{vh[u].w, vl[u].w});
+          }
+        }
+      }
+    }
+  }
+  __shared__ df red[4][KMAX];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    df v = acc[k].value();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const df w{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
+      v = df_add(v, w);
+    }
+    if (lane == 0) red[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < norder) {
+    const int k = threadIdx.x;
+    df v = red[0][k];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = df_add(v, red[w][k]);
+    part[((size_t)(m * norder + k) * 2 + cs) * nchunk + chunk] = df_to(v);
+  }
+}
 
 bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f) {
   CylHandle* h = static_cast<CylHandle*>(handle);
@@ -1105,8 +1200,8 @@ static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) 
   FusedLayout L;
   size_t o = 0;
   auto take = [&](size_t b) { size_t at = o; o += align256(b); return at; };
-  L.grid = take((size_t)(h->mmax + 1) * 2 * h->nnode * sizeof(double));
-  L.part = take((size_t)(h->mmax + 1) * h->norder * 2 * kContractChunks * sizeof(double));
+  L.grid = take((size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double));   // planes of pitch_f nodes
+  L.part = take((size_t)(h->mmax + 1) * h->norder * 2 * kContractChunksDf * sizeof(double));
   L.hist = take(ncell * sizeof(int));
   L.off = take(ncell * sizeof(int));
   L.tsum = take(kScanTile * sizeof(int));
@@ -1185,7 +1280,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   int* off = reinterpret_cast<int*>(ws + L.off);
   int* tsum = reinterpret_cast<int*>(ws + L.tsum);
   const int ncell = h->numx * h->numy;
-  XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->nnode * sizeof(double), st));
+  XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double), st));
   XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
   const int g256 = grid_for(n, 256, 8);
   const int g128 = grid_for(n, 128, 8);
@@ -1229,7 +1324,8 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         constexpr int RUN = decltype(rl)::value;
         const int gr = grid_for((n + RUN - 1) / RUN, 128, 8);
         using Mth = std::conditional_t<F64, DepDF, DepF32>;
-        k_cyl_deposit_sorted<Mth, MC, RUN><<<gr, 128, 0, st>>>(h->numy, h->mmax, n, srec, D, h->nnode);
+        constexpr int NP = F64 ? 2 : 1;
+        k_cyl_deposit_sorted<Mth, MC, RUN, NP><<<gr, 128, 0, st>>>(h->numy, h->mmax, n, srec, D, h->pitch_f);
       };
       auto dep_m = [&](auto rl) {
         if (h->mmax <= 2) dep(std::integral_constant<int, 2>{}, rl);
@@ -1247,13 +1343,21 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     }
     if ((rc = timing_mark(4, st))) return rc;
     const int nout = (h->mmax + 1) * h->norder * 2;
-    dim3 g(kContractChunks, nout);
-    // coefficient contraction from the FP64 tables in both precisions: it is a
-    // reduction of the accumulated sums and stays FP64
-    k_cyl_contract_partial<double><<<g, 256, 0, st>>>(tab_ptr(h, 0), tab_ptr(h, 4), D, h->mmax, h->norder,
-                                                      h->nnode, h->nnode, kContractChunks, part);
-    XT_CHECK_LAUNCH("k_cyl_contract_partial");
-    k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
+    // coefficient contraction in both precisions from the double-float tables;
+    // node chunks sized for one wave of four 128-thread blocks per SM
+    const int nch = std::max(1, std::min(kContractChunksDf, 4 * sm_count() / (2 * (h->mmax + 1))));
+    dim3 g(nch, h->mmax + 1, 2);
+    if (h->norder <= 12)
+      k_cyl_contract_df<12><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
+                                              nch, part);
+    else if (h->norder <= 18)
+      k_cyl_contract_df<18><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
+                                              nch, part);
+    else
+      k_cyl_contract_df<24><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
+                                              nch, part);
+    XT_CHECK_LAUNCH("k_cyl_contract_df");
+    k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
     if ((rc = timing_mark(5, st))) return rc;
     // FP64 path: double-float field from the double-float tables; mixed path:

@@ -1,8 +1,10 @@
 // Double-float ("df") arithmetic: an unevaluated sum hi + lo of two FP32
 // numbers carrying ~48 significant bits.  On GB300 the FP64 pipe issues at a
-// small fraction of the FP32 rate, so the inner products of the FP64 path
-// (bilinear field interpolation, deposit weights) run as df on the FP32 pipe;
-// per-particle set-up, atomics and reductions stay in true FP64.
+// small fraction of the FP32 rate, so the per-particle set-up (square roots,
+// quotients, logarithms), the inner products (bilinear interpolation, deposit
+// weights, field contractions) of the FP64 path run as df on the FP32 pipe;
+// the atomics and final reductions stay in true FP64, fed by exact integer
+// float -> double widening.
 //
 // Algorithms: TwoSum (Knuth) and FMA-based TwoProd (exact product error),
 // followed by FastTwoSum renormalisation, as in the double-double /
@@ -192,13 +194,16 @@ __device__ __forceinline__ df df_asinh(df a) {
   return df_log1p(df_add(a, df_div(a2, df_add(one, df_sqrt(df_add(one, a2))))));
 }
 
-// Exact float -> double conversion with integer operations (normal floats and zero).
+// Exact float -> double conversion with integer operations, keeping the FP64
+// pipe free (every float: zero, normal, infinity and NaN by bit manipulation,
+// subnormals through the hardware conversion).
 __device__ __forceinline__ double f2d_int(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
   const unsigned e = (u >> 23) & 0xFF;
-  if (e == 0) return __longlong_as_double((long long)sign);          // zero (subnormals flushed)
-  const unsigned long long bits = sign | ((unsigned long long)(e + 896) << 52) |
+  if ((u & 0x7FFFFFFFu) == 0) return __longlong_as_double((long long)sign);   // signed zero
+  if (e == 0) return (double)f;                                               // subnormal (rare)
+  const unsigned long long bits = sign | ((unsigned long long)(e == 0xFF ? 2047u : e + 896) << 52) |
                                   ((unsigned long long)(u & 0x7FFFFF) << 29);
   return __longlong_as_double((long long)bits);
 }

@@ -41,13 +41,18 @@ int cuda_fail(cudaError_t e, const char* what) {
   return (e == cudaErrorMemoryAllocation) ? XT_ERR_OOM : XT_ERR_CUDA;
 }
 
-int grid_for(long long n, int block, int blocks_per_sm) {
+int sm_count() {
   static int nsm = 0;
   if (nsm == 0) {
-    int dev = 0;
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
+    nsm = (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0) ? v : 152;
   }
+  return nsm;
+}
+
+int grid_for(long long n, int block, int blocks_per_sm) {
+  const int nsm = sm_count();
   long long need = (n + block - 1) / block;
   long long cap = (long long)nsm * blocks_per_sm;
   if (need < 1) need = 1;
