@@ -42,7 +42,18 @@ CFG0 = dict(lmax=4, nmax=10, numr=2000, rmin=1e-3, rmax=100.0, cmap=2, scale=1.0
 N0 = 100_000
 L2_BYTES = 129 * 1024 * 1024
 # DRAM bytes of one k_cyl_binrec<double, df> launch at the headline workload (ncu --set full)
-BINREC_F64_TRAFFIC = 32_177_664 + 3_989_504
+# DRAM bytes (read + write) of one FP64 launch of each fused stage at the headline
+# workload, from an ncu --set full capture of `bench.py --profile`, and what
+# bounds the stage there
+STAGE_TRAFFIC_F64 = {
+    "k_cyl_binrec": (32_194_304 + 2_405_632, "FP32-pipe bound (double-float set-up): FMA pipe 56 %, IPC 3.1 / SM"),
+    "k_cyl_scatter": (58_598_912 + 12_578_560, "scattered 16-byte record stores: LSU throttle"),
+    "k_cyl_deposit_sorted": (50_727_680 + 124_928, "issue/latency bound: 128 registers, FP32 + FP64 pipes"),
+    "k_cyl_contract_partial+final": (131_907_584 + 3_219_968, "HBM latency: one wave of blocks"),
+    "k_cyl_field": (370_985_472 + 3_255_296, "HBM: 67 % of peak DRAM throughput"),
+    "k_cyl_eval_sorted": (89_494_016 + 36_166_912,
+                          "FP32-pipe bound (double-float arithmetic): FMA pipe 63 %, IPC 2.9 / SM"),
+}
 
 
 def cache_dir():
@@ -522,12 +533,16 @@ def gpu_arm(args, rank, world):
                 "k_cyl_contract_partial+final", "k_cyl_field", "k_cyl_eval_sorted"]
 
     def stage_alg(rs):
-        # algorithmic bytes per launch of each stage (rs = bytes of the compute type)
-        rec = 5 * rs
-        return [N1 * (32 + rec + 8 + 8), 2 * 4 * 65536, N1 * 2 * (rec + 8), N1 * (rec + 4),
-                13 * 18 * nnode * 8 + 13 * nnode * 8,
-                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * 8 + nnode * 7 * 6 * rs,
-                N1 * (rec + 8 + 40) + nnode * 7 * 6 * rs]
+        # algorithmic bytes per launch of each stage (rs = bytes of the compute
+        # type): particle records are 48 B (double-float) or 32 B (FP32); the
+        # FP64 path reads its tables as hi + lo FP32 pairs (8 B an entry), the
+        # mixed path's field reads the FP32 tables alone
+        rec = 48 if rs == 8 else 32
+        grid = 14 * nnode * 8
+        return [N1 * (32 + rec + 8 + 4), 2 * 4 * 65536, N1 * (2 * rec + 4), N1 * rec + grid,
+                13 * 18 * nnode * 8 + grid,
+                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * rs + nnode * 7 * 6 * rs,
+                N1 * (rec + 40) + nnode * 7 * 6 * rs]
 
     alg64 = stage_alg(8)
     alg32 = stage_alg(4)
@@ -559,14 +574,15 @@ def gpu_arm(args, rank, world):
         "e2e": {"value": world * N1 / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients_and_forces, pinned numpy inputs",
                 "separate_calls_value": world * N1 / sep_s},
-        "pipeline": "fused: per-particle set-up once, counting sort by table cell, run-accumulated deposit, "
-                    "contraction, field, sorted evaluation (8 kernels)",
-        "gpu_launches": 8 * K,
+        "pipeline": "fused: double-float per-particle set-up once, counting sort of 48-byte records by table "
+                    "cell, run-accumulated cooperative deposit, double-float contraction, field and sorted "
+                    "evaluation (9 kernels)",
+        "gpu_launches": 9 * K,
         "roofline": {"bound": "hbm", "kernel": st_names[dom], "achieved": round(ach, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": BINREC_F64_TRAFFIC,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_cyl_binrec<double, df> "
-                                       "at this workload (one launch)",
-                     "bound_note": "FP64-issue-bound: ncu shows the FP64 pipe 87 % active at 1.5 % of DRAM peak",
+                     "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": STAGE_TRAFFIC_F64[st_names[dom]][0],
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this kernel's FP64 "
+                                       "launch at this workload (one launch)",
+                     "bound_note": STAGE_TRAFFIC_F64[st_names[dom]][1],
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg64[dom],
                      "launch_ms": round(float(stages64[dom]), 4)},
         "fused_stages": fused_stages,
