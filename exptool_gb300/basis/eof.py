@@ -220,14 +220,16 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     table = table_from_file(eof_file)
     # Particle arrays in page-locked host memory are read by the binning
     # kernel in place (the host -> device traffic overlaps its work); other
-    # inputs are copied to the device first.  Coefficients and results are
-    # computed into reused device blocks and leave in two copies to
-    # page-locked host memory, with one synchronisation at the end.  Particles
-    # with a NaN coordinate are placed at the origin on the device.
+    # inputs are copied to the device first.  R is written by the binning
+    # kernel straight into page-locked host memory; the coefficients and the
+    # other five results are computed into reused device blocks and leave in
+    # two copies, with one synchronisation at the end.  Particles with a NaN
+    # coordinate are placed at the origin on the device.
+    r_host = dev.pinned_empty(m.size, 1)[0]
     coef, res = table.accumulate_eval_blocks(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision,
-                                             m1=m1, m2=m2, nan_to_origin=not nanblock)
+                                             m1=m1, m2=m2, nan_to_origin=not nanblock, r_out=r_host)
     cs_h, res_h = dev.to_host_many([coef, res])
-    host = [cs_h[0], cs_h[1]] + list(res_h)
+    host = [cs_h[0], cs_h[1]] + list(res_h) + [r_host.numpy()]
     out = EOF_Object()
     out.time = getattr(PSPInput, "time", None)
     out.filename = getattr(PSPInput, "filename", None)

@@ -43,6 +43,22 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 int grid_for(long long n, int block, int blocks_per_sm = 8);
 int sm_count();   // multiprocessors of the current device (cached)
 
+// Blocks of `fn` (a __global__ function) resident per SM at this block size and
+// dynamic shared memory (cudaOccupancyMaxActiveBlocksPerMultiprocessor, cached).
+int resident_blocks_per_sm(const void* fn, int block, size_t smem);
+
+// Grid of at most one full wave: as many blocks as stay resident together, or
+// fewer when `units` (one per thread) needs fewer.  Grid-stride kernels launched
+// this way balance their work over every resident block instead of leaving a
+// partial last wave.
+template <typename Kern>
+int resident_grid(Kern fn, int block, size_t smem, long long units) {
+  const long long cap = (long long)resident_blocks_per_sm((const void*)fn, block, smem) * sm_count();
+  long long need = (units + block - 1) / block;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
 // Where a pointer lives, as far as kernels are concerned (XT_PTR_* values of
 // the public header): device (or managed) memory, pinned host memory, other
 // host memory the device can address (pageable access), or host memory it

@@ -13,6 +13,7 @@
 // reads 4 corners x (mmax+1) x 6 values instead of 4 x 6 x (mmax+1) x norder.
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -21,6 +22,45 @@
 #include "xt_internal.cuh"
 
 namespace xt {
+
+// CUDA graph of one fused accumulate + evaluate call (xt_cyl_accumulate_eval),
+// replayed while everything but the particle arrays and R stays the same;
+// those five pointers are patched into the captured binning node.
+struct FusedGraph {
+  struct Key {
+    long long n;
+    int precision, m1, m2, nan_to_origin;
+    const void* ws;
+    const double *cos_out, *sin_out;
+    double* outs[5];
+    bool same(const Key& o) const {
+      if (n != o.n || precision != o.precision || m1 != o.m1 || m2 != o.m2 || nan_to_origin != o.nan_to_origin ||
+          ws != o.ws || cos_out != o.cos_out || sin_out != o.sin_out)
+        return false;
+      for (int i = 0; i < 5; ++i)
+        if (outs[i] != o.outs[i]) return false;
+      return true;
+    }
+  };
+  bool valid = false;
+  Key key{};
+  bool seen = false;                  // `last` was run directly once: capture if it repeats
+  Key last{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t binrec = nullptr;   // the binning kernel's node in `graph`
+  cudaKernelNodeParams bp{};          // its launch shape as captured
+  const double *x = nullptr, *y = nullptr, *z = nullptr, *m = nullptr;
+  double* rout = nullptr;
+  void clear() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    binrec = nullptr;
+    valid = false;
+  }
+};
 
 struct CylHandle {
   int mmax, norder, numx, numy, cmap, dens;
@@ -32,6 +72,9 @@ struct CylHandle {
   size_t pitch_f = 0;        // row pitch of tab_f32 / tab_lo: nnode rounded up to 4 (16-byte node quads)
   CylTab<double> tab_d;
   CylTab<float> tab_f;
+  std::mutex graph_mu;       // guards fused and capture
+  FusedGraph fused;
+  cudaStream_t capture = nullptr;   // private stream the fused graph is captured on
 };
 
 static inline const double* tab_ptr(const CylHandle* h, int which) {
@@ -587,7 +630,7 @@ struct DepDF {
 
 constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 
-// Deposit of sorted records.  Each lane takes RUN consecutive particles and
+// Deposit of sorted records.  Each lane takes `run` consecutive particles and
 // sums their contributions per (m, cos/sin, corner) in registers while the
 // cell stays the same.  A lane whose cell changes (and every lane at the end
 // of its run) parks its sums in shared memory; the whole warp then widens
@@ -599,9 +642,9 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 // rest, so that half the sums are live at a time (double-float sums: 104 ->
 // 56 registers of accumulators, for more resident warps; the second pass
 // re-reads the run's records from L1).
-template <typename M, int MCAP, int RUN, int NPASS>
+template <typename M, int MCAP, int NPASS>
 __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
-    k_cyl_deposit_sorted(int numy, int mmax, long long n, const BinRec<typename M::T>* __restrict__ srec,
+    k_cyl_deposit_sorted(int numy, int mmax, long long n, int run, const BinRec<typename M::T>* __restrict__ srec,
                          double* __restrict__ D, size_t plane) {
   using T = typename M::T;
   using A = typename M::A;
@@ -614,7 +657,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int ny1 = numy + 1;
   const int nju = 2 * mmax + 1;                 // sums in use (global index j)
-  const long long nrun = (n + RUN - 1) / RUN;
+  const long long nrun = (n + run - 1) / run;
 
   auto run_pass = [&](long long q0, auto pass_tag) {
     constexpr int PASS = decltype(pass_tag)::value;
@@ -666,7 +709,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
     };
     int cur = -1;
 #pragma unroll 1
-    for (int u = 0; u < RUN; ++u) {
+    for (int u = 0; u < run; ++u) {
       const long long q = q0 + u;
       const bool valid = q < n;                 // also false for lanes past the last run
       BinRec<T> r;
@@ -707,7 +750,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
 
   for (long long r0 = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); r0 < nrun;
        r0 += (long long)gridDim.x * blockDim.x) {
-    const long long q0 = (r0 + lane) * RUN;
+    const long long q0 = (r0 + lane) * run;
     run_pass(q0, std::integral_constant<int, 0>{});
     if constexpr (NPASS == 2) {
       if (mmax > MH) run_pass(q0, std::integral_constant<int, 1>{});
@@ -1030,6 +1073,8 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
 int xt_cyl_table_destroy(void* handle) {
   CylHandle* h = static_cast<CylHandle*>(handle);
   if (h) {
+    h->fused.clear();
+    if (h->capture) cudaStreamDestroy(h->capture);
     if (h->tab) cudaFree(h->tab);
     if (h->tab_f32) cudaFree(h->tab_f32);
     delete h;
@@ -1165,15 +1210,6 @@ int xt_cyl_eval_points(void* handle, const void* field, int precision, int densi
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-static int deposit_run_length() {
-  static int v = 0;
-  if (v == 0) {
-    const char* e = getenv("XT_DEPOSIT_RUN");
-    const int r = e ? atoi(e) : 8;
-    v = (r == 8 || r == 16 || r == 32) ? r : 8;
-  }
-  return v;
-}
 
 // Optional stage timing of xt_cyl_accumulate_eval: CUDA events recorded on the
 // call's stream between its stages (binrec, scan, scatter, deposit, contract,
@@ -1233,6 +1269,127 @@ int xt_timing_read(double* ms_out, int max) {
   return k;
 }
 
+}  // extern "C"
+
+// Arguments of the binning kernels, rebuilt to patch the captured node.
+struct BinrecArgs {
+  CylTab<double> Td;
+  CylTab<float> Tf;
+  BinrecDf K;
+  const double *x, *y, *z, *m;
+  long long n;
+  int* hist;
+  void* rec;
+  double* rout;
+  int nan;
+  void* p[11];
+  void** list(bool f64) {
+    int i = 0;
+    if (f64) {
+      p[i++] = &Td;
+      p[i++] = &K;
+    } else {
+      p[i++] = &Tf;
+    }
+    for (void* a : {(void*)&x, (void*)&y, (void*)&z, (void*)&m, (void*)&n, (void*)&hist, (void*)&rec, (void*)&rout,
+                    (void*)&nan})
+      p[i++] = a;
+    return p;
+  }
+};
+
+static BinrecDf binrec_constants(const CylTab<double>& T) {
+  return BinrecDf{host_df(T.XMIN), host_df(T.inv_dX), host_df(T.YMIN), host_df(T.inv_dY), host_df(T.inv_ascale),
+                  host_df(T.inv_hscale), host_df(1.0e-10), host_df(1.0e-8), host_df(-FOUR_PI_C)};
+}
+
+// Launch the fused call as a CUDA graph.  A call whose shape, workspace and
+// result arrays match the cached graph's replays it, with the binning node
+// pointed at this call's particle arrays and R; the second consecutive call of
+// a new shape captures it (on the handle's private stream); any other call is
+// enqueued directly.  One graph launch replaces two memsets and nine kernel
+// launches.  If capture fails, the call is enqueued directly.
+template <typename Enq>
+static int fused_graph_launch(CylHandle* h, int precision, const double* x, const double* y, const double* z,
+                              const double* m, long long n, int m1, int m2, int nan_to_origin, double* cos_out,
+                              double* sin_out, double* const* outs, void* workspace, const FusedLayout& L,
+                              cudaStream_t& st, Enq&& enqueue) {
+  std::lock_guard<std::mutex> lock(h->graph_mu);
+  FusedGraph& G = h->fused;
+  FusedGraph::Key key{n, precision, m1, m2, nan_to_origin, workspace, cos_out, sin_out,
+                      {outs[0], outs[1], outs[2], outs[3], outs[4]}};
+  const bool f64 = precision == XT_F64;
+  if (!G.valid || !G.key.same(key)) {
+    if (!(G.seen && G.last.same(key))) {     // first sighting of this shape: run it directly
+      G.seen = true;
+      G.last = key;
+      return enqueue();
+    }
+    G.clear();
+    if (!h->capture) XT_CUDA(cudaStreamCreateWithFlags(&h->capture, cudaStreamNonBlocking));
+    const cudaStream_t user = st;
+    st = h->capture;
+    XT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    st = user;
+    if (rc != XT_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      G.seen = false;
+      return enqueue();
+    }
+    G.graph = g;
+    size_t nn = 0;
+    XT_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    XT_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+    const void* want = f64 ? (const void*)k_cyl_binrec_df : (const void*)k_cyl_binrec<float>;
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType t;
+      XT_CUDA(cudaGraphNodeGetType(nd, &t));
+      if (t != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      XT_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
+      if (kp.func == want) {
+        G.binrec = nd;
+        G.bp = kp;
+      }
+    }
+    XT_REQUIRE(G.binrec, "fused EOF graph: binning node not found");
+    const cudaError_t ei = cudaGraphInstantiate(&G.exec, g, 0);
+    if (ei != cudaSuccess) {
+      G.clear();
+      return cuda_fail(ei, "instantiate the fused EOF graph");
+    }
+    G.key = key;
+    G.x = x;
+    G.y = y;
+    G.z = z;
+    G.m = m;
+    G.rout = outs[5];
+    G.valid = true;
+  } else if (G.x != x || G.y != y || G.z != z || G.m != m || G.rout != outs[5]) {
+    char* ws = static_cast<char*>(workspace);
+    BinrecArgs a{h->tab_d, h->tab_f, binrec_constants(h->tab_d), x, y, z, m, n,
+                 reinterpret_cast<int*>(ws + L.hist), ws + L.rec, outs[5], nan_to_origin, {}};
+    cudaKernelNodeParams kp = G.bp;
+    kp.kernelParams = a.list(f64);
+    kp.extra = nullptr;
+    XT_CUDA(cudaGraphExecKernelNodeSetParams(G.exec, G.binrec, &kp));
+    G.x = x;
+    G.y = y;
+    G.z = z;
+    G.m = m;
+    G.rout = outs[5];
+  }
+  XT_CUDA(cudaGraphLaunch(G.exec, st));
+  return XT_OK;
+}
+
+extern "C" {
+
 size_t xt_cyl_accumulate_eval_workspace(void* handle, long long n, int precision) {
   CylHandle* h = static_cast<CylHandle*>(handle);
   if (!h || n < 0) return 0;
@@ -1264,7 +1421,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       if (!outs[i]) continue;
       const int k = pointer_access(outs[i]);
       XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
-      host_out |= k != XT_PTR_DEVICE;
+      if (i < 5) host_out |= k != XT_PTR_DEVICE;   // R (outs[5]) is written coalesced by the binning kernel
     }
   }
   const FusedLayout L = fused_layout(h, n, precision);
@@ -1272,7 +1429,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
     return XT_ERR_WORKSPACE;
   }
-  cudaStream_t st = as_stream(stream);
+  cudaStream_t st = as_stream(stream);   // the stream work is enqueued on (the capture stream while capturing)
   char* ws = static_cast<char*>(workspace);
   double* D = reinterpret_cast<double*>(ws + L.grid);
   double* part = reinterpret_cast<double*>(ws + L.part);
@@ -1280,11 +1437,9 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   int* off = reinterpret_cast<int*>(ws + L.off);
   int* tsum = reinterpret_cast<int*>(ws + L.tsum);
   const int ncell = h->numx * h->numy;
-  XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double), st));
-  XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
-  const int g256 = grid_for(n, 256, 8);
-  const int g128 = grid_for(n, 128, 8);
   auto run = [&](auto tag) -> int {
+    XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double), st));
+    XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
     using R = decltype(tag);
     constexpr bool F64 = std::is_same<R, double>::value;
     using RT = typename std::conditional<F64, df, float>::type;   // record arithmetic
@@ -1296,12 +1451,12 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     if ((rc = timing_mark(0, st))) return rc;
     if (n > 0) {
       if constexpr (F64) {
-        const BinrecDf K{host_df(T.XMIN), host_df(T.inv_dX), host_df(T.YMIN), host_df(T.inv_dY),
-                         host_df(T.inv_ascale), host_df(T.inv_hscale), host_df(1.0e-10), host_df(1.0e-8),
-                         host_df(-FOUR_PI_C)};
-        k_cyl_binrec_df<<<g256, 256, 0, st>>>(T, K, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
+        const BinrecDf K = binrec_constants(T);
+        k_cyl_binrec_df<<<resident_grid(k_cyl_binrec_df, 256, 0, n), 256, 0, st>>>(T, K, x, y, z, m, n, hist, rec,
+                                                                                   outs[5], nan_to_origin);
       } else {
-        k_cyl_binrec<float><<<g256, 256, 0, st>>>(T, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
+        k_cyl_binrec<float><<<resident_grid(k_cyl_binrec<float>, 256, 0, n), 256, 0, st>>>(
+            T, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
       }
       XT_CHECK_LAUNCH("k_cyl_binrec");
       if ((rc = timing_mark(1, st))) return rc;
@@ -1313,29 +1468,27 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         XT_CHECK_LAUNCH("k_scan_add");
       }
       if ((rc = timing_mark(2, st))) return rc;
-      k_cyl_scatter<RT><<<g256, 256, 0, st>>>(n, off, rec, srec);
+      k_cyl_scatter<RT><<<resident_grid(k_cyl_scatter<RT>, 256, 0, n), 256, 0, st>>>(n, off, rec, srec);
       XT_CHECK_LAUNCH("k_cyl_scatter");
       if ((rc = timing_mark(3, st))) return rc;
-      // run length (particles summed in registers per thread before the FP64
-      // atomics); XT_DEPOSIT_RUN = 8, 16 or 32 overrides the default
-      const int run_len = deposit_run_length();
-      auto dep = [&](auto mc, auto rl) {
+      // Run length: particles summed in registers per lane before the atomics.
+      // Measured on 1e6 disc particles (runs of 4 to 16, one resident wave or
+      // one block per 128 runs): 8 for the double-float sums and 6 for FP32,
+      // one block per 128 runs (the hardware fills later waves as blocks end).
+      auto dep = [&](auto mc) {
         constexpr int MC = decltype(mc)::value;
-        constexpr int RUN = decltype(rl)::value;
-        const int gr = grid_for((n + RUN - 1) / RUN, 128, 8);
         using Mth = std::conditional_t<F64, DepDF, DepF32>;
         constexpr int NP = F64 ? 2 : 1;
-        k_cyl_deposit_sorted<Mth, MC, RUN, NP><<<gr, 128, 0, st>>>(h->numy, h->mmax, n, srec, D, h->pitch_f);
+        auto kern = k_cyl_deposit_sorted<Mth, MC, NP>;
+        const int run = F64 ? 8 : 6;
+        const long long nrun = (n + run - 1) / run;
+        const int grid = (int)std::min<long long>((nrun + 127) / 128, 8LL * resident_grid(kern, 128, 0, nrun));
+        kern<<<grid, 128, 0, st>>>(h->numy, h->mmax, n, run, srec, D, h->pitch_f);
       };
-      auto dep_m = [&](auto rl) {
-        if (h->mmax <= 2) dep(std::integral_constant<int, 2>{}, rl);
-        else if (h->mmax <= 4) dep(std::integral_constant<int, 4>{}, rl);
-        else if (h->mmax <= 6) dep(std::integral_constant<int, 6>{}, rl);
-        else dep(std::integral_constant<int, 8>{}, rl);
-      };
-      if (run_len <= 8) dep_m(std::integral_constant<int, 8>{});
-      else if (run_len <= 16) dep_m(std::integral_constant<int, 16>{});
-      else dep_m(std::integral_constant<int, 32>{});
+      if (h->mmax <= 2) dep(std::integral_constant<int, 2>{});
+      else if (h->mmax <= 4) dep(std::integral_constant<int, 4>{});
+      else if (h->mmax <= 6) dep(std::integral_constant<int, 6>{});
+      else dep(std::integral_constant<int, 8>{});
       XT_CHECK_LAUNCH("k_cyl_deposit_sorted");
     } else {
       for (int k = 1; k <= 3; ++k)
@@ -1362,15 +1515,21 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     if ((rc = timing_mark(5, st))) return rc;
     // FP64 path: double-float field from the double-float tables; mixed path:
     // FP32 field from the FP32 tables (coefficients staged as df in both)
-    constexpr int TQ = 32;   // node quads per block
-    const int fblocks = (int)((h->nnode + 4 * TQ - 1) / (4 * TQ));
     using FT = std::conditional_t<F64, df, float>;
-    const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) +
-                      4 * TQ * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
-    if (sm > 48 * 1024)
-      XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TQ, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_cyl_field2<FT, TQ, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, cos_out, sin_out, h->mmax,
-                                                         h->norder, h->nnode, reinterpret_cast<FT*>(field));
+    auto fld = [&](auto tq) -> int {
+      constexpr int TQ = decltype(tq)::value;   // node quads per block
+      const int fblocks = (int)((h->nnode + 4 * TQ - 1) / (4 * TQ));
+      const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) +
+                        4 * TQ * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
+      if (sm > 48 * 1024)
+        XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TQ, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      k_cyl_field2<FT, TQ, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, cos_out, sin_out,
+                                                           h->mmax, h->norder, h->nnode, reinterpret_cast<FT*>(field));
+      return XT_OK;
+    };
+    // 32 quads (128 nodes) per block: 0.072 ms against 0.076 (16) and 0.094 (8)
+    // for the double-float field of the 257^2-node, M = 6, Q = 18 table
+    if ((rc = fld(std::integral_constant<int, 32>{}))) return rc;
     XT_CHECK_LAUNCH("k_cyl_field2");
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {
@@ -1383,8 +1542,9 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       const BinRec<RT>* er = sorted ? srec : rec;
       if constexpr (F64) {
         auto ev = [&](auto srt) {
-          k_cyl_eval_sorted_df<decltype(srt)::value><<<g128, 128, 0, st>>>(
-              T, reinterpret_cast<const df*>(field), n, er, m1, m2, outs[0], outs[1], outs[2], outs[3], outs[4]);
+          auto kern = k_cyl_eval_sorted_df<decltype(srt)::value>;
+          kern<<<resident_grid(kern, 128, 0, n), 128, 0, st>>>(T, reinterpret_cast<const df*>(field), n, er, m1, m2,
+                                                              outs[0], outs[1], outs[2], outs[3], outs[4]);
         };
         if (sorted) ev(std::true_type{});
         else ev(std::false_type{});
@@ -1393,17 +1553,21 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         o.mode = XT_CYL_ACCUMULATED_EVAL_PARTICLES; o.m1 = m1; o.m2 = m2; o.mmax_use = h->mmax; o.no_odd = 0;
         o.perturb = 0; o.density = 0; o.nf = 6;
         if (sorted)
-          k_cyl_eval_sorted<R, true><<<g128, 128, 0, st>>>(T, field, n, er, o, outs[0], outs[1], outs[2], outs[3],
-                                                           outs[4]);
+          k_cyl_eval_sorted<R, true><<<resident_grid(k_cyl_eval_sorted<R, true>, 128, 0, n), 128, 0, st>>>(
+              T, field, n, er, o, outs[0], outs[1], outs[2], outs[3], outs[4]);
         else
-          k_cyl_eval_sorted<R, false><<<g128, 128, 0, st>>>(T, field, n, er, o, outs[0], outs[1], outs[2], outs[3],
-                                                            outs[4]);
+          k_cyl_eval_sorted<R, false><<<resident_grid(k_cyl_eval_sorted<R, false>, 128, 0, n), 128, 0, st>>>(
+              T, field, n, er, o, outs[0], outs[1], outs[2], outs[3], outs[4]);
       }
       XT_CHECK_LAUNCH("k_cyl_eval_sorted");
     }
     return timing_mark(7, st);
   };
-  return precision == XT_F64 ? run(double{}) : run(float{});
+  auto enqueue = [&]() -> int { return precision == XT_F64 ? run(double{}) : run(float{}); };
+  // Stage timing records events between the launches: enqueue directly.
+  if (g_timing || n == 0) return enqueue();
+  return fused_graph_launch(h, precision, x, y, z, m, n, m1, m2, nan_to_origin, cos_out, sin_out, outs, workspace,
+                            L, st, enqueue);
 }
 
 }  // extern "C"

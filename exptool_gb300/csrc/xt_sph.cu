@@ -51,6 +51,26 @@ int sm_count() {
   return nsm;
 }
 
+int resident_blocks_per_sm(const void* fn, int block, size_t smem) {
+  struct Key {
+    const void* fn;
+    int block;
+    size_t smem;
+  };
+  static std::mutex mu;
+  static std::vector<std::pair<Key, int>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& e : cache)
+    if (e.first.fn == fn && e.first.block == block && e.first.smem == smem) return e.second;
+  int v = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, fn, block, smem) != cudaSuccess || v < 1) {
+    cudaGetLastError();
+    return 1;                                   // not cached: asked again next time
+  }
+  cache.push_back({Key{fn, block, smem}, v});
+  return v;
+}
+
 int grid_for(long long n, int block, int blocks_per_sm) {
   const int nsm = sm_count();
   long long need = (n + block - 1) / block;

@@ -317,11 +317,13 @@ class CylTable:
                                                     dptr(ws), ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return cos, sin, outs
 
-    def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True):
+    def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True, r_out=None):
         """accumulate_eval into per-thread buffers kept for the last particle
         count and precision: returns the (2, mmax+1, norder) coefficient block
-        (cos, sin) and the (6, n) result block.  The next call on this thread
-        with the same size overwrites both, so callers copy them out first."""
+        (cos, sin) and the (5, n) block of p0, p, fr, fp, fz.  The next call on
+        this thread with the same size overwrites both, so callers copy them
+        out first.  R goes to ``r_out`` (a length-n float64 tensor, device or
+        page-locked host memory; the binning kernel writes it directly)."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
         b = getattr(self._fused_bufs, "v", None)
@@ -332,9 +334,10 @@ class CylTable:
                  torch.empty((6, n), dtype=torch.float64, device=device()))
             self._fused_bufs.v = b
         _, ws, coef, res = b
+        outs = list(res[:5]) + [r_out if r_out is not None else res[5]]
         self.accumulate_eval(x, y, z, m, precision=precision, m1=m1, m2=m2, workspace=ws,
-                             nan_to_origin=nan_to_origin, outs=list(res), coef=coef)
-        return coef, res
+                             nan_to_origin=nan_to_origin, outs=outs, coef=coef)
+        return coef, res[:5]
 
     def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):
         pc = precision_code(precision)
