@@ -611,7 +611,7 @@ struct DepF32 {
   static __device__ __forceinline__ void acc(A& a, T x, T y) { a = x * y + a; }
   static __device__ __forceinline__ T cheb(T c1, T cur, T prev) { return 2.f * c1 * cur - prev; }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
-  static __device__ __forceinline__ void deposit(double* d, A a) { atomicAdd(d, (double)a); }
+  static __device__ __forceinline__ void deposit(double* D, float*, size_t i, A a) { atomicAdd(D + i, (double)a); }
 };
 struct DepDF {
   using T = df;
@@ -625,7 +625,13 @@ struct DepDF {
     return df_sub(df_scale(df_mul(c1, cur), 2.f), prev);
   }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { df_weights(dx, dy, w); }
-  static __device__ __forceinline__ void deposit(double* d, A a) { atomicAdd(d, df_to(a.raw())); }
+  // leading part into the FP64 grid (one conversion, no FP64 add), the small
+  // error part into the FP32 companion grid E (FP32 atomic); the contraction
+  // reads D + E
+  static __device__ __forceinline__ void deposit(double* D, float* E, size_t i, A a) {
+    atomicAdd(D + i, (double)a.s);
+    if (a.e != 0.f) atomicAdd(E + i, a.e);
+  }
 };
 
 constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
@@ -645,7 +651,7 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 template <typename M, int MCAP, int NPASS>
 __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
     k_cyl_deposit_sorted(int numy, int mmax, long long n, int run, const BinRec<typename M::T>* __restrict__ srec,
-                         double* __restrict__ D, size_t plane) {
+                         double* __restrict__ D, float* __restrict__ E, size_t plane) {
   using T = typename M::T;
   using A = typename M::A;
   constexpr int MH = NPASS == 2 ? MCAP / 2 : MCAP;      // last order of the first pass
@@ -700,7 +706,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
             const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
             const int m = (j + 1) >> 1;        // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
             const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
-            M::deposit(D + (size_t)(2 * m + cs) * plane + node, park[wib][sidx][e]);
+            M::deposit(D, E, (size_t)(2 * m + cs) * plane + node, park[wib][sidx][e]);
           }
         }
         __syncwarp();
@@ -918,7 +924,8 @@ static const int kContractChunks = 8;
 static const int kContractChunksDf = 64;   // most node chunks of k_cyl_contract_df
 
 // Coefficient contraction of the fused paths:
-//   cos/sin[m][k] = sum over nodes of D[2m+cs][node] * pot{C,S}[m][k][node].
+//   cos/sin[m][k] = sum over nodes of (D + E)[2m+cs][node] * pot{C,S}[m][k][node]
+// (E: the FP32 companion grid of the double-float deposit's error parts).
 // Block (chunk, m, cs) takes a range of node quads; each thread multiplies
 // the quads' FP64 sums (split into float pairs by integer operations) by the
 // double-float tables (16-byte loads of hi and lo, rows of `pitch` entries,
@@ -928,9 +935,9 @@ static const int kContractChunksDf = 64;   // most node chunks of k_cyl_contract
 // table rows share the pitch; padding entries are zero in both.
 template <int KMAX>
 __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                         size_t pitch, const double* __restrict__ D, int mmax,
-                                                         int norder, size_t nnode, int nchunk,
-                                                         double* __restrict__ part) {
+                                                         size_t pitch, const double* __restrict__ D,
+                                                         const float* __restrict__ E, int mmax, int norder,
+                                                         size_t nnode, int nchunk, double* __restrict__ part) {
   constexpr int RB = 6;                         // rows in flight
   static_assert(KMAX % RB == 0, "KMAX must be a multiple of the row batch");
   const int chunk = blockIdx.x, m = blockIdx.y, cs = blockIdx.z;
@@ -942,12 +949,14 @@ __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict
     const size_t tsz = (size_t)(mmax + 1) * norder * pitch;
     const size_t rowbase = (size_t)(cs ? 4 : 0) * tsz + (size_t)m * norder * pitch;
     const double* d = D + (size_t)(2 * m + cs) * pitch;
+    const float* ep = E + (size_t)(2 * m + cs) * pitch;
     for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       const size_t node = 4 * (size_t)q;
       const double2 da = *reinterpret_cast<const double2*>(d + node);
       const double2 db = *reinterpret_cast<const double2*>(d + node + 2);
-      const df dv[4] = {df_split_or_from(da.x), df_split_or_from(da.y), df_split_or_from(db.x),
-                        df_split_or_from(db.y)};
+      const float4 ev = *reinterpret_cast<const float4*>(ep + node);
+      const df dv[4] = {df_add(df_split_or_from(da.x), {ev.x, 0.f}), df_add(df_split_or_from(da.y), {ev.y, 0.f}),
+                        df_add(df_split_or_from(db.x), {ev.z, 0.f}), df_add(df_split_or_from(db.y), {ev.w, 0.f})};
 #pragma unroll
       for (int k0 = 0; k0 < KMAX; k0 += RB) {
         if (k0 >= norder) break;
@@ -1227,7 +1236,7 @@ static int timing_mark(int k, cudaStream_t st) {
 }
 
 struct FusedLayout {
-  size_t grid, part, hist, off, tsum, rec, srec, field, total;
+  size_t grid, egrid, part, hist, off, tsum, rec, srec, field, total;
 };
 
 static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) {
@@ -1237,6 +1246,7 @@ static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) 
   size_t o = 0;
   auto take = [&](size_t b) { size_t at = o; o += align256(b); return at; };
   L.grid = take((size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double));   // planes of pitch_f nodes
+  L.egrid = take((size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(float));   // FP32 companion (error parts)
   L.part = take((size_t)(h->mmax + 1) * h->norder * 2 * kContractChunksDf * sizeof(double));
   L.hist = take(ncell * sizeof(int));
   L.off = take(ncell * sizeof(int));
@@ -1432,6 +1442,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   cudaStream_t st = as_stream(stream);   // the stream work is enqueued on (the capture stream while capturing)
   char* ws = static_cast<char*>(workspace);
   double* D = reinterpret_cast<double*>(ws + L.grid);
+  float* E = reinterpret_cast<float*>(ws + L.egrid);
   double* part = reinterpret_cast<double*>(ws + L.part);
   int* hist = reinterpret_cast<int*>(ws + L.hist);
   int* off = reinterpret_cast<int*>(ws + L.off);
@@ -1439,6 +1450,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   const int ncell = h->numx * h->numy;
   auto run = [&](auto tag) -> int {
     XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double), st));
+    XT_CUDA(cudaMemsetAsync(E, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(float), st));
     XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
     using R = decltype(tag);
     constexpr bool F64 = std::is_same<R, double>::value;
@@ -1483,7 +1495,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         const int run = F64 ? 8 : 6;
         const long long nrun = (n + run - 1) / run;
         const int grid = (int)std::min<long long>((nrun + 127) / 128, 8LL * resident_grid(kern, 128, 0, nrun));
-        kern<<<grid, 128, 0, st>>>(h->numy, h->mmax, n, run, srec, D, h->pitch_f);
+        kern<<<grid, 128, 0, st>>>(h->numy, h->mmax, n, run, srec, D, E, h->pitch_f);
       };
       if (h->mmax <= 2) dep(std::integral_constant<int, 2>{});
       else if (h->mmax <= 4) dep(std::integral_constant<int, 4>{});
@@ -1501,14 +1513,14 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     const int nch = std::max(1, std::min(kContractChunksDf, 4 * sm_count() / (2 * (h->mmax + 1))));
     dim3 g(nch, h->mmax + 1, 2);
     if (h->norder <= 12)
-      k_cyl_contract_df<12><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
-                                              nch, part);
+      k_cyl_contract_df<12><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
+                                              h->nnode, nch, part);
     else if (h->norder <= 18)
-      k_cyl_contract_df<18><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
-                                              nch, part);
+      k_cyl_contract_df<18><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
+                                              h->nnode, nch, part);
     else
-      k_cyl_contract_df<24><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, h->mmax, h->norder, h->nnode,
-                                              nch, part);
+      k_cyl_contract_df<24><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
+                                              h->nnode, nch, part);
     XT_CHECK_LAUNCH("k_cyl_contract_df");
     k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
