@@ -46,13 +46,13 @@ L2_BYTES = 129 * 1024 * 1024
 # workload, from an ncu --set full capture of `bench.py --profile`, and what
 # bounds the stage there
 STAGE_TRAFFIC_F64 = {
-    "k_cyl_binrec": (32_194_304 + 2_405_632, "FP32-pipe bound (double-float set-up): FMA pipe 56 %, IPC 3.1 / SM"),
-    "k_cyl_scatter": (58_598_912 + 12_578_560, "scattered 16-byte record stores: LSU throttle"),
-    "k_cyl_deposit_sorted": (50_727_680 + 124_928, "issue/latency bound: 128 registers, FP32 + FP64 pipes"),
-    "k_cyl_contract_partial+final": (131_907_584 + 3_219_968, "HBM latency: one wave of blocks"),
-    "k_cyl_field": (370_985_472 + 3_255_296, "HBM: 67 % of peak DRAM throughput"),
-    "k_cyl_eval_sorted": (89_494_016 + 36_166_912,
-                          "FP32-pipe bound (double-float arithmetic): FMA pipe 63 %, IPC 2.9 / SM"),
+    "k_cyl_binrec": (32_197_120 + 2_609_408, "FP32-pipe bound (double-float set-up): FMA pipe 53 %, IPC 2.9 / SM"),
+    "k_cyl_scatter": (57_617_152 + 11_612_672, "scattered 16-byte record stores: LSU throttle"),
+    "k_cyl_deposit_sorted": (52_213_504 + 4_608, "issue/latency bound: 128 registers, IPC 2.2 / SM, FMA pipe 35 %"),
+    "k_cyl_contract_partial+final": (135_424_000 + 2_991_616, "HBM latency: 52 % of peak, one wave"),
+    "k_cyl_field": (370_984_448 + 3_244_800, "HBM: 68 % of peak DRAM throughput"),
+    "k_cyl_eval_sorted": (89_639_168 + 35_993_088,
+                          "FP32-pipe bound (double-float arithmetic): FMA pipe 57 %, IPC 2.6 / SM"),
 }
 
 
