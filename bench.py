@@ -518,6 +518,7 @@ def gpu_arm(args, rank, world):
     orbits = orbit_extra(path, c64, s64, cache, model, st, hxd, hyd, hzd, hmd, args)
     batched = batched_extra()
     learned_sl = learned_extra()
+    snap = snapshot_extra()
 
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
@@ -594,6 +595,7 @@ def gpu_arm(args, rank, world):
         "spherical_halo": {"workload": "Hernquist SL lmax=4 nmax=10 numr=2000 cmap=2, N=1e5, accumulate+eval",
                            "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
         "orbits": orbits,
+        "snapshot_reader": snap,
         "batched_spherical": batched,
         "learned_spherical": learned_sl,
         "clocks": clocks,
@@ -618,6 +620,58 @@ def stage_times(fused, prec, steps):
     lib.xt_timing_enable(0)
     torch.cuda.synchronize()
     return acc / steps
+
+
+def snapshot_extra(n=N1, reps=5):
+    """PSP snapshot read (file -> page-locked records -> GPU de-interleave) of
+    a 1e6-particle double-precision file with ids and one int / one float
+    attribute (84-byte records), from the page cache, to device columns and
+    to host columns; beside it the reference's method (NumPy structured memmap
+    and per-field copies, psp_io.py:196-230) on the same file."""
+    import tempfile
+    import torch
+    from exptool_gb300.io import psp_io, snapshot
+    rng = np.random.default_rng(11)
+    comp = {k: rng.normal(size=n) for k in ["m", "x", "y", "z", "vx", "vy", "vz", "potE", "f_attr0"]}
+    comp["i_attr0"] = rng.integers(0, 1000, n)
+    comp["id"] = np.arange(n)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "OUT.bench")
+        snapshot.write_psp(path, 0.0, {"disc": comp}, float_len=8, indexing=True)
+        nbytes = os.path.getsize(path)
+        rec, cols = snapshot.record_layout(8, True, 1, 1)
+        kinds = {"i8": "<i8", "i4": "<i4", "f8": "<f8"}
+        dt = np.dtype({"names": [c[0] for c in cols], "formats": [kinds[c[2]] for c in cols],
+                       "offsets": [c[1] for c in cols], "itemsize": rec})
+
+        def ref_read():
+            with open(path, "rb") as f:
+                _t, _fl, head = snapshot.read_psp_header(f)
+            h = head["disc"]
+            mm = np.memmap(path, dtype=dt, shape=(h["nbodies"],), offset=h["data_start"], mode="r")
+            out = {name: np.array(mm[name], copy=True) for name in dt.names}
+            del mm
+            return out
+
+        def timed(fn):
+            fn()
+            ts = []
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            return float(np.median(ts))
+
+        t_dev = timed(lambda: psp_io.Input(path, comp="disc", device=True))
+        t_host = timed(lambda: psp_io.Input(path, comp="disc"))
+        t_ref = timed(ref_read)
+    return {"workload": f"PSP snapshot, {n} particles, float64 with ids + 1 int + 1 float attribute "
+                        f"({rec}-byte records, {nbytes / 1e6:.1f} MB), page cache, read + de-interleave",
+            "device_columns_s": t_dev, "device_GBps": nbytes / t_dev / 1e9,
+            "host_columns_s": t_host, "host_GBps": nbytes / t_host / 1e9,
+            "reference_method_s": t_ref, "reference_method_GBps": nbytes / t_ref / 1e9}
 
 
 def orbit_extra(eof_path, cos_d, sin_d, sph_cache, sph_model, sph_table, hx, hy, hz, hm, args, n=N1, nint=2000,

@@ -29,6 +29,11 @@ XT_PTR_DEVICE = 0
 XT_PTR_PINNED = 1
 XT_PTR_PAGEABLE = 2
 XT_PTR_INACCESSIBLE = 3
+XT_COL_F32 = 0
+XT_COL_F64 = 1
+XT_COL_I32 = 2
+XT_COL_I64 = 3
+XT_COL_F32_TO_F64 = 4
 
 _lock = threading.Lock()
 _lib = None
@@ -88,6 +93,7 @@ _SIGS = {
     "xt_learned_radial_pass": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_int, c_vp, c_ll, c_int,
                                        c_vp, c_vp]),
     "xt_learned_status": (c_int, []),
+    "xt_records_to_columns": (c_int, [c_vp, c_ll, c_int, c_int, c_vp, c_vp, c_dpp, c_vp]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -216,16 +216,18 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     and particles are sorted by table cell on the device.  Returns
     (EOF_Object, (p0, p, fr, fp, fz, R)).  Particles with a NaN coordinate
     are placed at the origin (unless nanblock) for both passes."""
-    x, y, z, m = positions(PSPInput)
+    x, y, z, m = positions(PSPInput, allow_device=True)
+    n = int(m.numel()) if isinstance(m, torch.Tensor) else int(m.size)
     table = table_from_file(eof_file)
-    # Particle arrays in page-locked host memory are read by the binning
+    # Particle arrays already on the device (snapshots read with device=True)
+    # are used in place.  Particle arrays in page-locked host memory are read by the binning
     # kernel in place (the host -> device traffic overlaps its work); other
     # inputs are copied to the device first.  R is written by the binning
     # kernel straight into page-locked host memory; the coefficients and the
     # other five results are computed into reused device blocks and leave in
     # two copies, with one synchronisation at the end.  Particles with a NaN
     # coordinate are placed at the origin on the device.
-    r_host = dev.pinned_empty(m.size, 1)[0]
+    r_host = dev.pinned_empty(n, 1)[0]
     coef, res = table.accumulate_eval_blocks(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision,
                                              m1=m1, m2=m2, nan_to_origin=not nanblock, r_out=r_host)
     cs_h, res_h = dev.to_host_many([coef, res])
@@ -234,7 +236,7 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     out.time = getattr(PSPInput, "time", None)
     out.filename = getattr(PSPInput, "filename", None)
     out.comp = getattr(PSPInput, "comp", None)
-    out.nbodies = m.size
+    out.nbodies = n
     out.eof_file = eof_file
     out.mmax = table.mmax
     out.nmax = table.norder

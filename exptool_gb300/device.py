@@ -62,10 +62,12 @@ def host_access(a: np.ndarray) -> int:
 
 
 def kernel_input(a):
-    """A float64 particle array in the form the kernels read: a contiguous
-    array in page-locked host memory is passed in place (the kernels read it
-    over the host link, so the transfer overlaps their work); anything else is
-    copied to the device on the current stream first."""
+    """A float64 particle array in the form the kernels read: a CUDA tensor
+    stays on the device; a contiguous array in page-locked host memory is
+    passed in place (the kernels read it over the host link, so the transfer
+    overlaps their work); anything else is copied to the device first."""
+    if isinstance(a, torch.Tensor) and a.is_cuda:
+        return a.to(torch.float64).contiguous()
     a = np.asarray(a, dtype=np.float64)
     if a.size and a.flags.c_contiguous and host_access(a) == _lib.XT_PTR_PINNED:
         return a

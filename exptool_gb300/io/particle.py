@@ -2,8 +2,8 @@
 
 ``holder`` is the attribute container (``.xpos .ypos .zpos .mass`` ...,
 particle.py:142-157); ``ParticleData`` provides the ``.data`` dict of
-``particle.Input`` (keys x y z vx vy vz m potE) for in-memory arrays, since
-snapshot readers are outside this package.
+``particle.Input`` (keys x y z vx vy vz m potE) for in-memory arrays.  The
+snapshot readers are ``psp_io.Input`` and ``spl_io.Input``.
 """
 from __future__ import annotations
 
@@ -44,11 +44,15 @@ class ParticleData(object):
         self.comp = comp
 
 
-def positions(P):
-    """(x, y, z, m) float64 arrays of a holder-like or ``.data``-like container."""
+def positions(P, allow_device=False):
+    """(x, y, z, m) float64 arrays of a holder-like or ``.data``-like container.
+    With allow_device, columns that are CUDA tensors (a snapshot read with
+    ``device=True``) are returned as float64 CUDA tensors instead."""
     if hasattr(P, "data") and isinstance(getattr(P, "data"), dict) and "x" in P.data:
-        d = P.data
-        return (np.asarray(d["x"], dtype=np.float64), np.asarray(d["y"], dtype=np.float64),
-                np.asarray(d["z"], dtype=np.float64), np.asarray(d["m"], dtype=np.float64))
-    return (np.asarray(P.xpos, dtype=np.float64), np.asarray(P.ypos, dtype=np.float64),
-            np.asarray(P.zpos, dtype=np.float64), np.asarray(P.mass, dtype=np.float64))
+        cols = [P.data[k] for k in ("x", "y", "z", "m")]
+    else:
+        cols = [P.xpos, P.ypos, P.zpos, P.mass]
+    if allow_device and all(getattr(c, "is_cuda", False) for c in cols):
+        import torch
+        return tuple(c.to(torch.float64).contiguous() for c in cols)
+    return tuple(np.asarray(c.cpu() if hasattr(c, "cpu") else c, dtype=np.float64) for c in cols)

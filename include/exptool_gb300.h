@@ -275,6 +275,24 @@ int xt_learned_radial_pass(void *sph, void *mlp, const void *prep, int K, double
  * waiting for its MMAs: XT_ERR_DEVICE, else XT_OK. */
 int xt_learned_status(void);
 
+/* --------------------------------------------------------------- snapshot records */
+/* Column kinds of xt_records_to_columns: source field -> column element. */
+#define XT_COL_F32 0         /* float  -> float            */
+#define XT_COL_F64 1         /* double -> double           */
+#define XT_COL_I32 2         /* int32  -> int32            */
+#define XT_COL_I64 3         /* int64  -> int64            */
+#define XT_COL_F32_TO_F64 4  /* float  -> double           */
+
+/* De-interleave n packed particle records of rec_bytes bytes (a multiple of 4,
+ * at most 384) into ncol (<= 32) columns: field c at byte col_off[c] (a
+ * multiple of 4) of each record, converted per col_kind[c], is written to
+ * outs[c][0..n).  Replaces the NumPy structured memmap + per-field copies of
+ * exptool/io/psp_io.py:196-230 and spl_io.py:235-270.  records and outs may
+ * be device memory or host memory the device addresses (xt_pointer_access);
+ * col_off, col_kind and the outs array itself are host arrays. */
+int xt_records_to_columns(const void *records, long long n, int rec_bytes, int ncol, const int *col_off,
+                          const int *col_kind, void *const *outs, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

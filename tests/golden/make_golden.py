@@ -405,8 +405,67 @@ def centering_case(ref):
     print("centering done")
 
 
-def main():
+def snapshot_case():
+    """PSP and SPL snapshots (single and double precision, with and without
+    particle ids, with integer and float attributes, several components, an
+    unaligned float attribute in 84-byte records) written with
+    exptool_gb300.io.snapshot's writers and read by the reference's own
+    psp_io / spl_io.  PyYAML is not installed, so the reference readers'
+    yaml.safe_load is supplied by exptool_gb300.io.yaml_lite: these vectors pin
+    the binary layout, not the YAML parsing."""
+    import json
+    import types
+    from exptool_gb300.io import snapshot, yaml_lite
+    shim = types.ModuleType("yaml")
+    shim.safe_load = yaml_lite.load
+    sys.modules["yaml"] = shim
+    from exptool.io import psp_io, spl_io
+    psp_io.yaml = spl_io.yaml = shim        # imported earlier against the stub module
+    folder = P("snap")
+    os.makedirs(folder, exist_ok=True)
+    rng = np.random.default_rng(7)
+
+    def comp(n, nint, nfloat, with_id):
+        c = {k: rng.normal(size=n) for k in ["m", "x", "y", "z", "vx", "vy", "vz", "potE"]}
+        c["m"] = np.abs(c["m"]) * 1e-3
+        for i in range(nint):
+            c[f"i_attr{i}"] = rng.integers(-1000, 1000, n)
+        for i in range(nfloat):
+            c[f"f_attr{i}"] = rng.normal(size=n)
+        if with_id:
+            c["id"] = rng.integers(0, 2**40, n)
+        return c
+
+    cases = {
+        "OUT.f4idx": ("psp", 4, True, {"star": comp(300, 1, 2, True), "dark": comp(200, 0, 0, True)}),
+        "OUT.f8": ("psp", 8, False, {"star": comp(250, 1, 1, False)}),
+        "SPL.f4": ("spl", 4, False, {"star": comp(301, 0, 1, False), "gas": comp(77, 2, 0, False)}),
+        "SPL.f8idx": ("spl", 8, True, {"star": comp(150, 1, 0, True)}),
+    }
+    out = {}
+    for fname, (kind, fl, idx, comps) in cases.items():
+        path = os.path.join(folder, fname)
+        if kind == "psp":
+            snapshot.write_psp(path, 1.25, comps, float_len=fl, indexing=idx)
+        else:
+            snapshot.write_spl(path, 2.5, comps, nsub=3, float_len=fl, indexing=idx)
+        for cname in comps:
+            I = (psp_io if kind == "psp" else spl_io).Input(path, comp=cname)
+            for k, v in I.data.items():
+                out[f"{fname}/{cname}/{k}"] = v
+            out[f"{fname}/{cname}/time"] = np.float64(I.time)
+        out[f"{fname}/header"] = np.array(json.dumps({k: {kk: (int(vv) if isinstance(vv, np.integer) else vv)
+                                                           for kk, vv in h.items()}
+                                                       for k, h in I.header.items()}, sort_keys=True))
+    np.savez_compressed(P("snapshots.npz"), **out)
+
+
+def main(only_snapshots=False):
+    """All fixtures, or (argument ``snapshots``) only the snapshot-reader ones."""
     ref = refshim.load()
+    snapshot_case()
+    if only_snapshots:
+        return
     sl_out = {}
     for cmap in (0, 1, 2):
         sl_out[cmap] = sl_case(ref, cmap)
@@ -421,4 +480,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(only_snapshots=sys.argv[1:] == ["snapshots"])
