@@ -360,3 +360,30 @@ def extract_eof_coefficients(f):
     """eof.extract_eof_coefficients (eof.py:1743-1760)."""
     from ..io import coefficients
     return coefficients.extract_eof_coefficients(f, EOF_Object)
+
+
+# ---------------------------------------------------------------- EXP coefficient time series
+def read_binary_eof_coefficients(coeffile):
+    """eof.read_binary_eof_coefficients (eof.py:2230-2293): old-layout EXP
+    Cylinder coefficients -> (times, coefs[t, cos/sin, m, n])."""
+    from ..io import outcoef
+    return outcoef.read_old_cylinder(coeffile)
+
+
+def read_binary_eof_coefficients_dict(coeffile):
+    """eof.read_binary_eof_coefficients_dict (eof.py:2296-2360): {time: EOF_Object}."""
+    from ..io import outcoef
+    T, c = outcoef.read_old_cylinder(coeffile)
+    out = {}
+    for t in range(T.size):
+        E = EOF_Object()
+        E.time = T[t]
+        E.mmax, E.nmax = c.shape[2] - 1, c.shape[3]
+        E.filename = "[redacted]"
+        E.comp = "star"
+        E.nbodies = 0.0
+        E.eof_file = "[redacted]"
+        E.cos = np.array(c[t, 0])
+        E.sin = np.array(c[t, 1])
+        out[E.time] = E
+    return out

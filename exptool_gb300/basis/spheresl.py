@@ -259,3 +259,11 @@ def extract_sl_coefficients(f):
     """spheresl.extract_sl_coefficients (spheresl.py:1471-1488)."""
     from ..io import coefficients
     return coefficients.extract_sl_coefficients(f, SL_Object)
+
+
+# ---------------------------------------------------------------- EXP coefficient time series
+def read_binary_sl_coefficients(coeffile):
+    """spheresl.read_binary_sl_coefficients (spheresl.py:1636-1696): old-layout
+    EXP SphereSL coefficients -> (times, coefs[t, lm, n])."""
+    from ..io import outcoef
+    return outcoef.read_old_spheresl(coeffile)

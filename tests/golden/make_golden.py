@@ -460,10 +460,87 @@ def snapshot_case():
     np.savez_compressed(P("snapshots.npz"), **out)
 
 
+def outcoef_case(ref):
+    """EXP coefficient time series in the four layouts (new YAML-headed and old
+    SphereSL / Cylinder; the old files end in a partial record), written with
+    exptool_gb300.io.outcoef's writers and read by the reference's
+    io/outcoef.OutCoef and eof.read_binary_eof_coefficients(_dict) (yaml.load
+    supplied by exptool_gb300.io.yaml_lite: PyYAML is not installed), and by
+    spheresl.read_binary_sl_coefficients.  Under numpy 2 these readers stop at
+    dtype codes numpy removed ('aN' strings, np.float); they run here with
+    those two codes mapped to their replacements, their logic unchanged."""
+    import types
+    from exptool_gb300.io import outcoef, yaml_lite
+    shim = types.ModuleType("yaml")
+    shim.load = lambda s, Loader=None: yaml_lite.load(s)
+    shim.safe_load = yaml_lite.load
+    shim.FullLoader = None
+    from exptool.io import outcoef as ref_oc
+    ref_oc.yaml = shim
+
+    class _Numpy2:
+        """numpy for the reference's readers with the codes numpy 2 removed
+        mapped to their replacements ('aN' -> 'SN' byte strings, np.float ->
+        float); everything else is numpy itself."""
+        float = float
+
+        def __getattr__(self, k):
+            return getattr(np, k)
+
+        @staticmethod
+        def fromfile(f, dtype=float, count=-1, **kw):
+            if isinstance(dtype, str) and dtype.startswith("a"):
+                dtype = "S" + dtype[1:]
+            return np.fromfile(f, dtype=dtype, count=count, **kw)
+
+    saved = (ref_oc.np, ref.spheresl.np)
+    ref_oc.np = ref.spheresl.np = _Numpy2()
+    folder = P("outcoef")
+    os.makedirs(folder, exist_ok=True)
+    rng = np.random.default_rng(21)
+    T = np.array([0.0, 0.002, 1.0e-5, 0.75, 12.5])
+    sl = rng.normal(size=(5, 7 * 7, 9))
+    cy = rng.normal(size=(5, 2, 7, 11))
+    cy[:, 1, 0] = 0.0
+    files = {"sl_new": (outcoef.write_new_spheresl, sl), "sl_old": (outcoef.write_old_spheresl, sl),
+             "cyl_new": (outcoef.write_new_cylinder, cy), "cyl_old": (outcoef.write_old_cylinder, cy)}
+    out = {}
+    for name, (w, c) in files.items():
+        path = os.path.join(folder, name)
+        w(path, T, c)
+        if name.endswith("old"):
+            with open(path, "ab") as f:
+                f.write(b"\x01" * 37)          # a partial trailing record
+        O = ref_oc.OutCoef(path)
+        out[f"{name}/T"], out[f"{name}/coefs"] = O.T, O.coefs
+        out[f"{name}/basis"] = np.array(O.basis)
+        if name == "sl_new":
+            O._repackage_spherical_coefficients()
+            out["sl_new/C_2_1_sin_3"] = O.C[2][1]["sin"][3]
+            out["sl_new/C_3_0_cos_4"] = O.C[3][0]["cos"][4]
+        if name == "cyl_new":
+            O._repackage_cylindrical_coefficients()
+            out["cyl_new/C_4_sin_2"] = O.C[4]["sin"][2]
+            d = O._repackage_cylindrical_coefficients_compatibility()
+            out["cyl_new/dict_times"] = np.array(sorted(d))
+            out["cyl_new/dict_cos_at_0.75"] = d[0.75].cos
+    tr, cr = ref.eof.read_binary_eof_coefficients(os.path.join(folder, "cyl_old"))
+    out["eof_read_binary/T"], out["eof_read_binary/coefs"] = tr, cr
+    dct = ref.eof.read_binary_eof_coefficients_dict(os.path.join(folder, "cyl_old"))
+    out["eof_read_binary_dict/times"] = np.array(sorted(dct))
+    out["eof_read_binary_dict/sin_at_12.5"] = dct[12.5].sin
+    ts, cs = ref.spheresl.read_binary_sl_coefficients(os.path.join(folder, "sl_old"))
+    out["spheresl_read_binary/T"], out["spheresl_read_binary/coefs"] = ts, cs
+    ref_oc.np, ref.spheresl.np = saved
+    np.savez_compressed(P("outcoef.npz"), **out)
+
+
 def main(only_snapshots=False):
-    """All fixtures, or (argument ``snapshots``) only the snapshot-reader ones."""
+    """All fixtures, or (argument ``snapshots``) only the snapshot and
+    coefficient-file reader ones."""
     ref = refshim.load()
     snapshot_case()
+    outcoef_case(ref)
     if only_snapshots:
         return
     sl_out = {}
