@@ -519,6 +519,7 @@ def gpu_arm(args, rank, world):
     batched = batched_extra()
     learned_sl = learned_extra()
     snap = snapshot_extra()
+    snap["coefficient_series"] = series_extra()
 
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
@@ -672,6 +673,39 @@ def snapshot_extra(n=N1, reps=5):
             "device_columns_s": t_dev, "device_GBps": nbytes / t_dev / 1e9,
             "host_columns_s": t_host, "host_GBps": nbytes / t_host / 1e9,
             "reference_method_s": t_ref, "reference_method_GBps": nbytes / t_ref / 1e9}
+
+
+def series_extra(nfile=8, n=N1):
+    """SL coefficient time series (lmax 4, nmax 10 halo table) over `nfile`
+    PSP snapshots of n Hernquist particles each (float64, 72 MB each, page
+    cache): the overlapped series call against one psp_io read +
+    compute_coefficients call per file."""
+    import tempfile
+    import torch
+    from exptool_gb300.basis import spheresl
+    from exptool_gb300.io import psp_io, snapshot
+    from exptool_gb300.tables.samplers import hernquist_sample
+    cache, model = sl_table_paths()
+    with tempfile.TemporaryDirectory() as d:
+        files = []
+        for i in range(nfile):
+            x, y, z, m = hernquist_sample(n, seed=500 + i)
+            comp = {"m": m, "x": x, "y": y, "z": z, "vx": x, "vy": y, "vz": z, "potE": m}
+            files.append(os.path.join(d, f"OUT.bench.{i:05d}"))
+            snapshot.write_psp(files[-1], float(i), {"dark": comp})
+        spheresl.compute_coefficients_series(files[:2], "dark", cache, model)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        spheresl.compute_coefficients_series(files, "dark", cache, model)
+        t_series = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for f in files:
+            spheresl.compute_coefficients(psp_io.Input(f, comp="dark"), cache, model, verbose=0)
+        t_each = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(f) for f in files)
+    return {"workload": f"{nfile} PSP snapshots x {n} particles (float64, {nbytes / 1e6:.0f} MB), SL lmax 4 "
+                        "nmax 10, page cache", "series_s": t_series, "snapshots_per_s": nfile / t_series,
+            "particles_per_s": nfile * n / t_series, "per_file_calls_s": t_each}
 
 
 def orbit_extra(eof_path, cos_d, sin_d, sph_cache, sph_model, sph_table, hx, hy, hz, hm, args, n=N1, nint=2000,

@@ -387,3 +387,19 @@ def read_binary_eof_coefficients_dict(coeffile):
         E.sin = np.array(c[t, 1])
         out[E.time] = E
     return out
+
+
+def compute_coefficients_series(files, comp, eof_file, outfile=None, precision="f64", reader="psp"):
+    """Coefficients of component `comp` in each snapshot file (PSP, or SPL
+    main files with reader='spl'): (times, coefs[t, cos/sin, m, n]), the next
+    file read while the GPU accumulates the current one.  With `outfile`,
+    also written as an EXP Cylinder coefficient file
+    (exptool_gb300.io.outcoef.write_new_cylinder)."""
+    from ..io import outcoef, series
+    table = table_from_file(eof_file)
+    T, cs = series.coefficient_series(
+        files, comp, lambda x, y, z, m: torch.stack(table.accumulate(x, y, z, m, precision=precision)), reader)
+    c = series.stack_to_host(cs)
+    if outfile is not None:
+        outcoef.write_new_cylinder(outfile, T, c)
+    return T, c

@@ -267,3 +267,20 @@ def read_binary_sl_coefficients(coeffile):
     EXP SphereSL coefficients -> (times, coefs[t, lm, n])."""
     from ..io import outcoef
     return outcoef.read_old_spheresl(coeffile)
+
+
+def compute_coefficients_series(files, comp, sph_file, mod_file, outfile=None, no_odd=False, precision="f64",
+                                reader="psp"):
+    """Coefficients of component `comp` in each snapshot file (PSP, or SPL
+    main files with reader='spl'): (times, expcoef[t, (lmax+1)^2, nmax]), the
+    next file read while the GPU accumulates the current one.  With
+    `outfile`, also written as an EXP SphereSL coefficient file
+    (exptool_gb300.io.outcoef.write_new_spheresl)."""
+    from ..io import outcoef, series
+    table = table_from_files(sph_file, mod_file)
+    T, cs = series.coefficient_series(
+        files, comp, lambda x, y, z, m: table.accumulate(x, y, z, m, no_odd=no_odd, precision=precision), reader)
+    ec = series.stack_to_host(cs)
+    if outfile is not None:
+        outcoef.write_new_spheresl(outfile, T, ec)
+    return T, ec

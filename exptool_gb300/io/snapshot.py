@@ -131,6 +131,11 @@ def _pinned_bytes(nbytes):
     return torch.empty(max(int(nbytes), 16), dtype=torch.uint8, pin_memory=True)
 
 
+def _grow(buf, nbytes):
+    """`buf` if it holds nbytes, else a new page-locked buffer."""
+    return buf if buf is not None and buf.numel() >= nbytes else _pinned_bytes(nbytes)
+
+
 def _read_into(path, offset, buf, at, nbytes):
     """nbytes of `path` from `offset` into buf[at:at+nbytes] (one read)."""
     view = memoryview(buf.numpy())[at:at + nbytes]
