@@ -520,6 +520,7 @@ def gpu_arm(args, rank, world):
     learned_sl = learned_extra()
     snap = snapshot_extra()
     snap["coefficient_series"] = series_extra()
+    freqs = frequencies_extra()
 
     peak, peak_kind = measured_peaks()
     nnode = 257 * 257
@@ -597,6 +598,7 @@ def gpu_arm(args, rank, world):
                            "ms_per_step": sl_ms, "value": N0 / (sl_ms * 1e-3), "unit": "particles/s"},
         "orbits": orbits,
         "snapshot_reader": snap,
+        "orbit_frequencies": freqs,
         "batched_spherical": batched,
         "learned_spherical": learned_sl,
         "clocks": clocks,
@@ -673,6 +675,48 @@ def snapshot_extra(n=N1, reps=5):
             "device_columns_s": t_dev, "device_GBps": nbytes / t_dev / 1e9,
             "host_columns_s": t_host, "host_GBps": nbytes / t_host / 1e9,
             "reference_method_s": t_ref, "reference_method_GBps": nbytes / t_ref / 1e9}
+
+
+def frequencies_extra(no=16384, nt=2048, sample=512, order=4):
+    """Fundamental frequencies (Hann-windowed FFT of x + i vx, relative maxima,
+    three strongest) of `no` orbits x `nt` steps, host map in, host results
+    out; beside it the same algorithm vectorised in NumPy (pocketfft) on a
+    `sample` of the orbits, scaled to all."""
+    import torch
+    from exptool_gb300.orbits import frequencies as fq
+    from exptool_gb300.orbits.orbit import Orbits
+    rng = np.random.default_rng(41)
+    T = np.arange(nt) * 0.01
+    w = 6.0 * (1.0 + 0.5 * rng.random((3, no)))
+    amp = np.array([1.0, 0.45, 0.2])[:, None]
+    X = sum(amp[k] * np.cos(w[k] * T[:, None]) for k in range(3))
+    VX = sum(-amp[k] * w[k] * np.sin(w[k] * T[:, None]) for k in range(3))
+    O = Orbits()
+    O["T"], O["X"], O["VX"] = T, X, VX
+    fq.find_fundamental_frequency_map(O, order=order)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fq.find_fundamental_frequency_map(O, order=order)
+    t_gpu = time.perf_counter() - t0
+
+    def numpy_map(x, v):
+        freq = np.fft.fftfreq(x.shape[0], d=T[1] - T[0])
+        a = np.abs(np.fft.fft((x + 1j * v) * np.hanning(x.shape[0])[:, None], axis=0).real)
+        n = a.shape[0]
+        idx = np.arange(n)
+        mask = np.ones_like(a, dtype=bool)
+        for k in range(1, order + 1):
+            mask &= (a > a[np.clip(idx + k, 0, n - 1)]) & (a > a[np.clip(idx - k, 0, n - 1)])
+        mask &= (freq > 0)[:, None]
+        vals = np.where(mask, a, -np.inf)
+        return freq[np.argsort(-vals, axis=0)[:3]]
+
+    t0 = time.perf_counter()
+    numpy_map(X[:, :sample], VX[:, :sample])
+    t_np = (time.perf_counter() - t0) * no / sample
+    return {"workload": f"{no} orbits x {nt} steps, fundamental frequencies (order {order}), host map in and out",
+            "gpu_s": t_gpu, "orbits_per_s": no / t_gpu, "numpy_vectorised_s_scaled": t_np,
+            "numpy_sample_orbits": sample}
 
 
 def series_extra(nfile=8, n=N1):

@@ -535,12 +535,45 @@ def outcoef_case(ref):
     np.savez_compressed(P("outcoef.npz"), **out)
 
 
+def frequencies_case(ref):
+    """Orbit maps of 48 orbits x 2048 steps (freq_signals: three sinusoids of
+    distinct amplitudes per coordinate, plus noise) through the reference's
+    orbits/frequencies functions (each call given a fresh window list: the
+    reference's default list is modified by its calls).  The maps are stored
+    as their generating parameters."""
+    import freq_signals
+    from exptool.orbits import frequencies as fq
+    prm = freq_signals.params()
+    sig = freq_signals.build(prm)
+    T = sig["T"]
+    O = ref.orbit.Orbits()
+    for k, v in sig.items():
+        O[k] = v
+    out = {f"param_{k}": np.asarray(v) for k, v in prm.items()}
+    fq.find_fundamental_frequency_map(O, window=[0, 10000], order=4)
+    for i in (1, 2, 3):
+        out[f"map_OX{i}"] = O[f"OX{i}"]
+    one = {"T": T, "X": O["X"][:, 5], "VX": O["VX"][:, 5]}
+    one, freq, spec = fq.find_fundamental_frequency(one, window=[0, 10000], retall=True, order=3)
+    for i in (1, 2, 3):
+        out[f"one_OX{i}"] = np.float64(one[f"OX{i}"])
+    out["one_freq"], out["one_spec"] = freq, spec
+    out["org_omega"], out["org_power"] = fq.organize_frequencies(freq, spec, order=4)
+    R = np.sqrt(O["X"][:, 7] ** 2 + O["Y"][:, 7] ** 2)
+    phi = np.arctan2(O["Y"][:, 7], O["X"][:, 7])
+    out["orbit_freqs"] = np.array(fq.find_orbit_frequencies(T, R, phi, O["Z"][:, 7], window=[0, 10000]))
+    r, t, z = fq.find_orbit_map_frequencies(O, window=[0, 10000])
+    out["map_OmegaR"], out["map_OmegaT"], out["map_OmegaZ"] = r, t, z
+    np.savez_compressed(P("frequencies.npz"), **out)
+
+
 def main(only_snapshots=False):
-    """All fixtures, or (argument ``snapshots``) only the snapshot and
-    coefficient-file reader ones."""
+    """All fixtures, or (argument ``snapshots``) only the snapshot-reader,
+    coefficient-file and orbit-frequency ones."""
     ref = refshim.load()
     snapshot_case()
     outcoef_case(ref)
+    frequencies_case(ref)
     if only_snapshots:
         return
     sl_out = {}
