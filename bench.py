@@ -203,6 +203,16 @@ def learned_extra(steps=20000, batch=8192, n_eval=10_000_000, n_cal=200_000, rep
     ec_d = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)))
     ec = dev.to_host(ec_d)
     rep = lb.calibrate(ec, np.stack([x[:n_cal], y[:n_cal], z[:n_cal]], axis=1), bar=1e-5)
+    # the method without the trained network: output layer zeroed, the prior
+    # fitted by least squares alone, judged the same way; then restored
+    band_use, trained = lb.band_use.copy(), lb.params()
+    prior_only = trained.copy()
+    prior_only[:, learned.LAYOUT["W4"]:learned.LAYOUT["SIZE"]] = 0.0
+    lb.set_params(prior_only)
+    rep_prior = lb.calibrate(ec, np.stack([x[:n_cal], y[:n_cal], z[:n_cal]], axis=1), bar=1e-5)
+    lb.set_params(trained, step=lb.steps_done)
+    lb.prepare(ec)
+    lb.band_use = band_use
     xyzw = torch.zeros((n_eval, 4), dtype=torch.float32)
     for k, a in enumerate((x, y, z)):
         xyzw[:, k] = torch.from_numpy(a.astype(np.float32))
@@ -267,6 +277,7 @@ def learned_extra(steps=20000, batch=8192, n_eval=10_000_000, n_cal=200_000, rep
             "network_pass_tflops_incl_second_pass": {
                 k: round(rad_flops / (res[k]["ms"] * 1e-3) / 1e12, 1) for k in ("network_tcgen05", "network_mma_sync")},
             "force_err_vs_table_f64": {"bar": 1e-5, "network_median": rep["net_median"],
+                                       "prior_alone_median": rep_prior["net_median"],
                                        "table_f32_median": rep["table32_median"],
                                        "hybrid_median": rep["hybrid_median"], "hybrid_max": rep["hybrid_max"],
                                        "bands_on_network": rep["net_bands"],
