@@ -847,8 +847,10 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi
 
 // Double-float evaluation of the binned records (FP64 path,
 // accumulated_eval_particles); SORTED as for k_cyl_eval_sorted.
+// Launch bounds and the twice-unrolled m loop were measured on 1e6 disc
+// particles: 0.129 ms with up to ~127 registers, against 0.135 ms at 72.
 template <bool SORTED>
-__global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
+__global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
                                                             const BinRec<df>* __restrict__ recs, int m1, int m2,
                                                             double* o0, double* o1, double* o2, double* o3,
                                                             double* o4) {
@@ -883,14 +885,22 @@ __global__ void __launch_bounds__(128) k_cyl_eval_sorted_df(CylTab<double> T, co
     df p0{0.f, 0.f};
     dacc p, fr, fp, fz;
     if (m1 <= 0 && m2 >= 0) {                   // m = 0: cos 0 = 1, sin 0 = 0
-      df v[6];
-      interp(0, v);
+      df v[3];                                  // the sine fields of m = 0 are zero
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        dacc a;
+        a.fma(f00[k], w0);
+        a.fma(f10[k], w1);
+        a.fma(f01[k], w2);
+        a.fma(f11[k], w3);
+        v[k] = a.raw();
+      }
       p0 = v[0];
       fr.s = v[1].h; fr.e = v[1].l;
       fz.s = v[2].h; fz.e = v[2].l;
     }
     df cprev{1.f, 0.f}, sprev{0.f, 0.f}, ccur = c1, scur = s1;
-#pragma unroll 1
+#pragma unroll 2
     for (int m = 1; m <= T.mmax; ++m) {
       df cm, sm;
       if (m == 1) { cm = c1; sm = s1; }
@@ -1491,6 +1501,8 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         constexpr int MC = decltype(mc)::value;
         using Mth = std::conditional_t<F64, DepDF, DepF32>;
         constexpr int NP = F64 ? 2 : 1;
+        // (one pass with 2-3 blocks per SM, or two passes with 2-3, measured
+        // 0.127-0.131 ms against 0.121 ms for two passes at 4 blocks per SM)
         auto kern = k_cyl_deposit_sorted<Mth, MC, NP>;
         const int run = F64 ? 8 : 6;
         const long long nrun = (n + run - 1) / run;
