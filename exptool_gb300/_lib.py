@@ -46,6 +46,8 @@ _SIGS = {
     "xt_abi_version": (c_int, []),
     "xt_last_error": (ctypes.c_char_p, []),
     "xt_pointer_access": (c_int, [c_vp]),
+    "xt_copy_async": (c_int, [c_int, c_dpp, c_dpp, ctypes.POINTER(c_sz), c_vp]),
+    "xt_stream_sync": (c_int, [c_vp]),
     "xt_sph_table_create": (c_int, [c_int, c_int, c_int, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_vp, c_vp, c_vp, c_vp,
                                     ctypes.POINTER(c_vp)]),
     "xt_sph_table_destroy": (c_int, [c_vp]),

@@ -284,6 +284,21 @@ int xt_abi_version(void) { return 1; }
 const char* xt_last_error(void) { return xt::g_err.c_str(); }
 int xt_pointer_access(const void* p) { return xt::pointer_access(p); }
 
+int xt_copy_async(int ncopy, void* const* dst, const void* const* src, const size_t* bytes, void* stream) {
+  XT_REQUIRE(ncopy >= 0 && (ncopy == 0 || (dst && src && bytes)), "NULL copy list");
+  for (int i = 0; i < ncopy; ++i) {
+    if (!bytes[i]) continue;
+    XT_REQUIRE(dst[i] && src[i], "copy %d: NULL pointer", i);
+    XT_CUDA(cudaMemcpyAsync(dst[i], src[i], bytes[i], cudaMemcpyDefault, xt::as_stream(stream)));
+  }
+  return XT_OK;
+}
+
+int xt_stream_sync(void* stream) {
+  XT_CUDA(cudaStreamSynchronize(xt::as_stream(stream)));
+  return XT_OK;
+}
+
 int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, double rmax, double scale,
                         const double* xi, const double* p0, const double* d0, const double* ev, const double* ef,
                         void** handle) {

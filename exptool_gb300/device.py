@@ -80,6 +80,28 @@ def pinned_empty(n: int, count: int) -> list:
     return [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(count)]
 
 
+def _addr(a) -> int:
+    """Address of a tensor's, an array's or a raw address's data."""
+    if isinstance(a, int):
+        return a
+    if isinstance(a, torch.Tensor):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def copy_and_sync(pairs):
+    """Copy each (destination address, source address, bytes) on the current
+    stream with one library call, then wait for the stream."""
+    lib = _lib.load()
+    k = len(pairs)
+    dst = (ctypes.c_void_p * k)(*[p[0] for p in pairs])
+    src = (ctypes.c_void_p * k)(*[p[1] for p in pairs])
+    nb = (ctypes.c_size_t * k)(*[p[2] for p in pairs])
+    st = stream_ptr()
+    _lib.check(lib.xt_copy_async(k, dst, src, nb, st), "xt_copy_async")
+    _lib.check(lib.xt_stream_sync(st), "xt_stream_sync")
+
+
 def to_host_many(ts) -> list:
     """Several device tensors -> NumPy arrays in pinned host memory: all
     copies enqueued on the current stream, one synchronisation."""
@@ -324,21 +346,29 @@ class CylTable:
         count and precision: returns the (2, mmax+1, norder) coefficient block
         (cos, sin) and the (5, n) block of p0, p, fr, fp, fz.  The next call on
         this thread with the same size overwrites both, so callers copy them
-        out first.  R goes to ``r_out`` (a length-n float64 tensor, device or
-        page-locked host memory; the binning kernel writes it directly)."""
+        out first.  R goes to ``r_out`` (a length-n float64 tensor or a raw
+        address, device or page-locked host memory; the binning kernel writes
+        it directly).  The call's C arguments are kept with the buffers, so a
+        repeated call only sets the particle and R addresses."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
+        key = (n, pc)
         b = getattr(self._fused_bufs, "v", None)
-        if b is None or b[0] != (n, pc):
+        if b is None or b[0] != key:
             need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
-            b = ((n, pc), torch.empty(need, dtype=torch.uint8, device=device()),
-                 torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device()),
-                 torch.empty((6, n), dtype=torch.float64, device=device()))
+            ws = torch.empty(need, dtype=torch.uint8, device=device())
+            coef = torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device())
+            res = torch.empty((6, n), dtype=torch.float64, device=device())
+            outs = (ctypes.c_void_p * 6)(*[res.data_ptr() + 8 * n * k for k in range(6)])
+            b = (key, ws, coef, res, outs)
             self._fused_bufs.v = b
-        _, ws, coef, res = b
-        outs = list(res[:5]) + [r_out if r_out is not None else res[5]]
-        self.accumulate_eval(x, y, z, m, precision=precision, m1=m1, m2=m2, workspace=ws,
-                             nan_to_origin=nan_to_origin, outs=outs, coef=coef)
+        _, ws, coef, res, outs = b
+        outs[5] = _addr(r_out) if r_out is not None else res.data_ptr() + 40 * n
+        cos_p = coef.data_ptr()
+        _lib.check(self._lib.xt_cyl_accumulate_eval(self.handle, _addr(x), _addr(y), _addr(z), _addr(m), n, pc,
+                                                    int(m1), int(m2), int(bool(nan_to_origin)), cos_p,
+                                                    cos_p + 8 * (self.mmax + 1) * self.norder, outs, ws.data_ptr(),
+                                                    ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return coef, res[:5]
 
     def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):

@@ -59,6 +59,12 @@ const char *xt_last_error(void);
 /* XT_PTR_* class of p on the current device.  No counterpart in the reference
  * (it has no device); used to pass host arrays straight to the kernels. */
 int xt_pointer_access(const void *p);
+/* ncopy asynchronous copies dst[i] <- src[i] of bytes[i] bytes on `stream`
+ * (one cudaMemcpyAsync each, direction from the pointers), and a stream
+ * synchronisation.  No counterpart in the reference; they let a host caller
+ * collect several results with one call. */
+int xt_copy_async(int ncopy, void *const *dst, const void *const *src, const size_t *bytes, void *stream);
+int xt_stream_sync(void *stream);
 
 /* --------------------------------------------------------------- spherical (SL) */
 /* Upload an SL basis: replaces the per-call table reads of
