@@ -392,7 +392,10 @@ def gpu_arm(args, rank, world):
     table = eof.table_from_file(path)
     xd, yd, zd, md = (dev.to_dev(a) for a in (x, y, z, m))
     ws = torch.empty(_lib.load().xt_cyl_accumulate_workspace(table.handle), dtype=torch.uint8, device="cuda")
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    # L2 flush between timed steps: a 4 x L2 write, long enough on the device
+    # (~80 us) that the host has submitted the next step before it ends, so the
+    # timed events see no idle gap from host-side submission
+    flush = torch.empty(4 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     want = [1, 1, 1, 1, 1, 1, 0, 0]
 
     def step(prec):
@@ -404,8 +407,11 @@ def gpu_arm(args, rank, world):
     fws = torch.empty(_lib.load().xt_cyl_accumulate_eval_workspace(table.handle, N1, _lib.XT_F64), dtype=torch.uint8,
                       device="cuda")
 
+    fouts = [torch.empty(N1, dtype=torch.float64, device="cuda") for _ in range(6)]
+    fcoef = torch.empty((2, table.mmax + 1, table.norder), dtype=torch.float64, device="cuda")
+
     def fused(prec):
-        return table.accumulate_eval(xd, yd, zd, md, precision=prec, workspace=fws)
+        return table.accumulate_eval(xd, yd, zd, md, precision=prec, workspace=fws, outs=fouts, coef=fcoef)
 
     def timed_fused(prec, steps, warmup):
         for _ in range(warmup):
@@ -549,13 +555,15 @@ def gpu_arm(args, rank, world):
     def stage_alg(rs):
         # algorithmic bytes per launch of each stage (rs = bytes of the compute
         # type): particle records are 48 B (double-float) or 32 B (FP32); the
-        # FP64 path reads its tables as hi + lo FP32 pairs (8 B an entry), the
-        # mixed path's field reads the FP32 tables alone
+        # double-float tables are an FP32 rounding and a 16-bit remainder
+        # (6 B an entry), read by the contraction in both paths and by the FP64
+        # field; the mixed path's field reads the FP32 roundings alone
         rec = 48 if rs == 8 else 32
         grid = 14 * nnode * 8
+        tab = 6 if rs == 8 else 4
         return [N1 * (32 + rec + 8 + 4), 2 * 4 * 65536, N1 * (2 * rec + 4), N1 * rec + grid,
-                13 * 18 * nnode * 8 + grid,
-                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * rs + nnode * 7 * 6 * rs,
+                13 * 18 * nnode * 6 + grid + 14 * nnode * 4,
+                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * tab + nnode * 7 * 6 * rs,
                 N1 * (rec + 40) + nnode * 7 * 6 * rs]
 
     alg64 = stage_alg(8)
@@ -583,7 +591,7 @@ def gpu_arm(args, rank, world):
         "data": "synthetic (seeded exponential disc, seed 1; tables from the project's EOF builder)",
         "config": {"workload": "cylindrical EOF disc: accumulate + force eval", "particles_per_gpu": N1,
                    "mmax": 6, "norder": 18, "numx": 256, "numy": 256, "cmap": 1,
-                   "l2": "flushed between timed steps (512 MB write outside the timed events)",
+                   "l2": "flushed between timed steps (516 MB write outside the timed events)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * N1 / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients_and_forces, pinned numpy inputs",

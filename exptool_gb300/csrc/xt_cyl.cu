@@ -67,9 +67,15 @@ struct CylHandle {
   double XMIN, dX, YMIN, dY, ascale, hscale;
   size_t nnode;
   double* tab = nullptr;   // [8][mmax+1][norder][nnode]: potC rforceC zforceC densC potS rforceS zforceS densS
-  float* tab_f32 = nullptr;  // the same tables rounded to FP32 (mixed path), rows of pitch_f nodes
-  float* tab_lo = nullptr;   // FP32 remainders: tab_f32 + tab_lo is a double-float copy of tab
-  size_t pitch_f = 0;        // row pitch of tab_f32 / tab_lo: nnode rounded up to 4 (16-byte node quads)
+  float* tab_f32 = nullptr;  // the same tables rounded to FP32 (separate mixed path), rows of pitch_f nodes
+  size_t pitch_f = 0;        // row pitch of tab_f32 and of the deposit grids: nnode rounded up to 4
+  // Tables of the fused paths, tiled by blocks of kTileNodes nodes: block b
+  // holds, for rows r = (f * (mmax+1) + m) * norder + k with f = potC rforceC
+  // zforceC potS rforceS zforceS, the entries of nodes b*kTileNodes ... as
+  // FP32 roundings (tile_hi) and 16-bit remainders (tile_lo, lo16_decode).
+  float* tile_hi = nullptr;
+  short* tile_lo = nullptr;
+  size_t tile_rows = 0;      // 6 (mmax+1) norder
   CylTab<double> tab_d;
   CylTab<float> tab_f;
   std::mutex graph_mu;       // guards fused and capture
@@ -85,19 +91,36 @@ static inline const float* tab_ptr_f32(const CylHandle* h, int which) {
   return h->tab_f32 + (size_t)which * (h->mmax + 1) * h->norder * h->pitch_f;
 }
 
-// hi = FP32 rounding of a, lo = FP32 rounding of a - hi, rows of nnode
-// entries re-laid with a pitch of `pitch` entries (padding zeroed); table
-// set-up, once.
-__global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo,
-                            size_t rows, size_t nnode, size_t pitch) {
+// hi = FP32 rounding of a, rows of nnode entries re-laid with a pitch of
+// `pitch` entries (padding zeroed); table set-up, once.
+__global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi, size_t rows, size_t nnode,
+                            size_t pitch) {
   const size_t n = rows * pitch;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t row = i / pitch, node = i - row * pitch;
-    float h = 0.f, l = 0.f;
+    hi[i] = node < nnode ? (float)a[row * nnode + node] : 0.f;
+  }
+}
+
+constexpr int kTileNodes = 64;   // nodes per block of the tiled fused tables
+
+// Tiled fused tables (CylHandle::tile_hi/tile_lo) from the FP64 tables a
+// ([8][mmax+1][norder][nnode]); entries past nnode are zero.  Set-up, once.
+__global__ void k_tile_tab(const double* __restrict__ a, float* __restrict__ hi, short* __restrict__ lo,
+                           int nmk, size_t nnode, size_t nblk) {
+  const size_t rows = 6 * (size_t)nmk;
+  const size_t n = nblk * rows * kTileNodes;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = i / (rows * kTileNodes), rem = i - b * rows * kTileNodes;
+    const size_t row = rem / kTileNodes, node = b * kTileNodes + (rem - row * kTileNodes);
+    const int f = (int)(row / nmk), mk = (int)(row - (size_t)f * nmk);
+    const int t = f < 3 ? f : f + 1;                       // skip densC
+    float h = 0.f;
+    short l = 0;
     if (node < nnode) {
-      const double v = a[row * nnode + node];
+      const double v = a[((size_t)t * nmk + mk) * nnode + node];
       h = (float)v;
-      l = (float)(v - (double)h);
+      l = lo16_encode(v, h);
     }
     hi[i] = h;
     lo[i] = l;
@@ -196,10 +219,16 @@ __global__ void __launch_bounds__(256) k_cyl_contract_partial(const TT* __restri
 }
 
 // Fixed-order sum of the partials: cos[m,k], sin[m,k].
+// mzero_sin: norder when the m = 0 sine partials were not written (their
+// sums are zero), else 0.
 __global__ void k_cyl_contract_final(const double* __restrict__ part, int nout, int nchunk, double* __restrict__ cos_out,
-                                     double* __restrict__ sin_out) {
+                                     double* __restrict__ sin_out, int mzero_sin) {
   const int out = blockIdx.x * blockDim.x + threadIdx.x;
   if (out >= nout) return;
+  if (mzero_sin && (out & 1) && (out >> 1) < mzero_sin) {   // m = 0 sine: no partials, zero
+    sin_out[out >> 1] = 0.0;
+    return;
+  }
   double acc = 0.0;
   for (int c = 0; c < nchunk; ++c) acc += part[(size_t)out * nchunk + c];
   const int mk = out >> 1;
@@ -353,7 +382,13 @@ __global__ void __launch_bounds__(256) k_cyl_binrec(CylTab<R> T, const double* _
                                                     const double* __restrict__ y, const double* __restrict__ z,
                                                     const double* __restrict__ mass, long long n,
                                                     int* __restrict__ hist, BinRec<R>* __restrict__ rec,
-                                                    double* __restrict__ Rout, int nan_to_origin) {
+                                                    double* __restrict__ Rout, int nan_to_origin,
+                                                    double* __restrict__ zD, float* __restrict__ zE, long long nz) {
+  // zero the deposit grids (read by the deposit three kernels later)
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nz; i += (long long)gridDim.x * blockDim.x) {
+    zD[i] = 0.0;
+    zE[i] = 0.f;
+  }
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     R xx = (R)x[p], yy = (R)y[p], zz = (R)z[p];
@@ -418,7 +453,13 @@ __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecD
                                                        const double* __restrict__ y, const double* __restrict__ z,
                                                        const double* __restrict__ mass, long long n,
                                                        int* __restrict__ hist, BinRec<df>* __restrict__ rec,
-                                                       double* __restrict__ Rout, int nan_to_origin) {
+                                                       double* __restrict__ Rout, int nan_to_origin,
+                                                       double* __restrict__ zD, float* __restrict__ zE, long long nz) {
+  // zero the deposit grids (read by the deposit three kernels later)
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nz; i += (long long)gridDim.x * blockDim.x) {
+    zD[i] = 0.0;
+    zE[i] = 0.f;
+  }
   const df xmin = K.xmin, idx = K.idx, ymin = K.ymin, idy = K.idy, ias = K.ias, one = {1.f, 0.f};
   const df soft = K.soft, zeps = K.zeps, m4pi = K.m4pi;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
@@ -772,20 +813,20 @@ template <>
 __device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
 
 // Field of the fused paths: coefficients staged in shared memory as df,
-// lazily renormalised df sums on the FP32 pipe (no FP64 pipe work at all).  SPLIT:
-// double-float tables hi + lo and a df field (FP64 path); otherwise the FP32
-// tables alone and an FP32 field (mixed path).  Each thread computes one
-// (m, field) entry for a quad of consecutive nodes from 16-byte loads of the
-// tables (rows of `pitch` entries, a multiple of 4), with four table rows in
-// flight and four independent sums; a warp covers 128 nodes.  The block's
-// QN = 4 * TQ nodes are written back contiguously through shared memory in the
-// layout of k_cyl_field with nf = 6.
-template <typename OT, int TQ, bool SPLIT>
-__global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                    size_t pitch, const double* __restrict__ cosc,
-                                                    const double* __restrict__ sinc, int mmax, int norder,
-                                                    size_t nnode, OT* __restrict__ F) {
-  constexpr int QN = 4 * TQ;
+// lazily renormalised df sums on the FP32 pipe (no FP64 pipe work at all).
+// SPLIT: double-float tables (tiled FP32 roundings + 16-bit remainders) and
+// a df field (FP64 path); otherwise the tiled FP32 roundings alone and an
+// FP32 field (mixed path).  Block b owns node block b of the tiled tables
+// (kTileNodes nodes, one contiguous region of them).  Each thread computes
+// one (m, field) entry for a quad of consecutive nodes from 16-byte loads of
+// hi and 8-byte loads of the remainders, RB table rows in flight and four
+// independent sums.  The block's nodes are written back contiguously through
+// shared memory in the layout of k_cyl_field with nf = 6.
+template <typename OT, bool SPLIT, int RB, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict__ hi, const short* __restrict__ lo,
+                                                    const double* __restrict__ cosc, const double* __restrict__ sinc,
+                                                    int mmax, int norder, size_t nnode, OT* __restrict__ F) {
+  constexpr int QN = kTileNodes, TQ = QN / 4;
   extern __shared__ unsigned char smem_raw[];
   df* cf = reinterpret_cast<df*>(smem_raw);                       // [2][(mmax+1)*norder]
   OT* tile = reinterpret_cast<OT*>(cf + 2 * (mmax + 1) * norder);
@@ -795,45 +836,36 @@ __global__ void __launch_bounds__(256) k_cyl_field2(const float* __restrict__ hi
   const int nf = 6;
   const int mf_total = (mmax + 1) * nf;
   const size_t node0 = (size_t)blockIdx.x * QN;
-  const size_t tsize = (size_t)(mmax + 1) * norder * pitch;
-  const int tmap[6] = {0, 1, 2, 4, 5, 6};
+  const size_t tbase = (size_t)blockIdx.x * 6 * ncoef * QN;
   for (int task = threadIdx.x; task < TQ * mf_total; task += blockDim.x) {
     const int ql = task % TQ;
     const int mf = task / TQ;
     const int m = mf / nf, f = mf % nf;
-    const size_t node = node0 + 4 * ql;
     dacc acc[4];
-    if (node < nnode && !(m == 0 && f >= 3)) {
-      const int ti = tmap[f];
-      const df* coef = cf + ((ti >= 4) ? ncoef : 0) + m * norder;
-      const size_t t0 = (size_t)ti * tsize + (size_t)m * norder * pitch + node;
-      int k = 0;
-      for (; k + 4 <= norder; k += 4) {
-        float4 vh[4], vl[4];
+    if (node0 + 4 * ql < nnode && !(m == 0 && f >= 3)) {
+      const df* coef = cf + ((f >= 3) ? ncoef : 0) + m * norder;
+      const size_t t0 = tbase + (size_t)(f * ncoef + m * norder) * QN + 4 * ql;
+      for (int k0 = 0; k0 < norder; k0 += RB) {
+        float4 vh[RB];
+        short4 vl[RB];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          vh[u] = *reinterpret_cast<const float4*>(hi + t0 + (size_t)(k + u) * pitch);
-          vl[u] = SPLIT ? *reinterpret_cast<const float4*>(lo + t0 + (size_t)(k + u) * pitch)
-                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < RB; ++u) {
+          if (k0 + u < norder) {
+            vh[u] = *reinterpret_cast<const float4*>(hi + t0 + (size_t)(k0 + u) * QN);
+            vl[u] = SPLIT ? *reinterpret_cast<const short4*>(lo + t0 + (size_t)(k0 + u) * QN)
+                          : make_short4(0, 0, 0, 0);
+          }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const df c = coef[k + u];
-          acc[0].fma(c, df{vh[u].x, vl[u].x});
-          acc[1].fma(c, df{vh[u].y, vl[u].y});
-          acc[2].fma(c, df{vh[u].z, vl[u].z});
-          acc[3].fma(c, df{vh[u].w, vl[u].w});
+        for (int u = 0; u < RB; ++u) {
+          if (k0 + u < norder) {
+            const df c = coef[k0 + u];
+            acc[0].fma(c, df{vh[u].x, SPLIT ? lo16_decode(vh[u].x, vl[u].x) : 0.f});
+            acc[1].fma(c, df{vh[u].y, SPLIT ? lo16_decode(vh[u].y, vl[u].y) : 0.f});
+            acc[2].fma(c, df{vh[u].z, SPLIT ? lo16_decode(vh[u].z, vl[u].z) : 0.f});
+            acc[3].fma(c, df{vh[u].w, SPLIT ? lo16_decode(vh[u].w, vl[u].w) : 0.f});
+          }
         }
-      }
-      for (; k < norder; ++k) {
-        const float4 vh = *reinterpret_cast<const float4*>(hi + t0 + (size_t)k * pitch);
-        const float4 vl = SPLIT ? *reinterpret_cast<const float4*>(lo + t0 + (size_t)k * pitch)
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
-        const df c = coef[k];
-        acc[0].fma(c, df{vh.x, vl.x});
-        acc[1].fma(c, df{vh.y, vl.y});
-        acc[2].fma(c, df{vh.z, vl.z});
-        acc[3].fma(c, df{vh.w, vl.w});
       }
     }
 #pragma unroll
@@ -932,82 +964,86 @@ __global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T,
 
 static const int kContractChunks = 8;
 static const int kContractChunksDf = 64;   // most node chunks of k_cyl_contract_df
+static const int kContractRows = 6;        // orders k per k_cyl_contract_df block
 
 // Coefficient contraction of the fused paths:
 //   cos/sin[m][k] = sum over nodes of (D + E)[2m+cs][node] * pot{C,S}[m][k][node]
 // (E: the FP32 companion grid of the double-float deposit's error parts).
-// Block (chunk, m, cs) takes a range of node quads; each thread multiplies
-// the quads' FP64 sums (split into float pairs by integer operations) by the
-// double-float tables (16-byte loads of hi and lo, rows of `pitch` entries,
-// six rows in flight) for all k <= KMAX at once, in lazily renormalised df
-// sums.  The block's sums are reduced in df (warp shuffles, then shared
-// memory) and stored per chunk as FP64 for k_cyl_contract_final.  D planes and
-// table rows share the pitch; padding entries are zero in both.
-template <int KMAX>
-__global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict__ hi, const float* __restrict__ lo,
+// Block (x = chunk * ngroup + g, y = p) takes a range of node quads of the
+// (m, cs) pair p (0: m = 0 cosine; 2m - 1, 2m: m >= 1 cosine, sine; the m = 0
+// sine is identically zero and has no block) for the KB orders k of group g.
+// Each thread multiplies the quads' FP64 sums (split into float pairs by
+// integer operations) by the tiled double-float tables (16-byte loads of hi,
+// 8-byte loads of the 16-bit remainders, all KB rows in flight) in lazily
+// renormalised df sums.  The groups of one chunk are neighbouring blocks, so
+// D and E are read once from DRAM.  The block's sums are reduced in df (warp
+// shuffles, then shared memory) and stored per chunk as FP64 for
+// k_cyl_contract_final.  D planes have a pitch of `pitch` nodes; padding
+// entries are zero in D and in the tiled tables.
+template <int KB>
+__global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict__ hi, const short* __restrict__ lo,
                                                          size_t pitch, const double* __restrict__ D,
                                                          const float* __restrict__ E, int mmax, int norder,
-                                                         size_t nnode, int nchunk, double* __restrict__ part) {
-  constexpr int RB = 6;                         // rows in flight
-  static_assert(KMAX % RB == 0, "KMAX must be a multiple of the row batch");
-  const int chunk = blockIdx.x, m = blockIdx.y, cs = blockIdx.z;
-  dacc acc[KMAX];
-  if (!(cs == 1 && m == 0)) {
+                                                         size_t nnode, int nchunk, int ngroup,
+                                                         double* __restrict__ part) {
+  const int chunk = blockIdx.x / ngroup, g = blockIdx.x - chunk * ngroup, p = blockIdx.y;
+  const int m = (p + 1) >> 1, cs = p ? ((p + 1) & 1) : 0;
+  const int kbase = g * KB;
+  dacc acc[KB];
+  {
     const int nq = (int)((nnode + 3) / 4);
     const int per = (nq + nchunk - 1) / nchunk;
     const int q0 = chunk * per, q1 = min(q0 + per, nq);
-    const size_t tsz = (size_t)(mmax + 1) * norder * pitch;
-    const size_t rowbase = (size_t)(cs ? 4 : 0) * tsz + (size_t)m * norder * pitch;
+    const size_t nrow = 6 * (size_t)(mmax + 1) * norder;
+    const size_t row0 = ((size_t)(cs ? 3 : 0) * (mmax + 1) + m) * norder + kbase;
     const double* d = D + (size_t)(2 * m + cs) * pitch;
     const float* ep = E + (size_t)(2 * m + cs) * pitch;
     for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       const size_t node = 4 * (size_t)q;
+      const size_t tb = ((node / kTileNodes) * nrow + row0) * kTileNodes + node % kTileNodes;
+      float4 vh[KB];
+      short4 vl[KB];
+#pragma unroll
+      for (int u = 0; u < KB; ++u) {
+        if (kbase + u < norder) {
+          const size_t o = tb + (size_t)u * kTileNodes;
+          vh[u] = *reinterpret_cast<const float4*>(hi + o);
+          vl[u] = *reinterpret_cast<const short4*>(lo + o);
+        }
+      }
       const double2 da = *reinterpret_cast<const double2*>(d + node);
       const double2 db = *reinterpret_cast<const double2*>(d + node + 2);
       const float4 ev = *reinterpret_cast<const float4*>(ep + node);
       const df dv[4] = {df_add(df_split_or_from(da.x), {ev.x, 0.f}), df_add(df_split_or_from(da.y), {ev.y, 0.f}),
                         df_add(df_split_or_from(db.x), {ev.z, 0.f}), df_add(df_split_or_from(db.y), {ev.w, 0.f})};
 #pragma unroll
-      for (int k0 = 0; k0 < KMAX; k0 += RB) {
-        if (k0 >= norder) break;
-        float4 vh[RB], vl[RB];
-#pragma unroll
-        for (int u = 0; u < RB; ++u) {
-          if (k0 + u < norder) {
-            const size_t o = rowbase + (size_t)(k0 + u) * pitch + node;
-            vh[u] = *reinterpret_cast<const float4*>(hi + o);
-            vl[u] = *reinterpret_cast<const float4*>(lo + o);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < RB; ++u) {
-          if (k0 + u < norder) {
-            acc[k0 + u].fma(dv[0], df{vh[u].x, vl[u].x});
-            acc[k0 + u].fma(dv[1], df{vh[u].y, vl[u].y});
-            acc[k0 + u].fma(dv[2], df{vh[u].z, vl[u].z});
-            acc[k0 + u].fma(dv[3], df{vh[u].w, vl[u].w});
-          }
+      for (int u = 0; u < KB; ++u) {
+        if (kbase + u < norder) {
+          acc[u].fma(dv[0], df{vh[u].x, lo16_decode(vh[u].x, vl[u].x)});
+          acc[u].fma(dv[1], df{vh[u].y, lo16_decode(vh[u].y, vl[u].y)});
+          acc[u].fma(dv[2], df{vh[u].z, lo16_decode(vh[u].z, vl[u].z)});
+          acc[u].fma(dv[3], df{vh[u].w, lo16_decode(vh[u].w, vl[u].w)});
         }
       }
     }
   }
-  __shared__ df red[4][KMAX];
+  __shared__ df red[4][KB];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < KMAX; ++k) {
-    df v = acc[k].value();
+  for (int u = 0; u < KB; ++u) {
+    df v = acc[u].value();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const df w{__shfl_down_sync(0xffffffffu, v.h, o), __shfl_down_sync(0xffffffffu, v.l, o)};
       v = df_add(v, w);
     }
-    if (lane == 0) red[wid][k] = v;
+    if (lane == 0) red[wid][u] = v;
   }
   __syncthreads();
-  if (threadIdx.x < norder) {
-    const int k = threadIdx.x;
-    df v = red[0][k];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = df_add(v, red[w][k]);
+  if (threadIdx.x < KB && kbase + (int)threadIdx.x < norder) {
+    const int u = threadIdx.x, k = kbase + u;
+    df v = red[0][u];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = df_add(v, red[w][u]);
     part[((size_t)(m * norder + k) * 2 + cs) * nchunk + chunk] = df_to(v);
   }
 }
@@ -1065,17 +1101,25 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
   h->tab_f = CylTab<float>{mmax, norder, numx, numy, cmap, (float)XMIN, (float)dX, (float)YMIN, (float)dY,
                            (float)ascale, (float)hscale, (float)(1.0 / dX), (float)(1.0 / dY),
                            (float)(1.0 / ascale), (float)(1.0 / hscale)};
-  // FP32 copy of the tables (the mixed path reads it alone: half the table
-  // traffic of its field kernel) and the FP32 remainders, which with it form
-  // the double-float tables of the FP64 fused field (FP32-pipe arithmetic,
-  // same 8 bytes per entry as FP64)
+  // FP32 copy of the tables for the separate mixed path, and the tiled
+  // tables of the fused paths: FP32 roundings (the mixed path reads them
+  // alone) and 16-bit remainders, which with them form the double-float
+  // tables of the FP64 contraction and field (FP32-pipe arithmetic, 6 bytes
+  // per entry against 8 for FP64).  A field block of the tiled layout reads
+  // one contiguous region instead of hundreds of short row segments.
   h->pitch_f = (h->nnode + 3) & ~(size_t)3;
   const size_t rows = 8 * (size_t)(mmax + 1) * norder;
-  e = cudaMalloc((void**)&h->tab_f32, 2 * rows * h->pitch_f * sizeof(float));
+  const size_t nblk = (h->nnode + kTileNodes - 1) / kTileNodes;
+  h->tile_rows = 6 * (size_t)(mmax + 1) * norder;
+  const size_t ntile = nblk * h->tile_rows * kTileNodes;
+  e = cudaMalloc((void**)&h->tab_f32, rows * h->pitch_f * sizeof(float) + ntile * (sizeof(float) + sizeof(short)));
   if (e == cudaSuccess) {
-    h->tab_lo = h->tab_f32 + rows * h->pitch_f;
-    k_split_tab<<<grid_for((long long)(rows * h->pitch_f), 256, 8), 256>>>(h->tab, h->tab_f32, h->tab_lo, rows,
-                                                                           h->nnode, h->pitch_f);
+    h->tile_hi = h->tab_f32 + rows * h->pitch_f;
+    h->tile_lo = reinterpret_cast<short*>(h->tile_hi + ntile);
+    k_split_tab<<<grid_for((long long)(rows * h->pitch_f), 256, 8), 256>>>(h->tab, h->tab_f32, rows, h->nnode,
+                                                                           h->pitch_f);
+    k_tile_tab<<<grid_for((long long)ntile, 256, 8), 256>>>(h->tab, h->tile_hi, h->tile_lo, (mmax + 1) * norder,
+                                                            h->nnode, nblk);
     e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaGetLastError();
   }
@@ -1083,7 +1127,7 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
     cudaFree(h->tab);
     if (h->tab_f32) cudaFree(h->tab_f32);
     delete h;
-    return cuda_fail(e, "FP32 copy of the EOF tables");
+    return cuda_fail(e, "FP32 and tiled copies of the EOF tables");
   }
   *handle = h;
   return XT_OK;
@@ -1146,7 +1190,7 @@ int xt_cyl_accumulate(void* handle, const double* x, const double* y, const doub
     k_cyl_contract_partial<float><<<g, 256, 0, st>>>(tab_ptr_f32(h, 0), tab_ptr_f32(h, 4), D, h->mmax, h->norder,
                                                      h->nnode, h->pitch_f, kContractChunks, part);
   XT_CHECK_LAUNCH("k_cyl_contract_partial");
-  k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out);
+  k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, kContractChunks, cos_out, sin_out, 0);
   XT_CHECK_LAUNCH("k_cyl_contract_final");
   return XT_OK;
 }
@@ -1302,7 +1346,10 @@ struct BinrecArgs {
   void* rec;
   double* rout;
   int nan;
-  void* p[11];
+  double* zd;
+  float* ze;
+  long long nz;
+  void* p[14];
   void** list(bool f64) {
     int i = 0;
     if (f64) {
@@ -1312,7 +1359,7 @@ struct BinrecArgs {
       p[i++] = &Tf;
     }
     for (void* a : {(void*)&x, (void*)&y, (void*)&z, (void*)&m, (void*)&n, (void*)&hist, (void*)&rec, (void*)&rout,
-                    (void*)&nan})
+                    (void*)&nan, (void*)&zd, (void*)&ze, (void*)&nz})
       p[i++] = a;
     return p;
   }
@@ -1393,7 +1440,9 @@ static int fused_graph_launch(CylHandle* h, int precision, const double* x, cons
   } else if (G.x != x || G.y != y || G.z != z || G.m != m || G.rout != outs[5]) {
     char* ws = static_cast<char*>(workspace);
     BinrecArgs a{h->tab_d, h->tab_f, binrec_constants(h->tab_d), x, y, z, m, n,
-                 reinterpret_cast<int*>(ws + L.hist), ws + L.rec, outs[5], nan_to_origin, {}};
+                 reinterpret_cast<int*>(ws + L.hist), ws + L.rec, outs[5], nan_to_origin,
+                 reinterpret_cast<double*>(ws + L.grid), reinterpret_cast<float*>(ws + L.egrid),
+                 (long long)(h->mmax + 1) * 2 * (long long)h->pitch_f, {}};
     cudaKernelNodeParams kp = G.bp;
     kp.kernelParams = a.list(f64);
     kp.extra = nullptr;
@@ -1458,9 +1507,13 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   int* off = reinterpret_cast<int*>(ws + L.off);
   int* tsum = reinterpret_cast<int*>(ws + L.tsum);
   const int ncell = h->numx * h->numy;
+  const long long ngrid = (long long)(h->mmax + 1) * 2 * (long long)h->pitch_f;   // entries of D and of E
   auto run = [&](auto tag) -> int {
-    XT_CUDA(cudaMemsetAsync(D, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double), st));
-    XT_CUDA(cudaMemsetAsync(E, 0, (size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(float), st));
+    // the binning kernel zeroes D and E; without particles they are cleared here
+    if (n == 0) {
+      XT_CUDA(cudaMemsetAsync(D, 0, (size_t)ngrid * sizeof(double), st));
+      XT_CUDA(cudaMemsetAsync(E, 0, (size_t)ngrid * sizeof(float), st));
+    }
     XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
     using R = decltype(tag);
     constexpr bool F64 = std::is_same<R, double>::value;
@@ -1475,10 +1528,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       if constexpr (F64) {
         const BinrecDf K = binrec_constants(T);
         k_cyl_binrec_df<<<resident_grid(k_cyl_binrec_df, 256, 0, n), 256, 0, st>>>(T, K, x, y, z, m, n, hist, rec,
-                                                                                   outs[5], nan_to_origin);
+                                                                                   outs[5], nan_to_origin, D, E, ngrid);
       } else {
         k_cyl_binrec<float><<<resident_grid(k_cyl_binrec<float>, 256, 0, n), 256, 0, st>>>(
-            T, x, y, z, m, n, hist, rec, outs[5], nan_to_origin);
+            T, x, y, z, m, n, hist, rec, outs[5], nan_to_origin, D, E, ngrid);
       }
       XT_CHECK_LAUNCH("k_cyl_binrec");
       if ((rc = timing_mark(1, st))) return rc;
@@ -1520,40 +1573,37 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     }
     if ((rc = timing_mark(4, st))) return rc;
     const int nout = (h->mmax + 1) * h->norder * 2;
-    // coefficient contraction in both precisions from the double-float tables;
-    // node chunks sized for one wave of four 128-thread blocks per SM
-    const int nch = std::max(1, std::min(kContractChunksDf, 4 * sm_count() / (2 * (h->mmax + 1))));
-    dim3 g(nch, h->mmax + 1, 2);
-    if (h->norder <= 12)
-      k_cyl_contract_df<12><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
-                                              h->nnode, nch, part);
-    else if (h->norder <= 18)
-      k_cyl_contract_df<18><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
-                                              h->nnode, nch, part);
-    else
-      k_cyl_contract_df<24><<<g, 128, 0, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, D, E, h->mmax, h->norder,
-                                              h->nnode, nch, part);
+    // coefficient contraction in both precisions from the double-float tables:
+    // order groups of kContractRows, node chunks sized for one wave
+    // (3 and 6 orders per block measured alike, 9 slower: fewer resident blocks)
+    const int ngroup = (h->norder + kContractRows - 1) / kContractRows;
+    const int npair = 2 * h->mmax + 1;
+    const int cap = resident_blocks_per_sm((const void*)k_cyl_contract_df<kContractRows>, 128, 0) * sm_count();
+    const int nch = std::max(1, std::min(kContractChunksDf, cap / (ngroup * npair)));
+    k_cyl_contract_df<kContractRows><<<dim3(nch * ngroup, npair), 128, 0, st>>>(
+        h->tile_hi, h->tile_lo, h->pitch_f, D, E, h->mmax, h->norder, h->nnode, nch, ngroup, part);
     XT_CHECK_LAUNCH("k_cyl_contract_df");
-    k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out);
+    k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out, h->norder);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
     if ((rc = timing_mark(5, st))) return rc;
     // FP64 path: double-float field from the double-float tables; mixed path:
     // FP32 field from the FP32 tables (coefficients staged as df in both)
     using FT = std::conditional_t<F64, df, float>;
-    auto fld = [&](auto tq) -> int {
-      constexpr int TQ = decltype(tq)::value;   // node quads per block
-      const int fblocks = (int)((h->nnode + 4 * TQ - 1) / (4 * TQ));
+    // One block per node block of the tiled tables: 224 threads (the 672
+    // (m, field, quad) tasks of a 64-node block in three rounds, four blocks
+    // per SM), six rows in flight.  Measured on the 257^2-node, M = 6, Q = 18
+    // table: 0.059 ms against 0.067 (256 threads), 0.066 (672) and 0.072 (96).
+    {
+      constexpr int RB = 6, NT = 224, MINB = 4;
+      const int fblocks = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
       const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) +
-                        4 * TQ * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
+                        kTileNodes * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
       if (sm > 48 * 1024)
-        XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, TQ, F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      k_cyl_field2<FT, TQ, F64><<<fblocks, 256, sm, st>>>(h->tab_f32, h->tab_lo, h->pitch_f, cos_out, sin_out,
-                                                           h->mmax, h->norder, h->nnode, reinterpret_cast<FT*>(field));
-      return XT_OK;
-    };
-    // 32 quads (128 nodes) per block: 0.072 ms against 0.076 (16) and 0.094 (8)
-    // for the double-float field of the 257^2-node, M = 6, Q = 18 table
-    if ((rc = fld(std::integral_constant<int, 32>{}))) return rc;
+        XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, F64, RB, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm));
+      k_cyl_field2<FT, F64, RB, NT, MINB><<<fblocks, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_out, sin_out, h->mmax,
+                                                                   h->norder, h->nnode, reinterpret_cast<FT*>(field));
+    }
     XT_CHECK_LAUNCH("k_cyl_field2");
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {

@@ -211,6 +211,28 @@ __device__ __forceinline__ double f2d_int(float f) {
 // hi + lo as a double with one FP64 addition and no conversion instructions.
 __device__ __forceinline__ double df_to_int(df a) { return f2d_int(a.h) + f2d_int(a.l); }
 
+// Table remainders stored in 16 bits.  A double t is kept as hi = FP32
+// rounding of t and k = round((t - hi) / 2^(e-38)), e the exponent of hi:
+// |t - hi| <= 2^(e-24), so |k| <= 2^14, and hi + k 2^(e-38) equals t to
+// 2^-39 relative.  hi with a biased exponent below 39 (|hi| < 2^-88) keeps
+// k = 0, as do infinities and NaN.  The scale is built from hi's exponent
+// bits and k is converted by the 1.5 * 2^23 magic-number sum (exact for
+// |k| < 2^22), so decoding is four integer/FP32 instructions.
+constexpr int kLo16Shift = 38;
+
+__device__ __forceinline__ float lo16_decode(float hi, int k) {
+  const int b = (__float_as_int(hi) & 0x7f800000) - (kLo16Shift << 23);
+  const float kf = __fsub_rn(__int_as_float(0x4B400000 + k), 12582912.f);
+  return __fmul_rn(kf, __int_as_float(max(b, 0)));
+}
+
+__device__ __forceinline__ short lo16_encode(double t, float hi) {
+  const int hb = (__float_as_int(hi) >> 23) & 0xff;
+  if (hb < kLo16Shift + 1 || hb == 0xff) return 0;
+  const double r = t - (double)hi;                       // exact
+  return (short)llrint(ldexp(r, 127 + kLo16Shift - hb));  // r / 2^(e-38), exact scaling
+}
+
 __device__ __forceinline__ df df_split_or_from(double v) {
   bool ok;
   const df d = df_split(v, ok);
