@@ -41,18 +41,17 @@ N1 = 1_000_000
 CFG0 = dict(lmax=4, nmax=10, numr=2000, rmin=1e-3, rmax=100.0, cmap=2, scale=1.0)
 N0 = 100_000
 L2_BYTES = 129 * 1024 * 1024
-# DRAM bytes of one k_cyl_binrec<double, df> launch at the headline workload (ncu --set full)
 # DRAM bytes (read + write) of one FP64 launch of each fused stage at the headline
 # workload, from an ncu --set full capture of `bench.py --profile`, and what
 # bounds the stage there
 STAGE_TRAFFIC_F64 = {
-    "k_cyl_binrec": (32_197_120 + 2_609_408, "FP32-pipe bound (double-float set-up): FMA pipe 53 %, IPC 2.9 / SM"),
+    "k_cyl_binrec": (32_193_024 + 9_366_272, "FP32-pipe bound (double-float set-up): FMA pipe 52 %, IPC 2.9 / SM"),
     "k_cyl_scatter": (57_617_152 + 11_612_672, "scattered 16-byte record stores: LSU throttle"),
     "k_cyl_deposit_sorted": (52_213_504 + 4_608, "issue/latency bound: 128 registers, IPC 2.2 / SM, FMA pipe 35 %"),
-    "k_cyl_contract_partial+final": (135_424_000 + 2_991_616, "HBM latency: 52 % of peak, one wave"),
-    "k_cyl_field": (370_984_448 + 3_244_800, "HBM: 68 % of peak DRAM throughput"),
-    "k_cyl_eval_sorted": (89_639_168 + 35_993_088,
-                          "FP32-pipe bound (double-float arithmetic): FMA pipe 57 %, IPC 2.6 / SM"),
+    "k_cyl_contract_partial+final": (103_575_040 + 2_585_600, "HBM latency: 53 % of peak DRAM throughput"),
+    "k_cyl_field": (278_408_960 + 15_237_120, "HBM: 67 % of peak DRAM throughput, IPC 2.5 / SM"),
+    "k_cyl_eval_sorted": (89_720_832 + 35_955_200,
+                          "FP32-pipe bound (double-float arithmetic): FMA pipe 59 %, IPC 2.7 / SM"),
 }
 
 
