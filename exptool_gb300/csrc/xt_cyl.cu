@@ -907,7 +907,7 @@ __global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T,
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         dacc a;
-        a.fma(f00[b + k], w0);
+        a.set(f00[b + k], w0);
         a.fma(f10[b + k], w1);
         a.fma(f01[b + k], w2);
         a.fma(f11[b + k], w3);
@@ -921,7 +921,7 @@ __global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T,
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         dacc a;
-        a.fma(f00[k], w0);
+        a.set(f00[k], w0);
         a.fma(f10[k], w1);
         a.fma(f01[k], w2);
         a.fma(f11[k], w3);
@@ -1572,7 +1572,6 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         if ((rc = timing_mark(k, st))) return rc;
     }
     if ((rc = timing_mark(4, st))) return rc;
-    const int nout = (h->mmax + 1) * h->norder * 2;
     // coefficient contraction in both precisions from the double-float tables:
     // order groups of kContractRows, node chunks sized for one wave
     // (3 and 6 orders per block measured alike, 9 slower: fewer resident blocks)
@@ -1583,6 +1582,9 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     k_cyl_contract_df<kContractRows><<<dim3(nch * ngroup, npair), 128, 0, st>>>(
         h->tile_hi, h->tile_lo, h->pitch_f, D, E, h->mmax, h->norder, h->nnode, nch, ngroup, part);
     XT_CHECK_LAUNCH("k_cyl_contract_df");
+    // (the sum of the partials folded into the contraction's last block was
+    // measured no faster)
+    const int nout = (h->mmax + 1) * h->norder * 2;
     k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out, h->norder);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
     if ((rc = timing_mark(5, st))) return rc;

@@ -77,6 +77,14 @@ struct dacc {
     s = t;
     e = __fadd_rn(e, __fadd_rn(err, pe));
   }
+  // the same state as fma(x, y) from zero (the TwoSum with s = 0 is exact),
+  // without the TwoSum
+  __device__ __forceinline__ void set(df x, df y) {
+    s = __fmul_rn(x.h, y.h);
+    float pe = __fmaf_rn(x.h, y.h, -s);
+    pe = __fmaf_rn(x.h, y.l, pe);
+    e = __fmaf_rn(x.l, y.h, pe);
+  }
   __device__ __forceinline__ df raw() const { return {s, e}; }
   __device__ __forceinline__ df value() const { return fast_two_sum(s, e); }
 };
