@@ -475,9 +475,9 @@ __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecD
     float fx, fy;
     if (safe) {
       const df Rc = df_sqrt(df_add(s2, soft));
-      const df rho = df_sqrt(s2);
-      c1 = df_div(xd, rho);
-      s1 = df_div(yd, rho);
+      const df irho = df_rsqrt(s2);               // cos, sin phi = x, y / rho
+      c1 = df_mul(xd, irho);
+      s1 = df_mul(yd, irho);
       df xi;
       if (T.cmap == 1) {
         const df u = df_mul(Rc, ias);
@@ -650,7 +650,8 @@ struct DepF32 {
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ A acc0() { return 0.f; }
   static __device__ __forceinline__ void acc(A& a, T x, T y) { a = x * y + a; }
-  static __device__ __forceinline__ T cheb(T c1, T cur, T prev) { return 2.f * c1 * cur - prev; }
+  static __device__ __forceinline__ T twice(T c1) { return 2.f * c1; }
+  static __device__ __forceinline__ T cheb(T c2, T cur, T prev) { return c2 * cur - prev; }   // c2 = 2 cos phi
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
   static __device__ __forceinline__ void deposit(double* D, float*, size_t i, A a) { atomicAdd(D + i, (double)a); }
 };
@@ -662,8 +663,9 @@ struct DepDF {
   static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
   static __device__ __forceinline__ A acc0() { return dacc{}; }
   static __device__ __forceinline__ void acc(A& a, T x, T y) { a.fma(x, y); }
-  static __device__ __forceinline__ T cheb(T c1, T cur, T prev) {
-    return df_sub(df_scale(df_mul(c1, cur), 2.f), prev);
+  static __device__ __forceinline__ T twice(T c1) { return df_scale(c1, 2.f); }   // exact
+  static __device__ __forceinline__ T cheb(T c2, T cur, T prev) {   // c2 = 2 cos phi
+    return df_sub(df_mul(c2, cur), prev);
   }
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { df_weights(dx, dy, w); }
   // leading part into the FP64 grid (one conversion, no FP64 add), the small
@@ -767,7 +769,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
       if (!valid) continue;
       T w[4];
       M::weights(r.dx, r.dy, w);
-      const T c1 = r.c1, s1 = r.s1, base = r.base;
+      const T c1 = r.c1, s1 = r.s1, base = r.base, c2 = M::twice(c1);
       T cprev = M::one(), sprev = M::zero(), ccur = c1, scur = s1;
 #pragma unroll
       for (int m = 0; m <= MHI; ++m) {
@@ -776,8 +778,8 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
         if (m == 0) { cm = M::one(); sm = M::zero(); }
         else if (m == 1) { cm = c1; sm = s1; }
         else {
-          cm = M::cheb(c1, ccur, cprev);
-          sm = M::cheb(c1, scur, sprev);
+          cm = M::cheb(c2, ccur, cprev);
+          sm = M::cheb(c2, scur, sprev);
           cprev = ccur; sprev = scur; ccur = cm; scur = sm;
         }
         if (m < MLO) continue;
@@ -899,7 +901,7 @@ __global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T,
     df w[4];
     df_weights(r.dx, r.dy, w);
     const df w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
-    const df c1 = r.c1, s1 = r.s1;
+    const df c1 = r.c1, s1 = r.s1, c2 = df_scale(c1, 2.f);   // c2: exact
     // bilinear interpolation of the six fields of order m (lazy df sums, read
     // unnormalised by the products that follow)
     auto interp = [&](int m, df v[6]) {
@@ -937,8 +939,8 @@ __global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T,
       df cm, sm;
       if (m == 1) { cm = c1; sm = s1; }
       else {
-        cm = df_sub(df_scale(df_mul(c1, ccur), 2.f), cprev);
-        sm = df_sub(df_scale(df_mul(c1, scur), 2.f), sprev);
+        cm = df_sub(df_mul(c2, ccur), cprev);
+        sm = df_sub(df_mul(c2, scur), sprev);
         cprev = ccur; sprev = scur; ccur = cm; scur = sm;
       }
       if (m < m1 || m > m2) continue;

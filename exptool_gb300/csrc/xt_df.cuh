@@ -109,16 +109,32 @@ __device__ __forceinline__ df df_sqrt(df a) {
   return fast_two_sum(y, __fdiv_rn(r.h, __fmul_rn(2.f, y)));
 }
 
-// Quotient a / b by long division: three FP32 quotient digits, each from the
-// remainder of the previous ones (remainders formed in df); about 2^-46
-// relative for b away from zero.
+// Quotient a / b by long division: three FP32 quotient digits, each the
+// leading part of the remainder of the previous ones (remainders formed in df)
+// times one FP32 reciprocal of b's leading part.  Each digit leaves a
+// remainder ~2^-22 of the last, so three digits reach the df rounding level:
+// about 2^-46 relative for b away from zero.
 __device__ __forceinline__ df df_div(df a, df b) {
-  const float q1 = __fdiv_rn(a.h, b.h);
+  const float rb = __frcp_rn(b.h);
+  const float q1 = __fmul_rn(a.h, rb);
   df r = df_sub(a, df_mul({q1, 0.f}, b));
-  const float q2 = __fdiv_rn(r.h, b.h);
+  const float q2 = __fmul_rn(r.h, rb);
   r = df_sub(r, df_mul({q2, 0.f}, b));
-  const float q3 = __fdiv_rn(r.h, b.h);
+  const float q3 = __fmul_rn(r.h, rb);
   return df_add(fast_two_sum(q1, q2), {q3, 0.f});
+}
+
+// 1 / sqrt(a) for a > 0: z = the correctly rounded FP32 value, then one
+// Newton step z + z (1 - a z^2) / 2 with a z^2 formed in df (z^2 exactly by
+// TwoProd); 1 - a z^2 is ~2^-24, so its FP32 value suffices.  About 2^-46
+// relative.
+__device__ __forceinline__ df df_rsqrt(df a) {
+  const float z = __frsqrt_rn(a.h);
+  const float p = __fmul_rn(z, z);
+  const float e = __fmaf_rn(z, z, -p);            // z*z = p + e exactly
+  const df az2 = df_mul(a, {p, e});
+  const float d = __fsub_rn(__fsub_rn(1.f, az2.h), az2.l);
+  return fast_two_sum(z, __fmul_rn(__fmul_rn(z, d), 0.5f));
 }
 
 __device__ __forceinline__ df df_abs(df a) { return a.h < 0.f ? df_neg(a) : a; }
