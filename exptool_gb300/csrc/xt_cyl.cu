@@ -687,18 +687,19 @@ constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
 // divergent per-lane flush would occupy the FP64 unit for a full warp
 // instruction per value however few lanes are active.)  Loops are
 // warp-uniform so that the ballots see every lane.  With NPASS = 2 a run is
-// deposited in two passes over its records, orders m <= MCAP/2 and then the
-// rest, so that half the sums are live at a time (double-float sums: 104 ->
-// 56 registers of accumulators, for more resident warps; the second pass
-// re-reads the run's records from L1).
+// deposited in two passes over its records, the cosine sums (m = 0..MCAP)
+// and then the sine sums (m = 1..MCAP), so that half the sums are live at a
+// time (double-float sums: 104 -> 56 registers of accumulators, for more
+// resident warps) and each pass runs only its own Chebyshev recurrence; the
+// second pass re-reads the run's records from L1.
 template <typename M, int MCAP, int NPASS>
 __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
     k_cyl_deposit_sorted(int numy, int mmax, long long n, int run, const BinRec<typename M::T>* __restrict__ srec,
                          double* __restrict__ D, float* __restrict__ E, size_t plane) {
   using T = typename M::T;
   using A = typename M::A;
-  constexpr int MH = NPASS == 2 ? MCAP / 2 : MCAP;      // last order of the first pass
-  constexpr int NJ0 = 2 * MH + 1, NJ1 = 2 * (MCAP - MH);
+  // sums per pass: all 2 MCAP + 1 in one pass, else the cosines then the sines
+  constexpr int NJ0 = NPASS == 2 ? MCAP + 1 : 2 * MCAP + 1, NJ1 = MCAP;
   constexpr int NEMAX = 4 * (NJ0 > NJ1 ? NJ0 : NJ1);
   constexpr int PITCH = NEMAX + 1;              // conflict-free parking of up to 8 lanes
   __shared__ A park[4][kDepSlots][PITCH];
@@ -710,9 +711,11 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
 
   auto run_pass = [&](long long q0, auto pass_tag) {
     constexpr int PASS = decltype(pass_tag)::value;
-    constexpr int MLO = PASS == 0 ? 0 : MH + 1, MHI = PASS == 0 ? MH : MCAP;
-    constexpr int J0 = PASS == 0 ? 0 : 2 * MH + 1;
+    constexpr bool COS = NPASS == 1 || PASS == 0, SIN = NPASS == 1 || PASS == 1;
     constexpr int NJP = PASS == 0 ? NJ0 : NJ1;
+    // global sum index j (0: m = 0 cosine; 2m - 1: cosine m; 2m: sine m) of
+    // this pass's local index jl
+    auto gj = [](int jl) { return NPASS == 1 ? jl : (PASS == 0 ? (jl ? 2 * jl - 1 : 0) : 2 * (jl + 1)); };
     constexpr int NE = 4 * NJP;
     A acc[NJP][4];
 #pragma unroll
@@ -744,7 +747,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
         __syncwarp();
         for (int i = lane; i < nb * NE; i += 32) {
           const int sidx = i / NE, e = i - sidx * NE;
-          const int j = J0 + (e >> 2), k = e & 3;
+          const int j = gj(e >> 2), k = e & 3;
           if (j < nju) {
             const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
             const int m = (j + 1) >> 1;        // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
@@ -772,25 +775,28 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
       const T c1 = r.c1, s1 = r.s1, base = r.base, c2 = M::twice(c1);
       T cprev = M::one(), sprev = M::zero(), ccur = c1, scur = s1;
 #pragma unroll
-      for (int m = 0; m <= MHI; ++m) {
+      for (int m = 0; m <= MCAP; ++m) {
         if (m > mmax) break;
         T cm, sm;
         if (m == 0) { cm = M::one(); sm = M::zero(); }
         else if (m == 1) { cm = c1; sm = s1; }
         else {
-          cm = M::cheb(c2, ccur, cprev);
-          sm = M::cheb(c2, scur, sprev);
-          cprev = ccur; sprev = scur; ccur = cm; scur = sm;
+          if constexpr (COS) { cm = M::cheb(c2, ccur, cprev); cprev = ccur; ccur = cm; }
+          if constexpr (SIN) { sm = M::cheb(c2, scur, sprev); sprev = scur; scur = sm; }
         }
-        if (m < MLO) continue;
-        const T wc = M::mul(base, cm);
-        const int jc = ((m == 0) ? 0 : 2 * m - 1) - J0;
+        if constexpr (COS) {
+          const T wc = M::mul(base, cm);
+          const int jc = NPASS == 1 ? ((m == 0) ? 0 : 2 * m - 1) : m;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) M::acc(acc[jc][k], wc, w[k]);
-        if (m > 0) {
-          const T ws = M::mul(base, sm);
+          for (int k = 0; k < 4; ++k) M::acc(acc[jc][k], wc, w[k]);
+        }
+        if constexpr (SIN) {
+          if (m > 0) {
+            const T ws = M::mul(base, sm);
+            const int js = NPASS == 1 ? 2 * m : m - 1;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) M::acc(acc[2 * m - J0][k], ws, w[k]);
+            for (int k = 0; k < 4; ++k) M::acc(acc[js][k], ws, w[k]);
+          }
         }
       }
     }
@@ -802,7 +808,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
     const long long q0 = (r0 + lane) * run;
     run_pass(q0, std::integral_constant<int, 0>{});
     if constexpr (NPASS == 2) {
-      if (mmax > MH) run_pass(q0, std::integral_constant<int, 1>{});
+      if (mmax > 0) run_pass(q0, std::integral_constant<int, 1>{});
     }
   }
 }
