@@ -654,6 +654,7 @@ struct DepF32 {
   static __device__ __forceinline__ T cheb(T c2, T cur, T prev) { return c2 * cur - prev; }   // c2 = 2 cos phi
   static __device__ __forceinline__ void weights(T dx, T dy, T w[4]) { weights_from_frac(dx, dy, w); }
   static __device__ __forceinline__ void deposit(double* D, float*, size_t i, A a) { atomicAdd(D + i, (double)a); }
+  static __device__ __forceinline__ A merge(A a, A b) { return a + b; }
 };
 struct DepDF {
   using T = df;
@@ -674,6 +675,16 @@ struct DepDF {
   static __device__ __forceinline__ void deposit(double* D, float* E, size_t i, A a) {
     atomicAdd(D + i, (double)a.s);
     if (a.e != 0.f) atomicAdd(E + i, a.e);
+  }
+  // sum of two lazy sums: TwoSum of the leading parts, error parts added
+  static __device__ __forceinline__ A merge(A a, A b) {
+    const float t = __fadd_rn(a.s, b.s);
+    const float v = __fsub_rn(t, a.s);
+    const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, v)), __fsub_rn(b.s, v));
+    A r;
+    r.s = t;
+    r.e = __fadd_rn(__fadd_rn(a.e, b.e), err);
+    return r;
   }
 };
 
@@ -745,14 +756,29 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
             }
         }
         __syncwarp();
-        for (int i = lane; i < nb * NE; i += 32) {
-          const int sidx = i / NE, e = i - sidx * NE;
+        // one lane per sum entry e across the batch's slots; slots of the same
+        // cell (adjacent, as the runs are in cell order) are added before
+        // their atomics
+        for (int e = lane; e < NE; e += 32) {
           const int j = gj(e >> 2), k = e & 3;
           if (j < nju) {
-            const size_t node = (size_t)park_node[wib][sidx] + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
             const int m = (j + 1) >> 1;        // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
             const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
-            M::deposit(D, E, (size_t)(2 * m + cs) * plane + node, park[wib][sidx][e]);
+            const size_t off = (size_t)(2 * m + cs) * plane + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
+            int nd = park_node[wib][0];
+            A a = park[wib][0][e];
+            for (int sidx = 1; sidx < nb; ++sidx) {
+              const int nd2 = park_node[wib][sidx];
+              const A b = park[wib][sidx][e];
+              if (nd2 == nd) {
+                a = M::merge(a, b);
+              } else {
+                M::deposit(D, E, off + nd, a);
+                nd = nd2;
+                a = b;
+              }
+            }
+            M::deposit(D, E, off + nd, a);
           }
         }
         __syncwarp();
