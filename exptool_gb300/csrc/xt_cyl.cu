@@ -688,7 +688,11 @@ struct DepDF {
   }
 };
 
-constexpr int kDepSlots = 8;   // lanes parked per cooperative flush batch
+// Lanes parked per cooperative flush batch: the whole warp, so that every
+// same-cell run of a warp is added up before its atomics (measured on 1e6
+// disc particles: FP64 deposit 0.110 / 0.103 / 0.100 ms with 8 / 16 / 32 slots,
+// FP32 0.053 / 0.048 / 0.045 ms).
+constexpr int kDepSlots = 32;
 
 // Deposit of sorted records.  Each lane takes `run` consecutive particles and
 // sums their contributions per (m, cos/sin, corner) in registers while the
