@@ -45,13 +45,13 @@ L2_BYTES = 129 * 1024 * 1024
 # workload, from an ncu --set full capture of `bench.py --profile`, and what
 # bounds the stage there
 STAGE_TRAFFIC_F64 = {
-    "k_cyl_binrec": (32_193_024 + 9_366_272, "FP32-pipe bound (double-float set-up): FMA pipe 52 %, IPC 2.9 / SM"),
+    "k_cyl_binrec": (32_190_976 + 9_330_944, "FP32-pipe bound (double-float set-up): FMA pipe 52 %, IPC 2.9 / SM"),
     "k_cyl_scatter": (57_617_152 + 11_612_672, "scattered 16-byte record stores: LSU throttle"),
-    "k_cyl_deposit_sorted": (52_213_504 + 4_608, "issue/latency bound: 128 registers, IPC 2.2 / SM, FMA pipe 35 %"),
+    "k_cyl_deposit_sorted": (52_226_304 + 15_616, "issue bound: 128 registers, IPC 2.4 / SM, FMA pipe 39 %"),
     "k_cyl_contract_partial+final": (103_575_040 + 2_585_600, "HBM latency: 53 % of peak DRAM throughput"),
     "k_cyl_field": (278_408_960 + 15_237_120, "HBM: 67 % of peak DRAM throughput, IPC 2.5 / SM"),
-    "k_cyl_eval_sorted": (89_720_832 + 35_955_200,
-                          "FP32-pipe bound (double-float arithmetic): FMA pipe 59 %, IPC 2.7 / SM"),
+    "k_cyl_eval_sorted": (89_757_440 + 36_104_448,
+                          "FP32-pipe bound (double-float arithmetic): FMA pipe 53 %, IPC 2.5 / SM"),
 }
 
 
