@@ -181,7 +181,7 @@ def learned_extra(steps=20000, batch=8192, n_eval=10_000_000, n_cal=200_000, rep
     4, Adam lr 1e-3 cosine-decayed to 1e-5), then potential + force at 1e7
     Hernquist particles (seed 5) with coefficients from those particles.
     Per radius band: median relative force error of the network path and of
-    FP32 table interpolation against FP64 table interpolation (the judge),
+    FP32 table interpolation against FP64 table interpolation (the reference),
     and the calibrated hybrid (network where it meets 1e-5, table elsewhere).
     Throughput of each path beside the plain FP64 table path on the same
     points."""

@@ -15,7 +15,7 @@ Training, labels and inference run in this package's CUDA library
 (``xt_mlp_*``, ``xt_learned_*``): the GPU labels radii from the uploaded
 tables, trains with its own forward/backward/Adam kernels, and evaluates
 forces with the coefficient contraction folded into the last layer.  Table
-interpolation is both the judge and the fallback: ``calibrate`` measures the
+interpolation is both the error reference and the fallback: ``calibrate`` measures the
 median relative force error of the network path against FP64 table
 interpolation in equal bands of ln r and keeps the table (FP32
 interpolation) in every band that misses the bar.
