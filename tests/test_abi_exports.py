@@ -46,3 +46,21 @@ def test_argument_errors_without_gpu():
     assert rc == -1
     assert lib.xt_sph_accumulate_workspace(None) == 0
     assert lib.xt_cyl_field_bytes(None, 0, 0) == 0
+
+
+def test_copy_list_arguments_without_gpu():
+    """xt_copy_async checks its copy list before any CUDA call: an empty list
+    and zero-byte entries are no-ops, missing arrays and null addresses are
+    argument errors."""
+    lib = _lib.load()
+    assert lib.xt_copy_async(0, None, None, None, None) == 0
+    assert lib.xt_copy_async(-1, None, None, None, None) == -1
+    assert lib.xt_copy_async(2, None, None, None, None) == -1
+    assert b"NULL copy list" in lib.xt_last_error()
+    dst = (ctypes.c_void_p * 2)(None, None)
+    src = (ctypes.c_void_p * 2)(None, None)
+    nb = (ctypes.c_size_t * 2)(0, 0)
+    assert lib.xt_copy_async(2, dst, src, nb, None) == 0          # zero bytes: skipped
+    nb[1] = 8
+    assert lib.xt_copy_async(2, dst, src, nb, None) == -1
+    assert b"copy 1" in lib.xt_last_error()
