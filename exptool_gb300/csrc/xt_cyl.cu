@@ -1585,9 +1585,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       XT_CHECK_LAUNCH("k_cyl_scatter");
       if ((rc = timing_mark(3, st))) return rc;
       // Run length: particles summed in registers per lane before the atomics.
-      // Measured on 1e6 disc particles (runs of 4 to 16, one resident wave or
-      // one block per 128 runs): 8 for the double-float sums and 6 for FP32,
-      // one block per 128 runs (the hardware fills later waves as blocks end).
+      // Measured on 1e6 disc particles with same-cell lanes merged before the
+      // atomics (runs of 4 to 16): 4 in both precisions (FP64 deposit 0.096 ms
+      // against 0.100 at 8 and 0.126 at 16), one block per 128 runs (the
+      // hardware fills later waves as blocks end).
       auto dep = [&](auto mc) {
         constexpr int MC = decltype(mc)::value;
         using Mth = std::conditional_t<F64, DepDF, DepF32>;
@@ -1595,7 +1596,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
         // (one pass with 2-3 blocks per SM, or two passes with 2-3, measured
         // 0.127-0.131 ms against 0.121 ms for two passes at 4 blocks per SM)
         auto kern = k_cyl_deposit_sorted<Mth, MC, NP>;
-        const int run = F64 ? 8 : 6;
+        const int run = 4;
         const long long nrun = (n + run - 1) / run;
         const int grid = (int)std::min<long long>((nrun + 127) / 128, 8LL * resident_grid(kern, 128, 0, nrun));
         kern<<<grid, 128, 0, st>>>(h->numy, h->mmax, n, run, srec, D, E, h->pitch_f);
