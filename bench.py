@@ -161,9 +161,11 @@ def batched_extra(K=5):
         a, b = out[i].cpu().numpy(), ref.cpu().numpy()
         errs.append((float(np.max(np.abs(a - b)) / np.max(np.abs(b))), _block_err(a, b, table.lmax)))
     errs = np.array(errs)
+    tc = batched_tc_extra(table, xyzm, offs, K, fp64_ms=f64_ms)
     return {"workload": "256 Hernquist snapshots (counts log-uniform in [1e4,4e6), total %d), SL lmax=6 nmax=20 "
                         "numr=2000, one persistent launch (FP32 per particle + shared-memory grids, FP64 "
                         "cross-item sums and contraction)" % ntot,
+            "tensor_core": tc,
             "ms": ms, "particles_per_s": ntot / (ms * 1e-3), "autotuned": cfg,
             "autotune_candidates_ms": {k: round(v, 3) for k, v in tune_ms.items()},
             "fp64_per_snapshot_ms": f64_ms, "fp64_particles_per_s": ntot / (f64_ms * 1e-3),
@@ -173,6 +175,46 @@ def batched_extra(K=5):
                 "per_l_block_median": float(np.median(errs[:, 1])), "per_l_block_max": float(np.max(errs[:, 1])),
                 "metric": "normwise: max|dc|/max|c| over all rows; per_l_block: max over l of the same within "
                           "each l block"}}
+
+
+def batched_tc_extra(table, xyzm, offs, K=5, fp64_ms=None, refs=None):
+    """The same 256 snapshots through the tensor-core engine: counting sort by
+    (snapshot, radial window), tcgen05 BF16 products with FP32 accumulation,
+    FP64 window sums and contraction.  Work-item size and stages autotuned;
+    per-snapshot error against the FP64 path on the same FP32 particles."""
+    import torch
+    from exptool_gb300 import autotune as at, device as dev
+    ntot = int(offs[-1])
+    cfg, tune_ms = at.sph_batched_tc_config(table, xyzm, offs)
+    ws = torch.empty(table.batched_tc_workspace(offs, cfg["chunk"]), dtype=torch.uint8, device="cuda")
+    out = table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws)
+    e1.record()
+    torch.cuda.synchronize()
+    dev.batched_tc_status()
+    ms = e0.elapsed_time(e1) / K
+    sws = torch.empty(table._lib.xt_sph_accumulate_workspace(table.handle), dtype=torch.uint8, device="cuda")
+    errs = []
+    for i in range(len(offs) - 1):
+        blk = xyzm[int(offs[i]):int(offs[i + 1])].double()
+        ref = table.accumulate(*(blk[:, k].contiguous() for k in range(4)), workspace=sws)
+        a, b = out[i].cpu().numpy(), ref.cpu().numpy()
+        errs.append((float(np.max(np.abs(a - b)) / np.max(np.abs(b))), _block_err(a, b, table.lmax)))
+    errs = np.array(errs)
+    res = {"ms": ms, "particles_per_s": ntot / (ms * 1e-3), "autotuned": cfg,
+           "autotune_candidates_ms": {k: round(v, 3) for k, v in tune_ms.items()},
+           "tile": "M = 128 radial nodes, N = 64 (49 rows), K = 128 particles per stage, BF16 in, FP32 in TMEM",
+           "tensor_flop_per_particle": 2 * 128 * 64,
+           "err_vs_fp64_per_snapshot": {
+               "normwise_median": float(np.median(errs[:, 0])), "normwise_max": float(np.max(errs[:, 0])),
+               "per_l_block_median": float(np.median(errs[:, 1])), "per_l_block_max": float(np.max(errs[:, 1]))}}
+    if fp64_ms:
+        res["speedup_vs_fp64"] = fp64_ms / ms
+    return res
 
 
 def learned_extra(steps=20000, batch=8192, n_eval=10_000_000, n_cal=200_000, reps=5):
@@ -432,6 +474,28 @@ def gpu_arm(args, rank, world):
             dist.barrier()
         return max_over_ranks(tot, world)
 
+    def sorted_step(prec):
+        coef = table.accumulate_sorted(xd, yd, zd, md, precision=prec)
+        return table.eval_sorted(xd, yd, zd, coef[0], coef[1], precision=prec)
+
+    def timed_sorted(prec, steps, warmup):
+        """The drop-in calls eof.compute_coefficients + eof.compute_forces as
+        they run on device arrays: accumulation and evaluation through the
+        sorted pipeline, one call each."""
+        for _ in range(warmup):
+            sorted_step(prec)
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sorted_step(prec)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot
+
     def timed(prec, steps, warmup, phases=False):
         for _ in range(warmup):
             step(prec)
@@ -472,6 +536,8 @@ def gpu_arm(args, rank, world):
     clocks = clk.summary()
     tot64, ph64 = timed("f64", K, W)
     tot32, ph32 = timed("f32", K, W)
+    stot64 = timed_sorted("f64", K, W)
+    stot32 = timed_sorted("f32", K, W)
     ftot32 = timed_fused("f32", K, W)
     ms64 = ftot64 / K
     value = world * N1 / (ms64 * 1e-3)
@@ -500,7 +566,9 @@ def gpu_arm(args, rank, world):
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = float(np.median(e2e_times))
     sep_times = []
-    for _ in range(3):
+    E = eof.compute_coefficients(P, path, verbose=0)
+    eof.compute_forces(P, E, verbose=0)
+    for _ in range(max(3, min(K, 10))):
         t0 = time.perf_counter()
         E = eof.compute_coefficients(P, path, verbose=0)
         eof.compute_forces(P, E, verbose=0)
@@ -607,7 +675,15 @@ def gpu_arm(args, rank, world):
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg64[dom],
                      "launch_ms": round(float(stages64[dom]), 4)},
         "fused_stages": fused_stages,
-        "separate_calls_f64": {"ms_per_step": tot64 / K, "value": world * N1 / (tot64 / K * 1e-3), "phases": phases},
+        "separate_calls_f64": {"ms_per_step": stot64 / K, "value": world * N1 / (stot64 / K * 1e-3),
+                               "what": "the drop-in eof.compute_coefficients + eof.compute_forces on device arrays: "
+                                       "xt_cyl_accumulate_sorted + xt_cyl_eval_sorted",
+                               "f32_ms_per_step": stot32 / K},
+        "particle_order_calls_f64": {"ms_per_step": tot64 / K, "value": world * N1 / (tot64 / K * 1e-3),
+                                     "what": "particle-order kernels (xt_cyl_accumulate, xt_cyl_prepare, "
+                                             "xt_cyl_eval_points), used for tables outside the sorted path's limits "
+                                             "and for density",
+                                     "phases": phases},
         "mixed_f32": {"value": world * N1 / (ftot32 / K * 1e-3), "ms_per_step": ftot32 / K,
                       "separate_calls_ms_per_step": tot32 / K,
                       "phases_ms": [round(float(v), 4) for v in ph32], "coef_rel_err_vs_f64": coef_err,
@@ -963,6 +1039,92 @@ def profile_learned(args):
     return 0
 
 
+def profile_case(args):
+    """Short, fixed launch sequences of one workload each for ncu captures
+    (warm-up calls, then the profiled ones):
+    spherical   config 0 (halo lmax 4, N = 1e5): FP64 accumulation (k_sph_deposit,
+                k_sph_contract) and evaluation (k_sph_eval<double, 4>); then the
+                lmax 6 / nmax 20 FP64 table evaluation of 1e6 points
+                (k_sph_eval<double, 6>, the plain path the learned basis is
+                compared with);
+    orbits      65536 disc orbits in the halo + disc field, 100 steps in one
+                launch (k_leapfrog), FP32 then FP64 forces;
+    reader      a 1e6-particle PSP snapshot (double precision) read into device
+                columns (k_records_to_columns);
+    batched_tc  the first 16 batched snapshots through the tensor-core engine
+                (k_bt_*, k_sph_batched_tc, k_bt_reduce);
+    eof_tables  a GPU EOF build (mmax 2, norder 6, 64^2 grid, lmax 16; k_eof_basis)."""
+    import tempfile
+    import torch
+    from exptool_gb300 import _lib, device as dev
+    from exptool_gb300.basis import eof, potential, spheresl
+    case = args.profile_case
+    reps = args.warmup + 1
+    if case == "spherical":
+        cache, model = sl_table_paths()
+        st = spheresl.table_from_files(cache, model)
+        hx, hy, hz, hm = (dev.to_dev(a) for a in halo_particles())
+        for _ in range(reps):
+            ec = st.accumulate(hx, hy, hz, hm)
+            f = st.prepare(ec)
+            st.eval_points(f, hx, hy, hz, _lib.XT_SPH_ALL_EVAL_PARTICLES, _lib.XT_COORD_CART)
+        c6, m6 = sl6_table_paths()
+        t6 = spheresl.table_from_files(c6, m6)
+        from exptool_gb300.tables.samplers import hernquist_sample
+        px, py, pz, pm = (dev.to_dev(a) for a in hernquist_sample(1_000_000, seed=5))
+        e6 = t6.accumulate(px, py, pz, pm)
+        f6 = t6.prepare(e6)
+        for _ in range(reps):
+            t6.eval_points(f6, px, py, pz, _lib.XT_SPH_ALL_EVAL, _lib.XT_COORD_CART)
+    elif case == "orbits":
+        from exptool_gb300.tables.samplers import disc_sample
+        from exptool_gb300.utils import integrate
+        path = eof_table_path()
+        cache, model = sl_table_paths()
+        table = eof.table_from_file(path)
+        x, y, z, m = disc_particles()
+        c, s_ = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)))
+        st = spheresl.table_from_files(cache, model)
+        F = potential.Fields("synthetic", path, cache, model, verbose=0, halo_correct_m=True)
+        F.EOF = eof.EOF_Object()
+        F.EOF.eof_file, F.EOF.cos, F.EOF.sin = path, c.cpu().numpy(), s_.cpu().numpy()
+        F.SL = spheresl.SL_Object()
+        F.SL.sph_file, F.SL.model_file = cache, model
+        F.SL.expcoef = st.accumulate(*(dev.to_dev(a) for a in halo_particles())).cpu().numpy()
+        F.prep_tables()
+        ox, oy, oz, _ = disc_sample(65536, 2)
+        pos = np.stack([ox, oy, oz], axis=1)
+        R = np.hypot(ox, oy)
+        vel = np.stack([-oy / R * 0.6, ox / R * 0.6, np.zeros_like(R)], axis=1)
+        for prec in ["f32"] * args.warmup + ["f32", "f64"]:
+            integrate.Ensemble(F, pos, vel, 100, 0.002, precision=prec, chunk=100).run(graph=False)
+    elif case == "reader":
+        from exptool_gb300.io import psp_io, snapshot
+        x, y, z, m = disc_particles()
+        d = tempfile.mkdtemp()
+        path = os.path.join(d, "OUT.prof.00000")
+        comp = {"m": m, "x": x, "y": y, "z": z, "vx": x, "vy": y, "vz": z, "potE": m}
+        snapshot.write_psp(path, 0.0, {"star": comp}, float_len=8)
+        for _ in range(reps):
+            psp_io.Input(path, comp="star", device=True)
+    elif case == "batched_tc":
+        c6, m6 = sl6_table_paths()
+        t6 = spheresl.table_from_files(c6, m6)
+        xyzm, offs = batched_snapshots(16)
+        for _ in range(reps):
+            t6.accumulate_batched_tc(xyzm, offs, chunk=16384, stages=2)
+        dev.batched_tc_status()
+    elif case == "eof_tables":
+        from exptool_gb300.tables.eof_builder import EOFTables
+        for _ in range(reps):
+            EOFTables(mmax=2, norder=6, numx=64, numy=64, lmax_sph=16, nmax_sph=10, nsample=50000, engine="gpu")
+    else:
+        raise SystemExit(f"unknown profile case {case!r}")
+    torch.cuda.synchronize()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -978,7 +1140,12 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
                          "(a short, fixed launch sequence for ncu captures)")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["spherical", "orbits", "reader", "batched_tc", "eof_tables"],
+                    help="a short launch sequence of one workload for ncu captures (see profile_case)")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args)
     if args.profile:
         return profile_run(args)
     if args.profile_batched:

@@ -60,6 +60,9 @@ _SIGS = {
                                    c_int, c_int, c_dpp, c_vp]),
     "xt_sph_batched_workspace": (c_sz, [c_vp, c_int, c_ll, c_int]),
     "xt_sph_accumulate_batched": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_sph_batched_tc_workspace": (c_sz, [c_vp, c_int, c_vp, c_int]),
+    "xt_sph_accumulate_batched_tc": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_sz, c_vp]),
+    "xt_sph_batched_tc_status": (c_int, []),
     "xt_cyl_table_create": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl,
                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.POINTER(c_vp)]),
     "xt_cyl_table_destroy": (c_int, [c_vp]),
@@ -72,6 +75,10 @@ _SIGS = {
     "xt_cyl_accumulate_eval_workspace": (c_sz, [c_vp, c_ll, c_int]),
     "xt_cyl_accumulate_eval": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int, c_int, c_vp, c_vp,
                                        c_dpp, c_vp, c_sz, c_vp]),
+    "xt_cyl_accumulate_sorted": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_vp, c_vp, c_vp, c_sz,
+                                         c_vp]),
+    "xt_cyl_eval_sorted": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_int, c_int, c_int, c_vp, c_vp, c_dpp, c_vp, c_sz,
+                                   c_vp]),
     "xt_timing_enable": (c_int, [c_int]),
     "xt_timing_read": (c_int, [c_dp, c_int]),
     "xt_fields_forces": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp,
@@ -95,6 +102,8 @@ _SIGS = {
     "xt_learned_radial_pass": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_dbl, c_vp, c_int, c_vp, c_ll, c_int,
                                        c_vp, c_vp]),
     "xt_learned_status": (c_int, []),
+    "xt_eof_basis": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl,
+                             c_ll, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "xt_records_to_columns": (c_int, [c_vp, c_ll, c_int, c_int, c_vp, c_vp, c_dpp, c_vp]),
 }
 

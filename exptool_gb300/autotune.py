@@ -98,3 +98,29 @@ def sph_batched_config(table, xyzm, offsets, force=False, sample_snaps=32):
     cands = [{"chunk": c, "threads": t} for c in (32768, 65536, 131072, 262144) for t in (256, 512, 768, 1024)]
     return tune(k, cands, lambda cfg: table.accumulate_batched(sub, sub_offs, chunk=cfg["chunk"],
                                                                threads=cfg["threads"]), force=force)
+
+
+def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
+    """Work-item size (particles) and operand stages of
+    xt_sph_accumulate_batched_tc for this table, tuned on (up to) the first
+    ``sample_snaps`` snapshots of the batch.  The tile shape itself is fixed
+    by the table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16,
+    K = 128 particles per stage; stages = 2 lets two CTAs share an SM, 3
+    keeps one with a deeper pipeline."""
+    import numpy as np
+    offs = np.asarray(offsets, dtype=np.int64)
+    ns = min(len(offs) - 1, sample_snaps)
+    sub_offs = offs[:ns + 1]
+    sub = xyzm[:int(sub_offs[-1])]
+    k = key("sph_batched_tc_v1", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
+    cands = [{"chunk": c, "stages": st} for c in (4096, 8192, 16384, 32768, 65536) for st in (2, 3)]
+    ws = {}
+
+    def run(cfg):
+        need = table.batched_tc_workspace(sub_offs, cfg["chunk"])
+        if ws.get("n", 0) < need:
+            ws["t"] = torch.empty(need, dtype=torch.uint8, device=xyzm.device)
+            ws["n"] = need
+        table.accumulate_batched_tc(sub, sub_offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws["t"])
+
+    return tune(k, cands, run, force=force)

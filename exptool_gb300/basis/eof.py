@@ -168,9 +168,23 @@ def accumulate(ParticleInstance, potC, potS, MMAX, NMAX, XMIN, dX, YMIN, dY, NUM
     pC = np.asarray(potC)[:MMAX + 1, :NMAX]
     pS = np.asarray(potS)[:MMAX + 1, :NMAX]
     table = table_from_arrays(MMAX, NMAX, NUMX, NUMY, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, pC, potS=pS)
-    x, y, z, m = (dev.to_dev(a) for a in positions(ParticleInstance))
-    c, s = table.accumulate(x, y, z, m, precision=precision)
+    c, s = _accumulate_dev(table, positions(ParticleInstance, allow_device=True), precision, nan_to_origin=False)
     return dev.to_host(c), dev.to_host(s)
+
+
+def _accumulate_dev(table, xyzm, precision, nan_to_origin):
+    """(cos, sin) device tensors: the sorted pipeline where the table fits it
+    (particle arrays in page-locked host memory are read in place), else the
+    particle-order deposit."""
+    if table.sorted_ok():
+        coef = table.accumulate_sorted(*(dev.kernel_input(a) for a in xyzm), precision=precision,
+                                       nan_to_origin=nan_to_origin)
+        return coef[0], coef[1]
+    x, y, z, m = (dev.to_dev(a) for a in xyzm)
+    if nan_to_origin:
+        bad = torch.isnan(x) | torch.isnan(y) | torch.isnan(z)
+        x, y, z = (torch.where(bad, torch.zeros_like(a), a) for a in (x, y, z))
+    return table.accumulate(x, y, z, m, precision=precision)
 
 
 def make_coefficients_multi(ParticleInstance, nprocs, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy,
@@ -187,14 +201,9 @@ def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max
     .cos/.sin of shape (mmax+1, norder)."""
     if VAR:
         raise NotImplementedError("VAR jackknife partitions are not part of the GPU path")
-    x, y, z, m = positions(PSPInput)
-    bad = np.isnan(x) | np.isnan(y) | np.isnan(z)
-    if np.any(bad):
-        if verbose:
-            print("eof.compute_coefficients: NaN values found in output file {}.".format(
-                getattr(PSPInput, "filename", "")))
-        if not nanblock:
-            x, y, z = (np.where(bad, 0.0, a) for a in (x, y, z))
+    x, y, z, m = positions(PSPInput, allow_device=True)
+    if verbose and not isinstance(x, torch.Tensor) and np.isnan(np.sum(x) + np.sum(y) + np.sum(z)):
+        print("eof.compute_coefficients: NaN values found in output file {}.".format(getattr(PSPInput, "filename", "")))
     table = table_from_file(eof_file)
     out = EOF_Object()
     out.time = getattr(PSPInput, "time", None)
@@ -204,7 +213,9 @@ def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max
     out.eof_file = eof_file
     out.mmax = table.mmax
     out.nmax = table.norder
-    c, s = table.accumulate(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision)
+    # particles with a NaN coordinate are placed at the origin on the device
+    # (eof.py:1189-1204) unless nanblock
+    c, s = _accumulate_dev(table, (x, y, z, m), precision, nan_to_origin=not nanblock)
     out.cos = dev.to_host(c)
     out.sin = dev.to_host(s)
     return out
@@ -274,11 +285,29 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
             print("eof.accumulated_eval_particles: cannot compute density (functions not specified). moving on "
                   "without...")
         density = False
-    field = field_for(table, accum_cos, accum_sin, density=density, precision=precision)
     d = Particles.data
+    zsrc = Particles.zpos if hasattr(Particles, "zpos") and Particles.zpos is not None else d["z"]
+    if not density and table.sorted_ok():
+        # binning, counting sort by table cell, field and evaluation in cell
+        # order; particle arrays in page-locked host memory are read in place
+        c = dev.to_dev(np.asarray(accum_cos, dtype=np.float64) if not isinstance(accum_cos, torch.Tensor)
+                       else accum_cos)
+        s = dev.to_dev(np.asarray(accum_sin, dtype=np.float64) if not isinstance(accum_sin, torch.Tensor)
+                       else accum_sin)
+        c, s = dev.pad2(c, table.mmax + 1, table.norder), dev.pad2(s, table.mmax + 1, table.norder)
+        n = int(np.asarray(d["x"]).size) if not isinstance(d["x"], torch.Tensor) else int(d["x"].numel())
+        # one page-locked block for the results: R written into it by the
+        # binning kernel, p0 p fr fp fz copied in with one wait
+        blk = torch.empty(6 * n, dtype=torch.float64, pin_memory=True)
+        res = table.eval_sorted(*(dev.kernel_input(a) for a in (d["x"], d["y"], zsrc)), c, s, precision=precision,
+                                m1=m1, m2=m2, r_out=blk.data_ptr() + 40 * n)
+        dev.copy_and_sync([(blk.data_ptr(), res.data_ptr(), 40 * n)])
+        h = blk.numpy()
+        return tuple(h[k * n:(k + 1) * n] for k in range(6))
+    field = field_for(table, accum_cos, accum_sin, density=density, precision=precision)
     x = dev.to_dev(d["x"])
     y = dev.to_dev(d["y"])
-    z = dev.to_dev(Particles.zpos if hasattr(Particles, "zpos") and Particles.zpos is not None else d["z"])
+    z = dev.to_dev(zsrc)
     outs = table.eval_points(field, x, y, z, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, m1=m1, m2=m2,
                              want=[1, 1, 1, 1, 1, 1, int(density), int(density)])
     p0, p, fr, fp, fz, R, d0, dd = (dev.to_host(t) if t is not None else None for t in outs)

@@ -4,8 +4,9 @@
 ``prep_tables`` uploads both bases once; the coefficient-contracted fields are
 prepared on first use and cached for the current coefficients, halofac and
 truncation settings, so repeated force calls (orbit integration) only run the
-per-point kernel.  Snapshot reading is outside this package:
-``total_coefficients`` takes in-memory particle containers instead of a file.
+per-point kernel.  ``total_coefficients`` reads the snapshot named by the
+instance (or takes in-memory particle containers); ``get_fields`` is the
+snapshot -> prepared Fields driver of the reference.
 """
 from __future__ import annotations
 
@@ -40,20 +41,34 @@ class Fields:
 
     # ------------------------------------------------------------ coefficients
     def total_coefficients(self, disk_particles=None, halo_particles=None, halo_total=None, ncenter=10000):
-        """potential.Fields.total_coefficients (potential.py:98-252) on
-        in-memory particle containers (``.data`` dicts or holders) instead of
-        a snapshot file.  halofac = len(halo_particles) / halo_total when
-        halo_total is given (the reference divides the halo count by itself,
-        :139-142, so 1).  With ``centering``: the mass-weighted centre of the
-        ``ncenter`` disc particles nearest the origin (argsort of r) is taken
-        off the disc, and off the halo either the same centre
-        (``mutual_center``) or the centre of the halo particles at those same
-        indices (the reference ranks the disc radii for the halo too,
-        :196-205); then both bases are accumulated on the GPU."""
-        if disk_particles is None or halo_particles is None:
-            raise ValueError("total_coefficients needs disk_particles and halo_particles (no snapshot reader here)")
+        """potential.Fields.total_coefficients (potential.py:98-252).
+
+        Called without arguments, as in the reference: reads the components
+        'star' (disc) and 'dark' (halo) of the snapshot ``self.filename`` with
+        ``particle.Input`` (PSP or SPL by file name), sets ``self.time`` from
+        the disc component and halofac = 1 (the reference divides the halo
+        count by itself, :139-142).
+
+        Added keywords: ``disk_particles`` and ``halo_particles`` take
+        in-memory containers (``.data`` dicts or holders) instead of the file,
+        and halofac = len(halo_particles) / halo_total when halo_total is
+        given.
+
+        With ``centering``: the mass-weighted centre of the ``ncenter`` disc
+        particles nearest the origin (argsort of r) is taken off the disc, and
+        off the halo either the same centre (``mutual_center``) or the centre
+        of the halo particles at those same indices (the reference ranks the
+        disc radii for the halo too, :196-205); then both bases are
+        accumulated on the GPU."""
         if self.transform:
             raise NotImplementedError("transform=True needs the bar transform of exptool.analysis.pattern")
+        if disk_particles is None and halo_particles is None:
+            from ..io import particle
+            disk_particles = particle.Input(self.filename, comp='star', verbose=self.verbose)
+            halo_particles = particle.Input(self.filename, comp='dark', verbose=self.verbose)
+        elif disk_particles is None or halo_particles is None:
+            raise ValueError("total_coefficients: give both disk_particles and halo_particles, or neither "
+                             "(then components 'star' and 'dark' of the snapshot self.filename are read)")
         from ..io.particle import holder, positions
         self.time = getattr(disk_particles, "time", None)
         dx, dy, dz, dm = positions(disk_particles)
@@ -326,3 +341,26 @@ def restore_field(filename=''):
     F.halofac = float(F.halofac)
     F._upload_from_arrays()
     return F
+
+
+def get_fields(simulation_directory, simulation_name, intime, eof_file, sph_file, model_file, bar_file='',
+               nhalo=1000000, transform=True, fileprefix='OUT'):
+    """potential.get_fields (potential.py:1243-1288): the Fields of snapshot
+    ``simulation_directory + fileprefix + '.' + simulation_name + '.%05i' %
+    intime``, centred on the disc (centering=True, mutual_center=True), with
+    coefficients accumulated and tables prepared; returns (F, pattern speed,
+    rotation frequency) = (F, 0, 0).  transform=True (the reference's
+    default) rotates into the bar frame found from ``bar_file`` by
+    exptool.analysis.pattern, which is outside this package:
+    NotImplementedError."""
+    infile = simulation_directory + fileprefix + '.' + simulation_name + '.%05i' % intime
+    if transform:
+        raise NotImplementedError("get_fields(transform=True) needs the bar pattern of exptool.analysis.pattern; "
+                                  "pass transform=False")
+    patt = 0.
+    rotfreq = 0.
+    F = Fields(infile, eof_file, sph_file, model_file, nhalo=nhalo, transform=transform, no_odd=False,
+               centering=True, mutual_center=True)
+    F.total_coefficients()
+    F.prep_tables()
+    return F, patt, rotfreq

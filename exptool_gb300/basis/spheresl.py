@@ -119,16 +119,24 @@ def compute_coefficients(PSPInput, sph_file, mod_file, verbose=1, no_odd=False, 
 
 
 def compute_coefficients_batched(snapshots, sph_file, mod_file, no_odd=False, autotune=True, chunk=None,
-                                 threads=None):
-    """Coefficients of many snapshots in one persistent GPU launch (the
-    series spheresl.compute_coefficients would produce one call at a time).
+                                 threads=None, engine="deposit", stages=None):
+    """Coefficients of many snapshots in one pass on the GPU (the series
+    spheresl.compute_coefficients would produce one call at a time).
 
     ``snapshots``: a list of particle containers (holder-like or ``.data``),
     or a pair (xyzm, offsets) with xyzm an (N, 4) float32 array / CUDA tensor
-    of x y z m and offsets the nsnap+1 snapshot boundaries.  Mixed precision:
-    FP32 per-particle arithmetic and shared-memory accumulation, FP64 sums
-    across work items and FP64 contraction.  Returns an array of shape
-    (nsnap, (lmax+1)^2, nmax)."""
+    of x y z m and offsets the nsnap+1 snapshot boundaries.  Returns an array
+    of shape (nsnap, (lmax+1)^2, nmax).
+
+    engine="deposit": one persistent launch with FP32 per-particle arithmetic
+    and shared-memory accumulation, FP64 sums across work items and FP64
+    contraction (about 1e-7 of FP64).  engine="tensor": particles sorted by
+    (snapshot, radial window), BF16 products of interpolation weights and
+    angular basis values on the tensor cores with FP32 accumulation, FP64
+    window sums and contraction (BF16 operands: about 1e-4 of FP64 on
+    snapshots of 1e4 particles and more).  ``chunk``/``threads`` (deposit)
+    or ``chunk``/``stages`` (tensor) fix the launch shape; otherwise it is
+    autotuned (or a default with autotune=False)."""
     table = table_from_files(sph_file, mod_file)
     if isinstance(snapshots, tuple) and len(snapshots) == 2:
         xyzm, offsets = snapshots
@@ -144,6 +152,21 @@ def compute_coefficients_batched(snapshots, sph_file, mod_file, no_odd=False, au
             counts.append(x.size)
         offsets = np.cumsum(counts).astype(np.int64)
         xyzm = torch.from_numpy(np.concatenate(parts, axis=0)).to(dev.device()).contiguous()
+    if engine == "tensor":
+        if chunk is None or stages is None:
+            if autotune:
+                from .. import autotune as at
+                cfg, _ = at.sph_batched_tc_config(table, xyzm, offsets)
+            else:
+                cfg = {"chunk": 16384, "stages": 2}
+            chunk = cfg["chunk"] if chunk is None else chunk
+            stages = cfg["stages"] if stages is None else stages
+        out = table.accumulate_batched_tc(xyzm, offsets, no_odd=no_odd, chunk=chunk, stages=stages)
+        host = dev.to_host(out)
+        dev.batched_tc_status()
+        return host
+    if engine != "deposit":
+        raise ValueError(f"engine must be 'deposit' or 'tensor', not {engine!r}")
     if chunk is None or threads is None:
         if autotune:
             from .. import autotune as at

@@ -142,6 +142,15 @@ __global__ void __launch_bounds__(256) k_sph_contract_batched(const double* __re
 
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+int launch_sph_contract_batched(const double* efp, const double* G, int nsnap, int lmax, int nmax, int numr,
+                                double* out, cudaStream_t st) {
+  const long long nout = (long long)nsnap * (lmax + 1) * (lmax + 1) * nmax;
+  const int cgrid = (int)std::min<long long>((nout * 32 + 255) / 256, 152LL * 64);
+  k_sph_contract_batched<<<cgrid, 256, 0, st>>>(efp, G, nsnap, lmax, nmax, numr, out);
+  XT_CHECK_LAUNCH("k_sph_contract_batched");
+  return XT_OK;
+}
+
 }  // namespace xt
 
 using namespace xt;
@@ -236,13 +245,9 @@ int xt_sph_accumulate_batched(void* handle, const float* xyzm, const long long* 
     if (rc) return rc;
     XT_CHECK_LAUNCH("k_sph_batched");
   }
-  const long long nout = (long long)nsnap * nrow * d.nmax;
-  const int cgrid = (int)std::min<long long>((nout * 32 + 255) / 256, 152LL * 64);
   const double* efp = nullptr;
   XT_REQUIRE(sph_efp(handle, &efp), "NULL table handle");
-  k_sph_contract_batched<<<cgrid, 256, 0, st>>>(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out);
-  XT_CHECK_LAUNCH("k_sph_contract_batched");
-  return XT_OK;
+  return launch_sph_contract_batched(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
 }
 
 }  // extern "C"

@@ -1,0 +1,671 @@
+// Batched spherical accumulation on the 5th-generation tensor cores.
+//
+// The same sums as k_sph_batched (xt_batch.cu), the coefficient time series
+// spheresl.compute_coefficients (spheresl.py:439-475, accumulation loop
+// :598-654) would produce snapshot by snapshot, written as dense products.
+// The radial table interpolation is linear in the node values, so
+//   expcoef[s, row, n] = sum_node ef'[l(row), n, node] G[s, row, node],
+//   G[s, row, node]    = sum_p W[p, node] A[p, row],
+// with A[p, row] = P_l^m(cos th_p) {1, cos m phi_p, sin m phi_p} (the
+// angular basis values of particle p, the normalisation fact[l][m] applied
+// in FP64 to G; a BF16 rounding of it would bias every particle alike) and
+// W[p, node] its two non-zero
+// interpolation weights -4 pi m_p plerp_p {x1_p, x2_p} on nodes i_p, i_p + 1
+// (the nodal hat-function basis of the table interpolation).  G is a
+// particles x basis-terms product: for a window of 128 consecutive nodes,
+//   D[node, row] = sum_p W^T[node, p] A[p, row]
+// is one tcgen05.mma chain with M = 128 nodes, N = rows (padded to a multiple
+// of 16), K = particles, BF16 operands and FP32 accumulation in tensor memory.
+//
+// Pipeline (one call, all snapshots):
+//   1. k_bt_hist: the node interval i of every particle (kept), counts per
+//      (sorting chunk, window of 127 intervals);
+//   2. k_bt_offsets, k_bt_buckets, k_bt_items: per-chunk offsets inside each
+//      (snapshot, window) bucket, bucket bases, and work items (bucket pieces
+//      of at most `chunk` particles);
+//   3. k_bt_scatter: counting sort of the particles by (snapshot, window);
+//   4. k_sph_batched_tc: persistent; a CTA takes an item, builds the W^T and
+//      A tiles of 128 particles per K-tile in shared memory (one particle per
+//      thread, BF16, canonical K-major layout), one thread issues the MMAs
+//      and commits them to the stage's mbarrier while the next stage is
+//      built; at the item's end the accumulator (128 nodes x rows, FP32) is
+//      read from tensor memory into a per-item partial;
+//   5. k_bt_reduce: FP64 sum of the partials per (snapshot, row, node), in a
+//      fixed order (the window boundary node takes both windows' shares);
+//   6. k_sph_contract_batched: FP64 contraction with the radial tables.
+// Waits are bounded: a timeout sets the error flag read by
+// xt_sph_batched_tc_status, waits once more for the MMAs in flight, frees the
+// tensor memory and returns.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "xt_internal.cuh"
+#include "xt_launch.cuh"
+#include "xt_tc.cuh"
+
+namespace xt {
+
+constexpr int BT_M = 128;                   // nodes per window tile (tensor-memory lanes)
+constexpr int BT_NODES = BT_M - 1;          // interpolation intervals per window
+constexpr int BT_KT = 128;                  // particles per K-tile (one per thread)
+constexpr int BT_THREADS = 128;
+constexpr int BT_LBO = 128;                 // bytes between core matrices along K
+constexpr int BT_SBO = (BT_KT / 8) * 128;   // bytes between 8-row groups
+constexpr int BT_A_BYTES = BT_M * BT_KT * 2;
+constexpr int BT_SORT_CHUNK = 4096;         // particles per sorting chunk
+constexpr int BT_MAXWIN = 64;               // windows per snapshot (numr <= 64 * 127 + 1)
+constexpr float BT_FOUR_PI = 12.566370614359172f;
+
+struct BtChunk {
+  int snap;
+  int pad;
+  long long begin, end;
+};
+
+struct BtItem {
+  int bucket, snap, win, pad;
+  long long begin, end;
+};
+
+struct BtArgs {
+  SphTab<float> T;
+  const float4* sorted;
+  const int* sidx;
+  const BtItem* items;
+  const int* nitems;
+  int* counter;
+  float* partial;       // [item][nrow][128]
+  int* err;
+  int nrow, no_odd;
+};
+
+__device__ __forceinline__ int bt_off(int row, int k) {
+  return (row >> 3) * BT_SBO + (k >> 3) * BT_LBO + (row & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ void bt_st(unsigned char* tile, int row, int k, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(tile + bt_off(row, k)) = __float2bfloat16_rn(v);
+}
+
+__device__ __forceinline__ float bt_radius(float4 q) {
+  float r = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
+  return (r >= 1.0e-10f) ? r : 1.0e-10f;
+}
+
+// Interpolation weights x1 plerp, x2 plerp of radius r on interval i (the
+// FP32 weights of sph_bins, spheresl.py:121-143, for a given interval; used
+// when the interval recomputed here differs from the one the sort stored).
+__device__ __noinline__ float2 bt_weights_at(const SphTab<float>& T, float r, int i) {
+  float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
+  if (T.cmap == 1) x = fminf(fmaxf(x, -1.f), 1.f - 1.0e-8f);
+  if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
+  const float x2 = (x - T.xi[i]) * T.inv_dxi, x1 = 1.f - x2;
+  const float plerp = x1 * T.p0[i] + x2 * T.p0[i + 1];
+  return make_float2(x1 * plerp, x2 * plerp);
+}
+
+// Interpolation interval of radius r: the node index of sph_bins
+// (spheresl.py:121-131) without its weights (no table reads).
+__device__ __forceinline__ int bt_interval(const SphTab<float>& T, float r) {
+  float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
+  if (T.cmap == 1) {
+    if (x < -1.f) x = -1.f;
+    if (x >= 1.f) x = 1.f - 1.0e-08f;
+  }
+  if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
+  float fi = floorf((x - T.xi0) * T.inv_dxi);
+  if (!(fi >= 0.f)) fi = 0.f;
+  if (fi > (float)(T.numr - 2)) fi = (float)(T.numr - 2);
+  return (int)fi;
+}
+
+// ------------------------------------------------------------------ sort
+// Exclusive scan over a block of 256 threads; *total receives the block sum.
+__device__ __forceinline__ int bt_block_scan(int v, int* wsum, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int t = lane < 8 ? wsum[lane] : 0;
+    int u = t;
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, u, d);
+      if (lane >= d) u += y;
+    }
+    if (lane < 8) wsum[lane] = u - t;
+    if (lane == 7) wsum[8] = u;
+  }
+  __syncthreads();
+  const int r = x - v + wsum[wid];
+  *total = wsum[8];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_bt_hist(SphTab<float> T, const float4* __restrict__ xyzm,
+                                                 const BtChunk* __restrict__ chunks, int nchunk, int nwin,
+                                                 int* __restrict__ pidx, int* __restrict__ ccount) {
+  __shared__ int cnt[BT_MAXWIN];
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+    for (int w = threadIdx.x; w < nwin; w += blockDim.x) cnt[w] = 0;
+    __syncthreads();
+    const BtChunk C = chunks[c];
+    for (long long p = C.begin + threadIdx.x; p < C.end; p += blockDim.x) {
+      const int i = bt_interval(T, bt_radius(xyzm[p]));
+      pidx[p] = i;
+      atomicAdd(&cnt[i / BT_NODES], 1);
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < nwin; w += blockDim.x) ccount[(size_t)c * nwin + w] = cnt[w];
+    __syncthreads();
+  }
+}
+
+// One block per snapshot: offsets of each chunk inside its (snapshot, window)
+// bucket and the bucket sizes.
+__global__ void __launch_bounds__(256) k_bt_offsets(const int* __restrict__ cfirst, int nwin,
+                                                    const int* __restrict__ ccount, int* __restrict__ coff,
+                                                    long long* __restrict__ bsize) {
+  __shared__ int wsum[9];
+  const int s = blockIdx.x;
+  const int c0 = cfirst[s], c1 = cfirst[s + 1];
+  for (int w = 0; w < nwin; ++w) {
+    long long carry = 0;
+    for (int base = c0; base < c1; base += blockDim.x) {
+      const int c = base + threadIdx.x;
+      const int v = c < c1 ? ccount[(size_t)c * nwin + w] : 0;
+      int tot;
+      const int ex = bt_block_scan(v, wsum, &tot);
+      if (c < c1) coff[(size_t)c * nwin + w] = (int)carry + ex;
+      carry += tot;
+    }
+    if (threadIdx.x == 0) bsize[(size_t)s * nwin + w] = carry;
+  }
+}
+
+// One block: bucket bases (particle offsets in the sorted stream) and the
+// first work item of every bucket.
+__global__ void __launch_bounds__(256) k_bt_buckets(const long long* __restrict__ bsize, int nb, int chunk,
+                                                    long long* __restrict__ bbase, int* __restrict__ ifirst,
+                                                    int* __restrict__ nitems) {
+  __shared__ int wsum[9];
+  __shared__ long long tile[256];
+  __shared__ long long carry_p;
+  int carry_i = 0;
+  if (threadIdx.x == 0) carry_p = 0;
+  for (int base = 0; base < nb; base += blockDim.x) {
+    const int b = base + threadIdx.x;
+    const long long sz = b < nb ? bsize[b] : 0;
+    int tot;
+    const int ex = bt_block_scan((int)((sz + chunk - 1) / chunk), wsum, &tot);
+    tile[threadIdx.x] = sz;
+    __syncthreads();
+    if (threadIdx.x == 0) {            // particle offsets exceed int: a serial scan of the tile
+      long long acc = carry_p;
+      for (int k = 0; k < (int)blockDim.x; ++k) {
+        const long long t = tile[k];
+        tile[k] = acc;
+        acc += t;
+      }
+      carry_p = acc;
+    }
+    __syncthreads();
+    if (b < nb) {
+      bbase[b] = tile[threadIdx.x];
+      ifirst[b] = carry_i + ex;
+    }
+    carry_i += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ifirst[nb] = carry_i;
+    *nitems = carry_i;
+  }
+}
+
+__global__ void k_bt_items(const long long* __restrict__ bsize, const long long* __restrict__ bbase,
+                           const int* __restrict__ ifirst, int nb, int nwin, int chunk, BtItem* __restrict__ items) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    const long long sz = bsize[b], b0 = bbase[b];
+    int it = ifirst[b];
+    for (long long o = 0; o < sz; o += chunk, ++it)
+      items[it] = BtItem{b, b / nwin, b % nwin, 0, b0 + o, b0 + (o + chunk < sz ? o + chunk : sz)};
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bt_scatter(const float4* __restrict__ xyzm, const BtChunk* __restrict__ chunks,
+                                                    int nchunk, int nwin, const int* __restrict__ pidx,
+                                                    const int* __restrict__ coff, const long long* __restrict__ bbase,
+                                                    long long n_total, float4* __restrict__ sorted,
+                                                    int* __restrict__ sidx, int* __restrict__ err) {
+  __shared__ int cnt[BT_MAXWIN];
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+    for (int w = threadIdx.x; w < nwin; w += blockDim.x) cnt[w] = 0;
+    __syncthreads();
+    const BtChunk C = chunks[c];
+    for (long long p = C.begin + threadIdx.x; p < C.end; p += blockDim.x) {
+      const int i = pidx[p];
+      const int w = i / BT_NODES;
+      const int slot = atomicAdd(&cnt[w], 1);
+      const long long dst = bbase[(size_t)C.snap * nwin + w] + coff[(size_t)c * nwin + w] + slot;
+      if (dst >= 0 && dst < n_total) {
+        sorted[dst] = xyzm[p];
+        sidx[dst] = i;
+      } else {
+        atomicExch(err, 2);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ tensor-core products
+template <int LCAP, int NPAD, int STAGES>
+__global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
+  constexpr int B_BYTES = NPAD * BT_KT * 2;
+  constexpr int STAGE_BYTES = BT_A_BYTES + B_BYTES;
+  constexpr int NCOLS = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
+  constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + STAGES * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + STAGES);
+  int* s_item = reinterpret_cast<int*>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const SphTab<float>& T = a.T;
+  const int lmax = T.lmax;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(NCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid < STAGES) mbar_init(smem_u32(bars + tid));
+  // operand tiles start at zero: padded rows of A and the rows of W^T that no
+  // particle touches stay zero
+  for (int o = tid * 16; o < STAGES * STAGE_BYTES; o += BT_THREADS * 16)
+    *reinterpret_cast<uint4*>(sm + o) = make_uint4(0u, 0u, 0u, 0u);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = tc_idesc(BT_M, NPAD);
+  const int nitems = *a.nitems;
+  int prev_row[STAGES];
+#pragma unroll
+  for (int s = 0; s < STAGES; ++s) prev_row[s] = -1;
+  long long g = 0;          // K-tiles issued by this CTA (stage g % STAGES)
+  bool ok = true;           // block-uniform: every failure test is a __syncthreads_or
+
+  for (;;) {
+    if (tid == 0) *s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int it = *s_item;
+    if (it >= nitems) break;
+    const BtItem I = a.items[it];
+    const int wbase = I.win * BT_NODES;
+    const long long ntile = (I.end - I.begin + BT_KT - 1) / BT_KT;
+    // this thread's particle of the next K-tile is loaded one tile ahead
+    float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+    int in = 0;
+    if (I.begin + tid < I.end) {
+      qn = a.sorted[I.begin + tid];
+      in = a.sidx[I.begin + tid];
+    }
+    for (long long t = 0; t < ntile; ++t, ++g) {
+      const float4 q = qn;
+      const int i = in;
+      const long long pn = I.begin + (t + 1) * BT_KT + tid;
+      if (pn < I.end) {
+        qn = a.sorted[pn];
+        in = a.sidx[pn];
+      }
+      const int st = (int)(g % STAGES);
+      unsigned char* At = sm + st * STAGE_BYTES;
+      unsigned char* Bt = At + BT_A_BYTES;
+      // the MMAs that last read this stage (K-tile g - STAGES) must be done
+      bool lf = g >= STAGES && !mbar_wait(smem_u32(bars + st), (uint32_t)(((g / STAGES) - 1) & 1));
+      if (__syncthreads_or(lf)) {
+        ok = false;
+        break;
+      }
+      // column `tid` of this stage: clear the weights the last particle here left
+      int pr = -1;
+#pragma unroll
+      for (int s = 0; s < STAGES; ++s)
+        if (s == st) pr = prev_row[s];
+      if (pr >= 0) {
+        *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr, tid)) = __float2bfloat16_rn(0.f);
+        *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr + 1, tid)) = __float2bfloat16_rn(0.f);
+      }
+      int nr = -1;
+      const long long p = I.begin + t * BT_KT + tid;
+      if (p < I.end) {
+        const float r = bt_radius(q);
+        const SphBins<float> B = sph_bins(T, r, false, false);
+        float2 lw = make_float2(B.lw0, B.lw1);
+        if (B.i != i) lw = bt_weights_at(T, r, i);
+        const int li = i - wbase;
+        if (li >= 0 && li < BT_NODES) {
+          const float base = -BT_FOUR_PI * q.w;
+          bt_st(At, li, tid, lw.x * base);
+          bt_st(At, li + 1, tid, lw.y * base);
+          nr = li;
+        } else {
+          atomicExch(a.err, 3);
+        }
+        const float costh = q.z / r;
+        float c1, s1;
+        unit_phi(q.x, q.y, c1, s1);
+        float P[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) P[k] = 0.f;
+        legendre<float, LCAP>(costh, lmax, P);
+        float cm[LCAP + 1], sn[LCAP + 1];
+        multiples<float, LCAP>(c1, s1, lmax, cm, sn);
+#pragma unroll
+        for (int l = 0; l <= LCAP; ++l) {
+          if (l > lmax) break;
+          if (a.no_odd && (l & 1)) continue;     // rows of odd l stay zero
+          const int loff = l * l;
+#pragma unroll
+          for (int m = 0; m <= l; ++m) {
+            // the normalisation fact[l][m] is applied in FP64 by k_bt_reduce:
+            // a BF16 rounding of it would be the same for every particle
+            const float v = P[tri(l, m)];
+            if (m == 0) {
+              bt_st(Bt, loff, tid, v);
+            } else {
+              bt_st(Bt, loff + 2 * m - 1, tid, v * cm[m]);
+              bt_st(Bt, loff + 2 * m, tid, v * sn[m]);
+            }
+          }
+        }
+      } else {
+        // no particle: a zero angular column (a stale non-finite value would
+        // survive the zero weights)
+        for (int row = 0; row < a.nrow; ++row) bt_st(Bt, row, tid, 0.f);
+      }
+#pragma unroll
+      for (int s = 0; s < STAGES; ++s)
+        if (s == st) prev_row[s] = nr;
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid == 0) {
+        const uint32_t ab = smem_u32(At), bb = smem_u32(Bt);
+#pragma unroll
+        for (int kk = 0; kk < BT_KT / 16; ++kk)
+          tc_mma(tmem, tc_desc(ab + kk * 2 * BT_LBO, BT_LBO, BT_SBO), tc_desc(bb + kk * 2 * BT_LBO, BT_LBO, BT_SBO),
+                 idesc, (t > 0 || kk > 0) ? 1u : 0u);
+        tc_commit(smem_u32(bars + st));
+      }
+    }
+    if (!ok) break;
+    // the item's sums: wait for its last MMAs, read the accumulator rows
+    const int lst = (int)((g - 1) % STAGES);
+    const bool lf = !mbar_wait(smem_u32(bars + lst), (uint32_t)(((g - 1) / STAGES) & 1));
+    if (__syncthreads_or(lf)) {
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    float* dst = a.partial + (size_t)it * a.nrow * BT_M + 32 * warp + (tid & 31);
+#pragma unroll 1
+    for (int c16 = 0; c16 < NPAD / 16; ++c16) {
+      float v[16];
+      tc_ld16(trow + 16 * c16, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int row = 16 * c16 + j;
+        if (row < a.nrow) dst[(size_t)row * BT_M] = v[j];
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  // after a wait gave up, the MMAs still in flight finish (bounded) before the
+  // tensor memory is released
+  if (!ok && g > 0) mbar_wait(smem_u32(bars + (int)((g - 1) % STAGES)), (uint32_t)(((g - 1) / STAGES) & 1));
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && !ok) atomicExch(a.err, 1);
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS) : "memory");
+  }
+}
+
+// G[s, row, node] = fact[l][m] times the FP64 sum of the partials of the
+// windows holding the node, in item order.  Node 127 w (w >= 1) is lane 0 of
+// window w and lane 127 of window w - 1.
+__global__ void __launch_bounds__(256) k_bt_reduce(const float* __restrict__ partial, const int* __restrict__ ifirst,
+                                                   const double* __restrict__ fact, int lmax, int nsnap, int nrow,
+                                                   int numr, int nwin, double* __restrict__ G) {
+  const long long total = (long long)nsnap * nrow * numr;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
+       o += (long long)gridDim.x * blockDim.x) {
+    const int node = (int)(o % numr);
+    const long long sr = o / numr;
+    const int row = (int)(sr % nrow), s = (int)(sr / nrow);
+    const int w = node / BT_NODES, lane = node - w * BT_NODES;
+    double acc = 0.0;
+    if (w < nwin) {
+      const int b = s * nwin + w;
+      for (int it = ifirst[b]; it < ifirst[b + 1]; ++it)
+        acc += (double)partial[((size_t)it * nrow + row) * BT_M + lane];
+    }
+    if (lane == 0 && w >= 1) {
+      const int b = s * nwin + w - 1;
+      for (int it = ifirst[b]; it < ifirst[b + 1]; ++it)
+        acc += (double)partial[((size_t)it * nrow + row) * BT_M + BT_NODES];
+    }
+    int l = 0;
+    while ((l + 1) * (l + 1) <= row) ++l;
+    const int m = (row - l * l + 1) >> 1;            // row l^2 (m = 0), l^2 + 2m - 1 (cos), l^2 + 2m (sin)
+    G[o] = fact[l * (lmax + 1) + m] * acc;
+  }
+}
+
+static __device__ int g_bt_err;
+
+static size_t bt_al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct BtLayout {
+  size_t G, pidx, sorted, sidx, chunks, cfirst, ccount, coff, bsize, bbase, ifirst, items, partial, ctr, total;
+  long long max_items;
+  int nwin, nb;
+  long long nchunk;
+};
+
+static BtLayout bt_layout(const SphTab<double>& d, int nsnap, long long n_total, long long nchunk, int chunk) {
+  BtLayout L;
+  const int nrow = (d.lmax + 1) * (d.lmax + 1);
+  L.nwin = (d.numr - 2) / BT_NODES + 1;
+  L.nb = nsnap * L.nwin;
+  L.nchunk = nchunk;
+  L.max_items = n_total / chunk + L.nb + 1;
+  size_t o = 0;
+  auto take = [&](size_t b) { const size_t at = o; o += bt_al(b); return at; };
+  L.G = take((size_t)nsnap * nrow * d.numr * sizeof(double));
+  L.pidx = take((size_t)n_total * sizeof(int));
+  L.sorted = take((size_t)n_total * sizeof(float4));
+  L.sidx = take((size_t)n_total * sizeof(int));
+  L.chunks = take((size_t)nchunk * sizeof(BtChunk));
+  L.cfirst = take((size_t)(nsnap + 1) * sizeof(int));
+  L.ccount = take((size_t)nchunk * L.nwin * sizeof(int));
+  L.coff = take((size_t)nchunk * L.nwin * sizeof(int));
+  L.bsize = take((size_t)L.nb * sizeof(long long));
+  L.bbase = take((size_t)L.nb * sizeof(long long));
+  L.ifirst = take((size_t)(L.nb + 1) * sizeof(int));
+  L.items = take((size_t)L.max_items * sizeof(BtItem));
+  L.partial = take((size_t)L.max_items * nrow * BT_M * sizeof(float));
+  L.ctr = take(4 * sizeof(int));
+  L.total = o;
+  return L;
+}
+
+static long long bt_nchunk(const long long* off, int nsnap) {
+  long long n = 0;
+  for (int s = 0; s < nsnap; ++s) n += (off[s + 1] - off[s] + BT_SORT_CHUNK - 1) / BT_SORT_CHUNK;
+  return n;
+}
+
+template <int LC, int NPAD, int STAGES>
+static int bt_launch_gemm(const BtArgs& A, cudaStream_t st) {
+  constexpr size_t smem = (size_t)STAGES * (BT_A_BYTES + NPAD * BT_KT * 2) + STAGES * 8 + 8;
+  auto kern = k_sph_batched_tc<LC, NPAD, STAGES>;
+  XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  XT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT_THREADS, smem));
+  XT_REQUIRE(per_sm >= 1, "k_sph_batched_tc does not fit on an SM with %zu bytes of shared memory", smem);
+  // tensor memory: every resident CTA holds NCOLS of the SM's 512 columns
+  const int ncols = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
+  per_sm = std::min(per_sm, 512 / ncols);
+  kern<<<sm_count() * per_sm, BT_THREADS, smem, st>>>(A);
+  XT_CHECK_LAUNCH("k_sph_batched_tc");
+  return XT_OK;
+}
+
+}  // namespace xt
+
+using namespace xt;
+
+extern "C" {
+
+size_t xt_sph_batched_tc_workspace(void* handle, int nsnap, const long long* offsets_host, int chunk) {
+  SphTab<double> d;
+  if (!sph_tabs(handle, &d, nullptr) || nsnap <= 0 || !offsets_host || chunk < BT_KT) return 0;
+  const long long n_total = offsets_host[nsnap] - offsets_host[0];
+  if (n_total < 0) return 0;
+  return bt_layout(d, nsnap, n_total, bt_nchunk(offsets_host, nsnap), chunk).total;
+}
+
+int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long long* offsets_host, int nsnap,
+                                 int no_odd, int chunk, int stages, double* expcoef_out, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  SphTab<double> d;
+  SphTab<float> f;
+  XT_REQUIRE(sph_tabs(handle, &d, &f), "NULL table handle");
+  XT_REQUIRE(nsnap > 0 && offsets_host && expcoef_out, "need nsnap > 0, host offsets and an output");
+  XT_REQUIRE(chunk >= BT_KT && chunk <= (1 << 30), "chunk must be in [%d, 2^30] particles", BT_KT);
+  XT_REQUIRE(stages == 2 || stages == 3, "stages must be 2 or 3");
+  XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
+  XT_REQUIRE(d.numr >= 2 && (d.numr - 2) / BT_NODES + 1 <= BT_MAXWIN, "numr must be in [2, %d]",
+             BT_MAXWIN * BT_NODES + 1);
+  const long long n_total = offsets_host[nsnap] - offsets_host[0];
+  XT_REQUIRE(n_total >= 0 && offsets_host[0] == 0, "offsets must start at 0 and be non-decreasing");
+  for (int s = 0; s < nsnap; ++s) XT_REQUIRE(offsets_host[s + 1] >= offsets_host[s], "offsets must be non-decreasing");
+  XT_REQUIRE(n_total < (1LL << 31), "at most 2^31 - 1 particles per call");
+  XT_REQUIRE(n_total == 0 || xyzm, "NULL particle stream");
+  XT_REQUIRE(((uintptr_t)xyzm & 15) == 0, "xyzm must be 16-byte aligned (float4 per particle)");
+  const long long nchunk = bt_nchunk(offsets_host, nsnap);
+  const BtLayout L = bt_layout(d, nsnap, n_total, nchunk, chunk);
+  if (!workspace || workspace_bytes < L.total) {
+    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  const int nrow = (d.lmax + 1) * (d.lmax + 1);
+  cudaStream_t st = as_stream(stream);
+  char* ws = static_cast<char*>(workspace);
+  double* G = reinterpret_cast<double*>(ws + L.G);
+  int* ctr = reinterpret_cast<int*>(ws + L.ctr);      // [0] items, [1] item counter
+  int* err = nullptr;
+  XT_CUDA(cudaGetSymbolAddress((void**)&err, g_bt_err));
+  XT_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st));
+  if (n_total == 0) {
+    XT_CUDA(cudaMemsetAsync(G, 0, (size_t)nsnap * nrow * d.numr * sizeof(double), st));
+  } else {
+    std::vector<BtChunk> chunks;
+    std::vector<int> cfirst(nsnap + 1);
+    chunks.reserve((size_t)nchunk);
+    for (int s = 0; s < nsnap; ++s) {
+      cfirst[s] = (int)chunks.size();
+      for (long long b = offsets_host[s]; b < offsets_host[s + 1]; b += BT_SORT_CHUNK)
+        chunks.push_back(BtChunk{s, 0, b, std::min(b + (long long)BT_SORT_CHUNK, offsets_host[s + 1])});
+    }
+    cfirst[nsnap] = (int)chunks.size();
+    BtChunk* dchunks = reinterpret_cast<BtChunk*>(ws + L.chunks);
+    int* dcfirst = reinterpret_cast<int*>(ws + L.cfirst);
+    XT_CUDA(cudaMemcpyAsync(dchunks, chunks.data(), chunks.size() * sizeof(BtChunk), cudaMemcpyHostToDevice, st));
+    XT_CUDA(cudaMemcpyAsync(dcfirst, cfirst.data(), cfirst.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    int* pidx = reinterpret_cast<int*>(ws + L.pidx);
+    int* ccount = reinterpret_cast<int*>(ws + L.ccount);
+    int* coff = reinterpret_cast<int*>(ws + L.coff);
+    long long* bsize = reinterpret_cast<long long*>(ws + L.bsize);
+    long long* bbase = reinterpret_cast<long long*>(ws + L.bbase);
+    int* ifirst = reinterpret_cast<int*>(ws + L.ifirst);
+    BtItem* items = reinterpret_cast<BtItem*>(ws + L.items);
+    float4* sorted = reinterpret_cast<float4*>(ws + L.sorted);
+    int* sidx = reinterpret_cast<int*>(ws + L.sidx);
+    const float4* q = reinterpret_cast<const float4*>(xyzm);
+    const int cgrid = (int)std::min<long long>(nchunk, (long long)sm_count() * 8);
+    k_bt_hist<<<cgrid, 256, 0, st>>>(f, q, dchunks, (int)nchunk, L.nwin, pidx, ccount);
+    XT_CHECK_LAUNCH("k_bt_hist");
+    k_bt_offsets<<<nsnap, 256, 0, st>>>(dcfirst, L.nwin, ccount, coff, bsize);
+    XT_CHECK_LAUNCH("k_bt_offsets");
+    k_bt_buckets<<<1, 256, 0, st>>>(bsize, L.nb, chunk, bbase, ifirst, ctr);
+    XT_CHECK_LAUNCH("k_bt_buckets");
+    k_bt_items<<<(L.nb + 255) / 256, 256, 0, st>>>(bsize, bbase, ifirst, L.nb, L.nwin, chunk, items);
+    XT_CHECK_LAUNCH("k_bt_items");
+    k_bt_scatter<<<cgrid, 256, 0, st>>>(q, dchunks, (int)nchunk, L.nwin, pidx, coff, bbase, n_total, sorted, sidx,
+                                        err);
+    XT_CHECK_LAUNCH("k_bt_scatter");
+    BtArgs A;
+    A.T = f;
+    A.sorted = sorted;
+    A.sidx = sidx;
+    A.items = items;
+    A.nitems = ctr;
+    A.counter = ctr + 1;
+    A.partial = reinterpret_cast<float*>(ws + L.partial);
+    A.err = err;
+    A.nrow = nrow;
+    A.no_odd = no_odd;
+    int rc = with_lcap(d.lmax, [&](auto lc) -> int {
+      constexpr int LC = decltype(lc)::value;
+      constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
+      return stages == 2 ? bt_launch_gemm<LC, NPAD, 2>(A, st) : bt_launch_gemm<LC, NPAD, 3>(A, st);
+    });
+    if (rc) return rc;
+    const long long nred = (long long)nsnap * nrow * d.numr;
+    k_bt_reduce<<<(int)std::min<long long>((nred + 255) / 256, (long long)sm_count() * 16), 256, 0, st>>>(
+        A.partial, ifirst, d.fact, d.lmax, nsnap, nrow, d.numr, L.nwin, G);
+    XT_CHECK_LAUNCH("k_bt_reduce");
+  }
+  const double* efp = nullptr;
+  XT_REQUIRE(sph_efp(handle, &efp), "NULL table handle");
+  return launch_sph_contract_batched(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
+}
+
+int xt_sph_batched_tc_status(void) {
+  int* err = nullptr;
+  XT_CUDA(cudaDeviceSynchronize());
+  XT_CUDA(cudaGetSymbolAddress((void**)&err, g_bt_err));
+  int v = 0;
+  XT_CUDA(cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    const int zero = 0;
+    XT_CUDA(cudaMemcpy(err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    set_error("batched tensor-core accumulation: %s", v == 1 ? "an MMA wait timed out"
+                                                            : (v == 2 ? "a sorted slot fell outside its bucket"
+                                                                      : "a particle fell outside its window"));
+    return XT_ERR_DEVICE;
+  }
+  return XT_OK;
+}
+
+}  // extern "C"

@@ -1462,11 +1462,14 @@ static int fused_graph_launch(CylHandle* h, int precision, const double* x, cons
         G.bp = kp;
       }
     }
-    XT_REQUIRE(G.binrec, "fused EOF graph: binning node not found");
-    const cudaError_t ei = cudaGraphInstantiate(&G.exec, g, 0);
+    const cudaError_t ei = G.binrec ? cudaGraphInstantiate(&G.exec, g, 0) : cudaErrorInvalidValue;
     if (ei != cudaSuccess) {
+      // no patchable binning node, or no executable graph: run this call (and
+      // the next of this shape) directly, as after a failed capture
       G.clear();
-      return cuda_fail(ei, "instantiate the fused EOF graph");
+      cudaGetLastError();
+      G.seen = false;
+      return enqueue();
     }
     G.key = key;
     G.x = x;
@@ -1503,40 +1506,20 @@ size_t xt_cyl_accumulate_eval_workspace(void* handle, long long n, int precision
   return fused_layout(h, n, precision).total;
 }
 
-int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const double* z, const double* m,
-                           long long n, int precision, int m1, int m2, int nan_to_origin, double* cos_out,
-                           double* sin_out, double* const* outs, void* workspace, size_t workspace_bytes,
-                           void* stream) {
-  CylHandle* h = static_cast<CylHandle*>(handle);
-  XT_REQUIRE(h, "NULL table handle");
-  XT_REQUIRE(n >= 0 && n < (1LL << 31), "particle count must be in [0, 2^31)");
-  XT_REQUIRE(cos_out && sin_out && outs, "NULL output");
-  XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
-  XT_REQUIRE(precision == XT_F64 || precision == XT_F32, "bad precision %d", precision);
-  XT_REQUIRE(h->mmax <= 8 && h->norder <= 24, "the fused path supports mmax <= 8, norder <= 24 (got %d, %d)",
-             h->mmax, h->norder);
-  XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
-             "the fused path supports numx*numy <= %d cells", kScanTile * kScanTile);
-  // particle arrays and results may live in host memory the device can
-  // address (pinned, or any host memory where the device has pageable access)
-  bool host_out = false;
-  if (n > 0) {
-    for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
-      XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
-                 p);
-    for (int i = 0; i < 6; ++i) {
-      if (!outs[i]) continue;
-      const int k = pointer_access(outs[i]);
-      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
-      if (i < 5) host_out |= k != XT_PTR_DEVICE;   // R (outs[5]) is written coalesced by the binning kernel
-    }
-  }
-  const FusedLayout L = fused_layout(h, n, precision);
-  if (!workspace || workspace_bytes < L.total) {
-    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
-    return XT_ERR_WORKSPACE;
-  }
-  cudaStream_t st = as_stream(stream);   // the stream work is enqueued on (the capture stream while capturing)
+}  // extern "C"
+
+// The stages of the sorted pipeline on one snapshot: binning (per-particle
+// set-up once, records with the particle's cell), counting sort by cell, then
+// with do_acc the run-accumulated deposit and the contraction into
+// cos_out/sin_out, and with do_eval the field from cos_src/sin_src and the
+// evaluation into outs (p0 p fr fp fz; R, outs[5], is written by the binning
+// kernel when non-NULL).  Results in host memory (host_out) are evaluated in
+// particle order, others in cell order.
+static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, const double* x, const double* y,
+                          const double* z, const double* m, long long n, int precision, int m1, int m2,
+                          int nan_to_origin, bool do_acc, bool do_eval, double* cos_out, double* sin_out,
+                          const double* cos_src, const double* sin_src, double* const* outs, bool host_out,
+                          cudaStream_t st) {
   char* ws = static_cast<char*>(workspace);
   double* D = reinterpret_cast<double*>(ws + L.grid);
   float* E = reinterpret_cast<float*>(ws + L.egrid);
@@ -1548,7 +1531,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
   const long long ngrid = (long long)(h->mmax + 1) * 2 * (long long)h->pitch_f;   // entries of D and of E
   auto run = [&](auto tag) -> int {
     // the binning kernel zeroes D and E; without particles they are cleared here
-    if (n == 0) {
+    if (n == 0 && do_acc) {
       XT_CUDA(cudaMemsetAsync(D, 0, (size_t)ngrid * sizeof(double), st));
       XT_CUDA(cudaMemsetAsync(E, 0, (size_t)ngrid * sizeof(float), st));
     }
@@ -1584,6 +1567,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       k_cyl_scatter<RT><<<resident_grid(k_cyl_scatter<RT>, 256, 0, n), 256, 0, st>>>(n, off, rec, srec);
       XT_CHECK_LAUNCH("k_cyl_scatter");
       if ((rc = timing_mark(3, st))) return rc;
+      if (do_acc) {
       // Run length: particles summed in registers per lane before the atomics.
       // Measured on 1e6 disc particles with same-cell lanes merged before the
       // atomics (runs of 4 to 16): 4 in both precisions (FP64 deposit 0.096 ms
@@ -1606,11 +1590,13 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       else if (h->mmax <= 6) dep(std::integral_constant<int, 6>{});
       else dep(std::integral_constant<int, 8>{});
       XT_CHECK_LAUNCH("k_cyl_deposit_sorted");
+      }
     } else {
       for (int k = 1; k <= 3; ++k)
         if ((rc = timing_mark(k, st))) return rc;
     }
     if ((rc = timing_mark(4, st))) return rc;
+    if (do_acc) {
     // coefficient contraction in both precisions from the double-float tables:
     // order groups of kContractRows, node chunks sized for one wave
     // (3 and 6 orders per block measured alike, 9 slower: fewer resident blocks)
@@ -1626,7 +1612,9 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     const int nout = (h->mmax + 1) * h->norder * 2;
     k_cyl_contract_final<<<(nout + 127) / 128, 128, 0, st>>>(part, nout, nch, cos_out, sin_out, h->norder);
     XT_CHECK_LAUNCH("k_cyl_contract_final");
+    }
     if ((rc = timing_mark(5, st))) return rc;
+    if (!do_eval) return timing_mark(6, st);
     // FP64 path: double-float field from the double-float tables; mixed path:
     // FP32 field from the FP32 tables (coefficients staged as df in both)
     using FT = std::conditional_t<F64, df, float>;
@@ -1642,7 +1630,7 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
       if (sm > 48 * 1024)
         XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, F64, RB, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm));
-      k_cyl_field2<FT, F64, RB, NT, MINB><<<fblocks, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_out, sin_out, h->mmax,
+      k_cyl_field2<FT, F64, RB, NT, MINB><<<fblocks, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax,
                                                                    h->norder, h->nnode, reinterpret_cast<FT*>(field));
     }
     XT_CHECK_LAUNCH("k_cyl_field2");
@@ -1678,11 +1666,119 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
     }
     return timing_mark(7, st);
   };
-  auto enqueue = [&]() -> int { return precision == XT_F64 ? run(double{}) : run(float{}); };
+  return precision == XT_F64 ? run(double{}) : run(float{});
+}
+
+extern "C" {
+
+int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const double* z, const double* m,
+                           long long n, int precision, int m1, int m2, int nan_to_origin, double* cos_out,
+                           double* sin_out, double* const* outs, void* workspace, size_t workspace_bytes,
+                           void* stream) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  XT_REQUIRE(h, "NULL table handle");
+  XT_REQUIRE(n >= 0 && n < (1LL << 31), "particle count must be in [0, 2^31)");
+  XT_REQUIRE(cos_out && sin_out && outs, "NULL output");
+  XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
+  XT_REQUIRE(precision == XT_F64 || precision == XT_F32, "bad precision %d", precision);
+  XT_REQUIRE(h->mmax <= 8 && h->norder <= 24, "the fused path supports mmax <= 8, norder <= 24 (got %d, %d)",
+             h->mmax, h->norder);
+  XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
+             "the fused path supports numx*numy <= %d cells", kScanTile * kScanTile);
+  // particle arrays and results may live in host memory the device can
+  // address (pinned, or any host memory where the device has pageable access)
+  bool host_out = false;
+  if (n > 0) {
+    for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
+      XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
+                 p);
+    for (int i = 0; i < 6; ++i) {
+      if (!outs[i]) continue;
+      const int k = pointer_access(outs[i]);
+      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
+      if (i < 5) host_out |= k != XT_PTR_DEVICE;   // R (outs[5]) is written coalesced by the binning kernel
+    }
+  }
+  const FusedLayout L = fused_layout(h, n, precision);
+  if (!workspace || workspace_bytes < L.total) {
+    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  cudaStream_t st = as_stream(stream);   // the stream work is enqueued on (the capture stream while capturing)
+  auto enqueue = [&]() -> int {
+    return sorted_enqueue(h, L, workspace, x, y, z, m, n, precision, m1, m2, nan_to_origin, true, true, cos_out,
+                          sin_out, cos_out, sin_out, outs, host_out, st);
+  };
   // Stage timing records events between the launches: enqueue directly.
   if (g_timing || n == 0) return enqueue();
   return fused_graph_launch(h, precision, x, y, z, m, n, m1, m2, nan_to_origin, cos_out, sin_out, outs, workspace,
                             L, st, enqueue);
+}
+
+
+// Shared argument checks of the sorted entry points; sets host_out when a
+// result array is host memory.
+static int sorted_checks(const CylHandle* h, const double* x, const double* y, const double* z, const double* m,
+                         long long n, int precision, double* const* outs, int nouts, bool& host_out) {
+  XT_REQUIRE(h, "NULL table handle");
+  XT_REQUIRE(n >= 0 && n < (1LL << 31), "particle count must be in [0, 2^31)");
+  XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
+  XT_REQUIRE(precision == XT_F64 || precision == XT_F32, "bad precision %d", precision);
+  XT_REQUIRE(h->mmax <= 8 && h->norder <= 24, "the sorted path supports mmax <= 8, norder <= 24 (got %d, %d)",
+             h->mmax, h->norder);
+  XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
+             "the sorted path supports numx*numy <= %d cells", kScanTile * kScanTile);
+  host_out = false;
+  if (n > 0) {
+    for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
+      XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
+                 p);
+    for (int i = 0; i < nouts; ++i) {
+      if (!outs[i]) continue;
+      const int k = pointer_access(outs[i]);
+      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
+      if (i < 5) host_out |= k != XT_PTR_DEVICE;
+    }
+  }
+  return XT_OK;
+}
+
+int xt_cyl_accumulate_sorted(void* handle, const double* x, const double* y, const double* z, const double* m,
+                             long long n, int precision, int nan_to_origin, double* cos_out, double* sin_out,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  bool host_out = false;
+  double* const none[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  int rc = sorted_checks(h, x, y, z, m, n, precision, none, 6, host_out);
+  if (rc) return rc;
+  XT_REQUIRE(cos_out && sin_out, "NULL output");
+  const FusedLayout L = fused_layout(h, n, precision);
+  if (!workspace || workspace_bytes < L.total) {
+    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  return sorted_enqueue(h, L, workspace, x, y, z, m, n, precision, 0, 0, nan_to_origin, true, false, cos_out,
+                        sin_out, nullptr, nullptr, none, false, as_stream(stream));
+}
+
+int xt_cyl_eval_sorted(void* handle, const double* x, const double* y, const double* z, long long n, int precision,
+                       int m1, int m2, const double* cos_c, const double* sin_c, double* const* outs,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  XT_REQUIRE(outs, "NULL output list");
+  bool host_out = false;
+  // the binning kernel reads a mass per particle for the deposit weight, which
+  // evaluation does not use: it is given the x array
+  int rc = sorted_checks(h, x, y, z, x, n, precision, outs, 6, host_out);
+  if (rc) return rc;
+  XT_REQUIRE(cos_c && sin_c, "NULL coefficients");
+  const FusedLayout L = fused_layout(h, n, precision);
+  if (!workspace || workspace_bytes < L.total) {
+    set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  return sorted_enqueue(h, L, workspace, x, y, z, x, n, precision, m1, m2, 0, false, true, nullptr, nullptr, cos_c,
+                        sin_c, outs, host_out, as_stream(stream));
 }
 
 }  // extern "C"

@@ -12,6 +12,8 @@
 // Evaluation first contracts the coefficients with the radial tables (per
 // node, per row) so each point does 3-point gathers per row instead of
 // nmax-long dot products.
+#include <cuda.h>
+
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
@@ -251,11 +253,41 @@ static __device__ __align__(256) double g_sph_noalloc_grid[XT_SPH_NOALLOC_MAX_DO
 
 namespace {
 std::mutex g_noalloc_mu;
-double* g_noalloc_addr[256] = {};   // device address of the array, per device ordinal
-}
+double* g_noalloc_addr[256] = {};             // device address of the array, per device ordinal
+unsigned long long g_noalloc_ctx[256] = {};   // the context it was looked up in (cuCtxGetId)
 
-// Device address of the static grid on the current device, looked up once per
-// device (cudaGetSymbolAddress with that device current) and then cached.
+// Identifier of the calling thread's current context (unique for the
+// process's lifetime), through the driver entry points the runtime exposes,
+// so the library needs no link to the driver library.  False when there is
+// no current context yet or the entry points are unavailable.
+bool current_context_id(unsigned long long* id) {
+  typedef CUresult (*GetCurrent)(CUcontext*);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  if (!get_current || !get_id) return false;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+}  // namespace
+
+// Device address of the static grid on the current device: looked up
+// (cudaGetSymbolAddress with that device current) on the first call and
+// again whenever the device's context has changed since, as after
+// cudaDeviceReset, when the module and its array are loaded anew.
 static int noalloc_grid(double** out) {
   int dev = 0;
   XT_CUDA(cudaGetDevice(&dev));
@@ -263,12 +295,15 @@ static int noalloc_grid(double** out) {
     set_error("device ordinal %d out of range for the static accumulation grid", dev);
     return XT_ERR_ARG;
   }
+  unsigned long long id = 0;
+  const bool have = current_context_id(&id);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  if (!g_noalloc_addr[dev] || !have || g_noalloc_ctx[dev] != id) {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_sph_noalloc_grid);
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sph_noalloc_grid);   // creates the context if there is none
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_sph_noalloc_grid)");
     g_noalloc_addr[dev] = static_cast<double*>(p);
+    g_noalloc_ctx[dev] = current_context_id(&id) ? id : 0;
   }
   *out = g_noalloc_addr[dev];
   return XT_OK;

@@ -232,6 +232,34 @@ class SphTable:
                    "xt_sph_accumulate_batched")
         return out
 
+    def accumulate_batched_tc(self, xyzm, offsets, no_odd=False, chunk=16384, stages=2, workspace=None):
+        """Coefficients of many snapshots on the tensor cores: particles
+        counting-sorted by (snapshot, radial window), then per window a BF16
+        tcgen05 product of the interpolation weights and the angular basis
+        values with FP32 accumulation, FP64 sums of the window partials and an
+        FP64 contraction.  Arguments as for accumulate_batched; ``chunk`` is
+        the most particles of one work item, ``stages`` the operand buffers in
+        flight (2 or 3).  Returns a (nsnap, (lmax+1)^2, nmax) float64 tensor."""
+        offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        nsnap = offs.size - 1
+        if xyzm.dtype != torch.float32 or xyzm.dim() != 2 or xyzm.shape[1] != 4 or not xyzm.is_contiguous():
+            raise ValueError("xyzm must be a contiguous (N, 4) float32 CUDA tensor")
+        out = torch.empty((nsnap, self.nrow, self.nmax), dtype=torch.float64, device=xyzm.device)
+        need = self._lib.xt_sph_batched_tc_workspace(self.handle, nsnap, offs.ctypes.data, int(chunk))
+        if need == 0:
+            raise ValueError("bad batched arguments (offsets, chunk)")
+        ws = workspace if (workspace is not None and workspace.numel() >= need) else \
+            torch.empty(need, dtype=torch.uint8, device=xyzm.device)
+        _lib.check(self._lib.xt_sph_accumulate_batched_tc(self.handle, dptr(xyzm), offs.ctypes.data, nsnap,
+                                                          int(bool(no_odd)), int(chunk), int(stages), dptr(out),
+                                                          dptr(ws), ws.numel(), stream_ptr()),
+                   "xt_sph_accumulate_batched_tc")
+        return out
+
+    def batched_tc_workspace(self, offsets, chunk=16384):
+        offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        return int(self._lib.xt_sph_batched_tc_workspace(self.handle, offs.size - 1, offs.ctypes.data, int(chunk)))
+
     def prepare(self, expcoef, coef_scale=1.0, lmax_use=-1, nmax_use=-1, precision="f64"):
         pc = precision_code(precision)
         nbytes = self._lib.xt_sph_field_bytes(self.handle, pc)
@@ -294,6 +322,7 @@ class CylTable:
         self._lib = lib
         self.field_cache = _Cache(limit=8)
         self._fused_bufs = threading.local()
+        self._sorted_ws = threading.local()
 
     def __del__(self):
         try:
@@ -371,14 +400,61 @@ class CylTable:
                                                     ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return coef, res[:5]
 
+    def sorted_ok(self):
+        """Whether the table fits the sorted pipeline (mmax <= 8, norder <= 24,
+        numx * numy <= 2^20 cells)."""
+        return self.mmax <= 8 and self.norder <= 24 and self.numx * self.numy <= (1 << 20)
+
+    def _sorted_workspace(self, n, pc):
+        """Per-thread device workspace of the sorted calls, grown as needed."""
+        need = self._lib.xt_cyl_accumulate_eval_workspace(self.handle, n, pc)
+        ws = getattr(self._sorted_ws, "v", None)
+        if ws is None or ws.numel() < need:
+            ws = torch.empty(need, dtype=torch.uint8, device=device())
+            self._sorted_ws.v = ws
+        return ws
+
+    def accumulate_sorted(self, x, y, z, m, precision="f64", nan_to_origin=True):
+        """Coefficients through the sorted pipeline (binning, counting sort by
+        cell, run-accumulated deposit, contraction): a (2, mmax+1, norder)
+        device tensor of cos and sin.  x, y, z, m as for accumulate_eval."""
+        n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
+        pc = precision_code(precision)
+        ws = self._sorted_workspace(n, pc)
+        coef = torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device())
+        _lib.check(self._lib.xt_cyl_accumulate_sorted(self.handle, _addr(x), _addr(y), _addr(z), _addr(m), n, pc,
+                                                      int(bool(nan_to_origin)), dptr(coef[0]), dptr(coef[1]),
+                                                      ws.data_ptr(), ws.numel(), stream_ptr()),
+                   "xt_cyl_accumulate_sorted")
+        return coef
+
+    def eval_sorted(self, x, y, z, cos, sin, precision="f64", m1=0, m2=1000, r_out=None):
+        """accumulated_eval_particles (no density) through the sorted pipeline
+        from device coefficients cos, sin ((mmax+1, norder) float64): a (6, n)
+        device tensor of p0, p, fr, fp, fz, R in particle order.  With
+        ``r_out`` (a length-n float64 tensor or a raw address, device or
+        page-locked host memory) R is written there by the binning kernel
+        instead of into row 5."""
+        n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
+        pc = precision_code(precision)
+        ws = self._sorted_workspace(n, pc)
+        res = torch.empty((6, n), dtype=torch.float64, device=device())
+        outs = (ctypes.c_void_p * 6)(*[res.data_ptr() + 8 * n * k for k in range(6)])
+        if r_out is not None:
+            outs[5] = _addr(r_out)
+        _lib.check(self._lib.xt_cyl_eval_sorted(self.handle, _addr(x), _addr(y), _addr(z), n, pc, int(m1), int(m2),
+                                                dptr(cos), dptr(sin), outs, ws.data_ptr(), ws.numel(), stream_ptr()),
+                   "xt_cyl_eval_sorted")
+        return res
+
     def prepare(self, cos, sin, mmax_use=-1, nmax_use=-1, density=False, precision="f64"):
         pc = precision_code(precision)
         nbytes = self._lib.xt_cyl_field_bytes(self.handle, int(bool(density)), pc)
         field = torch.empty(nbytes, dtype=torch.uint8, device=device())
         c = to_dev(np.asarray(cos, dtype=np.float64) if not isinstance(cos, torch.Tensor) else cos)
         s = to_dev(np.asarray(sin, dtype=np.float64) if not isinstance(sin, torch.Tensor) else sin)
-        c = _pad2(c, self.mmax + 1, self.norder)
-        s = _pad2(s, self.mmax + 1, self.norder)
+        c = pad2(c, self.mmax + 1, self.norder)
+        s = pad2(s, self.mmax + 1, self.norder)
         _lib.check(self._lib.xt_cyl_prepare(self.handle, dptr(c), dptr(s), int(mmax_use), int(nmax_use),
                                             int(bool(density)), pc, dptr(field), nbytes, stream_ptr()),
                    "xt_cyl_prepare")
@@ -397,7 +473,7 @@ class CylTable:
         return outs
 
 
-def _pad2(t, rows, cols):
+def pad2(t, rows, cols):
     """Zero-pad / crop a (r, c) coefficient tensor to (rows, cols)."""
     if t.shape == (rows, cols):
         return t.contiguous()
@@ -410,6 +486,13 @@ def _pad2(t, rows, cols):
 class CylField:
     def __init__(self, table, buf, precision, density):
         self.table, self.buf, self.precision, self.density = table, buf, precision, density
+
+
+def batched_tc_status():
+    """Raise XTError if a batched tensor-core launch reported an error (an
+    MMA wait that timed out, or a particle outside its sorted window);
+    synchronises the device."""
+    _lib.check(_lib.load().xt_sph_batched_tc_status(), "xt_sph_batched_tc_status")
 
 
 def fields_forces(sph_field, cyl_field, x, y, z, rotpos=None, rotpos_scalar=0.0, halo_l=-1, disk_m=-1,

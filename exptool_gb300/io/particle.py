@@ -1,13 +1,46 @@
 """Particle containers with the interface of ``exptool/io/particle.py``.
 
-``holder`` is the attribute container (``.xpos .ypos .zpos .mass`` ...,
-particle.py:142-157); ``ParticleData`` provides the ``.data`` dict of
-``particle.Input`` (keys x y z vx vy vz m potE) for in-memory arrays.  The
-snapshot readers are ``psp_io.Input`` and ``spl_io.Input``.
+``Input`` reads one component of an EXP snapshot, choosing the SPL or PSP
+reader from the file name (particle.py:17-106); ``holder`` is the attribute
+container (``.xpos .ypos .zpos .mass`` ..., particle.py:142-157);
+``ParticleData`` provides the ``.data`` dict of ``particle.Input`` (keys x y z
+vx vy vz m potE) for in-memory arrays.
 """
 from __future__ import annotations
 
 import numpy as np
+
+
+class Input:
+    """particle.Input (particle.py:66-106): ``SPL.`` in the file name selects
+    ``spl_io.Input``, every other name ``psp_io.Input`` (the reference's
+    ``elif 'OUT.':`` tests a non-empty string, so it never reaches its
+    'unknown' branch).  Exposes ``.header .filename .time``; with a component,
+    ``.comp`` and either ``.data`` or, with ``legacy=True``, the holder
+    attributes (``.id`` when the component is indexed).  ``device=True``
+    leaves the columns on the GPU as float64 CUDA tensors (no counterpart in
+    the reference)."""
+
+    def __init__(self, filename, comp=None, legacy=False, verbose=0, device=False):
+        from . import psp_io, spl_io
+        self.style = "SPL" if "SPL." in filename else "OUT"
+        reader = spl_io.Input if self.style == "SPL" else psp_io.Input
+        I = reader(filename, comp=comp, verbose=verbose, device=device)
+        self.header = I.header
+        self.filename = I.filename
+        self.time = I.time
+        if I.comp is None:
+            return
+        if legacy:
+            d = I.data
+            self.mass, self.xpos, self.ypos, self.zpos = d["m"], d["x"], d["y"], d["z"]
+            self.xvel, self.yvel, self.zvel, self.pote = d["vx"], d["vy"], d["vz"], d["potE"]
+            from .snapshot import _indexing
+            if _indexing(I.header[I.comp]):
+                self.id = d["id"]
+        else:
+            self.data = I.data
+        self.comp = I.comp
 
 
 class holder(object):

@@ -16,6 +16,14 @@ constructs them in the same spirit as EmpCylSL:
    defines, and written in the old-style 76-byte-header layout
    (``eof.py:163-181, 261-308``).
 
+Two engines build the same tables.  ``engine="gpu"`` (the default) evaluates
+every basis function at the sample and at the table nodes with one CUDA kernel
+per m (``xt_eof_basis``: Legendre recurrence, spline of u_nl(ln r), forces and
+density in FP64) and forms the second-moment matrix and the tabulation as FP64
+products on the device; only the small symmetric eigenproblems and the spline
+coefficients are computed on the host.  ``engine="numpy"`` is the host
+restatement, kept as the reference the GPU engine is tested against.
+
 Force tables hold forces (``rforce = -dPhi/dR``, ``zforce = -dPhi/dz``): the sign
 ``potential.Fields.return_forces_cart`` assumes (``potential.py:487-494``).  The
 angular factor is the same ``factorial_return`` normalisation the spherical code
@@ -121,7 +129,9 @@ class EOFTables:
 
     def __init__(self, mmax=6, norder=18, numx=256, numy=256, rmin=0.001, rmax=30.0,
                  ascale=1.0, hscale=0.1, cmap=1, lmax_sph=32, nmax_sph=14,
-                 nsample=100000, seed=12345, disc_h=0.1, disc_rmax=20.0, disc_zmax=2.0):
+                 nsample=100000, seed=12345, disc_h=0.1, disc_rmax=20.0, disc_zmax=2.0, engine="gpu"):
+        if engine not in ("gpu", "numpy"):
+            raise ValueError(f"engine must be 'gpu' or 'numpy', not {engine!r}")
         self.mmax, self.norder, self.numx, self.numy = mmax, norder, numx, numy
         self.rmin, self.rmax, self.ascale, self.hscale, self.cmap = rmin, rmax, ascale, hscale, cmap
         r_lo = 0.5 * rmin * ascale
@@ -139,28 +149,90 @@ class EOFTables:
         self.eigvals = np.zeros((mmax + 1, norder))
         nodes_R = RR.ravel()
         nodes_z = ZZ.ravel()
+        if engine == "gpu":
+            self._build_gpu(nodes_R, nodes_z, Rs, zs, lmax_sph, nsample)
+            return
         cache_nodes = self._radial_cache(nodes_R, nodes_z, lmax_sph)
         cache_samp = self._radial_cache(Rs, zs, lmax_sph)
         for m in range(mmax + 1):
             psi_s, _, _, _ = self._functions(m, cache_samp, lmax_sph, need_derivs=False)
             C = psi_s @ psi_s.T / nsample
-            w, V = np.linalg.eigh(C)
-            order = np.argsort(w)[::-1][:norder]
-            w = w[order]
-            V = V[:, order]
+            V = self._eigvecs(m, C)
             psi_n, dR_n, dz_n, rho_n = self._functions(m, cache_nodes, lmax_sph, need_derivs=True)
-            pot = V.T @ psi_n
-            for k in range(norder):
-                # deterministic sign: potential at the innermost midplane node negative
-                ref = pot[k].reshape(numx + 1, numy + 1)[:, (numy + 1) // 2]
-                j = int(np.argmax(np.abs(ref)))
-                if ref[j] > 0:
-                    V[:, k] = -V[:, k]
-            self.eigvals[m] = w
+            V = self._orient(V, V.T @ psi_n)
             self.pot[m] = (V.T @ psi_n).reshape(norder, numx + 1, numy + 1)
             self.rforce[m] = (-(V.T @ dR_n)).reshape(norder, numx + 1, numy + 1)
             self.zforce[m] = (-(V.T @ dz_n)).reshape(norder, numx + 1, numy + 1)
             self.dens[m] = (V.T @ rho_n).reshape(norder, numx + 1, numy + 1)
+
+    def _eigvecs(self, m, C):
+        """The norder leading eigenvectors of the second-moment matrix
+        (columns), eigenvalues kept in self.eigvals[m]."""
+        w, V = np.linalg.eigh(C)
+        order = np.argsort(w)[::-1][:self.norder]
+        self.eigvals[m] = w[order]
+        return V[:, order]
+
+    def _orient(self, V, pot):
+        """Deterministic sign: the potential of each EOF at the midplane node
+        of largest magnitude is negative."""
+        V = V.copy()
+        for k in range(self.norder):
+            ref = np.asarray(pot[k]).reshape(self.numx + 1, self.numy + 1)[:, (self.numy + 1) // 2]
+            j = int(np.argmax(np.abs(ref)))
+            if ref[j] > 0:
+                V[:, k] = -V[:, k]
+        return V
+
+    def _build_gpu(self, nodes_R, nodes_z, Rs, zs, lmax, nsample):
+        """Basis functions by the xt_eof_basis kernel, second moments and
+        tabulation as FP64 products on the device."""
+        import torch
+        from scipy.interpolate import CubicSpline
+        from .. import _lib, device as dev
+        lib = _lib.load()
+        sl = self.sl
+        knots = dev.to_dev(sl.t)
+        nseg = sl.t.size - 1
+        coef = np.empty((lmax + 1, nseg, sl.nmax, 4))
+        for l in range(lmax + 1):
+            coef[l] = np.transpose(CubicSpline(sl.t, sl.u[l], axis=1).c, (1, 2, 0))
+        coef_d = dev.to_dev(coef)
+        ise = dev.to_dev(1.0 / np.sqrt(sl.ev[:lmax + 1]))
+        se = dev.to_dev(np.sqrt(sl.ev[:lmax + 1]))
+
+        def points(R, z):
+            r = np.maximum(np.sqrt(R * R + z * z), sl.rmin)
+            return [dev.to_dev(a) for a in (R, z, sl.model.potential(r), sl.model.dpotential(r),
+                                             sl.model.density(r))]
+
+        P_n, P_s = points(nodes_R, nodes_z), points(Rs, zs)
+        norder, nx, ny = self.norder, self.numx + 1, self.numy + 1
+
+        def basis(m, P, derivs):
+            nf = ((lmax - m) // 2 + 1) * sl.nmax
+            npt = P[0].numel()
+            outs = [torch.empty((nf, npt), dtype=torch.float64, device=P[0].device) for _ in range(4 if derivs else 1)]
+            ptr = [dev.dptr(o) for o in outs] + [None] * (4 - len(outs))
+            _lib.check(lib.xt_eof_basis(m, lmax, sl.nmax, nseg, dev.dptr(knots), dev.dptr(coef_d), dev.dptr(ise),
+                                        dev.dptr(se), *(dev.dptr(a) for a in P), float(sl.rmin), npt,
+                                        int(bool(derivs)), *ptr, dev.stream_ptr()), "xt_eof_basis")
+            return outs
+
+        for m in range(self.mmax + 1):
+            (psi_s,) = basis(m, P_s, False)
+            C = dev.to_host(psi_s @ psi_s.T / nsample)
+            del psi_s
+            V = self._eigvecs(m, C)
+            psi_n, dR_n, dz_n, rho_n = basis(m, P_n, True)
+            Vt = dev.to_dev(np.ascontiguousarray(V.T))
+            V = self._orient(V, dev.to_host(Vt @ psi_n))
+            Vt = dev.to_dev(np.ascontiguousarray(V.T))
+            self.pot[m] = dev.to_host(Vt @ psi_n).reshape(norder, nx, ny)
+            self.rforce[m] = (-dev.to_host(Vt @ dR_n)).reshape(norder, nx, ny)
+            self.zforce[m] = (-dev.to_host(Vt @ dz_n)).reshape(norder, nx, ny)
+            self.dens[m] = dev.to_host(Vt @ rho_n).reshape(norder, nx, ny)
+            del psi_n, dR_n, dz_n, rho_n
 
     def _radial_cache(self, R, z, lmax):
         r = np.sqrt(R * R + z * z)

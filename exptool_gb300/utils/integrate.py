@@ -386,3 +386,68 @@ def read_integrations(infile):
 def read_integrations_3D(infile):
     """integrate.read_integrations_3D (integrate.py:1001-1038)."""
     return _read_lines(infile, ["R_0", "V_0", "Z_0", "VZ_0", "dT"], ["X", "Y", "Z", "TX", "TY", "VX", "VY", "VZ"])
+
+
+# ---------------------------------------------------------------- snapshot -> orbit grid driver
+def run_time_mod(simulation_directory, simulation_name, eof_file, sph_file, model_file, intime, rads, vels, nint, dt,
+                 no_odd, halo_l, max_m, dyn_res, ap_max, verbose, nprocs=-1, omegap=-1., orbitfile='',
+                 transform=False, save_field=True, field_file_name='', field_file=None, bar_file='', fileprefix='OUT',
+                 threedee=False, zs=None, vzs=None, launch='x'):
+    """integrate.run_time_mod (integrate.py:638-758): the Fields of snapshot
+    ``intime`` (potential.get_fields, or potential.restore_field of
+    ``field_file_name`` when ``field_file`` is given, as the reference reads
+    the name rather than the argument), optionally saved with save_field
+    (default name 'field_file' in the working directory), then an orbit grid
+    by do_integrate_multi written with print_orbit_array(_3D) to
+    ``orbitfile`` or ``simulation_directory + 'omap_<intime>.txt'``
+    ('omap_3D_<intime>.txt' in 3D).  The grid rotates with frequency
+    -|omegap| / 2 pi when omegap >= 0, else 0.  transform=True (bar frame,
+    exptool.analysis.pattern) is outside this package: NotImplementedError
+    (after the reference's own missing-bar-file message and return)."""
+    from ..basis import potential
+    if verbose:
+        print('exptool.integrate.run_time: in directory {}, run {} at output {}, with transform={}'
+              .format(simulation_directory, simulation_name, intime, transform))
+    if transform:
+        if bar_file == '':
+            print('error - no bar file supplied for transform')
+            return
+        raise NotImplementedError("run_time_mod(transform=True) needs the bar pattern of exptool.analysis.pattern")
+    patt = 0.
+    if field_file is None:
+        F, patt, rotfreq = potential.get_fields(simulation_directory, simulation_name, intime, eof_file, sph_file,
+                                                model_file, transform=transform, bar_file=bar_file,
+                                                fileprefix=fileprefix)
+        if save_field:
+            if str(field_file_name) != '':
+                F.save_field(str(field_file_name))
+            else:
+                print('saving field file with default name (field_file) to local directory')
+                F.save_field('field_file')
+    else:
+        print('field file supplied! File name:')
+        print(field_file_name)
+        F = potential.restore_field(str(field_file_name))
+    if omegap >= 0.:
+        patt = omegap
+    rotfreq = -1. * abs(patt / (2. * np.pi))
+    if not threedee:
+        print('launching from ', launch, ' axis')
+        OrbitArray = do_integrate_multi(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, max_m, dyn_res, ap_max,
+                                        verbose=verbose, nprocs=nprocs, launch=launch)
+        if orbitfile == '':
+            print('Saving 2D orbit')
+            orbitfile = simulation_directory + 'omap_' + str(intime) + '.txt'
+        with open(orbitfile, 'w') as f:
+            print_orbit_array(f, OrbitArray)
+        return
+    if (zs is None) or (vzs is None):
+        print('ERROR: 3D orbit specified, but no z or vz values passed!')
+        return
+    OrbitArray = do_integrate_multi(rads, vels, F, nint, dt, rotfreq, no_odd, halo_l, max_m, dyn_res, ap_max,
+                                    verbose=verbose, nprocs=nprocs, threedee=threedee, zs=zs, vzs=vzs, launch=launch)
+    if orbitfile == '':
+        print('Saving 3D orbit')
+        orbitfile = simulation_directory + 'omap_3D_' + str(intime) + '.txt'
+    with open(orbitfile, 'w') as f:
+        print_orbit_array_3D(f, OrbitArray)

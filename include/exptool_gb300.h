@@ -94,8 +94,9 @@ int xt_sph_accumulate(void *handle, const double *x, const double *y, const doub
  * until exit), so the call allocates nothing; inputs and the output are
  * still caller-owned device pointers.  Limit: (lmax+1)^2 * numr <= 262144
  * doubles, larger tables return XT_ERR_ARG.  The first call on each device
- * looks up the array's address (cudaGetSymbolAddress); make that first
- * call before any stream capture.  All calls share the one array, which
+ * looks up the array's address (cudaGetSymbolAddress), and so does the first
+ * call after the device's context changed (cudaDeviceReset); make those
+ * calls before any stream capture.  All calls share the one array, which
  * keeps the last call's contents (each call zeroes what it uses first), so
  * calls that overlap on the GPU (concurrent streams) race: serialise them. */
 int xt_sph_accumulate_noalloc(void *handle, const double *x, const double *y, const double *z,
@@ -133,6 +134,28 @@ size_t xt_sph_batched_workspace(void *handle, int nsnap, long long n_total, int 
 int xt_sph_accumulate_batched(void *handle, const float *xyzm, const long long *offsets_host, int nsnap,
                               int no_odd, int chunk, int threads, double *expcoef_out, void *workspace,
                               size_t workspace_bytes, void *stream);
+
+/* The batched accumulation above on the tensor cores, the same sums written
+ * as particles x basis-terms products: spheresl.compute_coefficients
+ * (spheresl.py:439-475, accumulation loop :598-654) for every snapshot of a
+ * time series.  Particles are counting-sorted by (snapshot, window of 127
+ * radial table intervals); for each window, D[node, row] = sum over particles
+ * of W^T[node, p] A[p, row] (W: the two interpolation weights -4 pi m plerp
+ * {x1, x2} of each particle; A: its angular basis values fact P_l^m
+ * {1, cos m phi, sin m phi}) runs as tcgen05 MMAs with BF16 operands and FP32
+ * accumulation in tensor memory (M = 128 nodes, N = rows padded to 16,
+ * K = particles); window partials are summed in FP64 and contracted with the
+ * radial tables in FP64.  Same arguments as xt_sph_accumulate_batched, with
+ * chunk = the most particles of one work item (>= 128) and stages = operand
+ * buffers in flight (2 or 3).  numr <= 8129, lmax <= 8, at most 2^31 - 1
+ * particles.  The workspace size depends on the snapshot sizes.
+ * xt_sph_batched_tc_status synchronises the device and reports (and clears)
+ * an error flag a launch set: XT_ERR_DEVICE, else XT_OK. */
+size_t xt_sph_batched_tc_workspace(void *handle, int nsnap, const long long *offsets_host, int chunk);
+int xt_sph_accumulate_batched_tc(void *handle, const float *xyzm, const long long *offsets_host, int nsnap,
+                                 int no_odd, int chunk, int stages, double *expcoef_out, void *workspace,
+                                 size_t workspace_bytes, void *stream);
+int xt_sph_batched_tc_status(void);
 
 /* --------------------------------------------------------------- cylindrical (EOF) */
 /* Upload EOF tables parsed by eof.parse_eof (eof.py:224-313); each table is
@@ -186,6 +209,25 @@ int xt_cyl_accumulate_eval(void *handle, const double *x, const double *y, const
                            long long n, int precision, int m1, int m2, int nan_to_origin, double *cos_out,
                            double *sin_out, double *const *outs, void *workspace, size_t workspace_bytes,
                            void *stream);
+
+/* The two halves of xt_cyl_accumulate_eval as separate calls, for the
+ * drop-in functions that the reference runs one at a time; workspace size from
+ * xt_cyl_accumulate_eval_workspace, the same limits (mmax <= 8, norder <= 24)
+ * and the same host-memory rules for x, y, z, m and outs.
+ * xt_cyl_accumulate_sorted: eof.accumulate / eof.compute_coefficients
+ * (eof.py:492-640, 1158-1260) by binning, counting sort by table cell,
+ * run-accumulated deposit and contraction into cos_out/sin_out.
+ * xt_cyl_eval_sorted: eof.accumulated_eval_particles / eof.compute_forces
+ * (eof.py:989-1144, 1263-1317) without density, for m1 <= m <= m2, from the
+ * coefficients cos_c/sin_c ((mmax+1) x norder, device): binning, counting
+ * sort, field and evaluation in cell order; outs = p0 p fr fp fz R (6 arrays
+ * of n, any may be NULL), results in particle order. */
+int xt_cyl_accumulate_sorted(void *handle, const double *x, const double *y, const double *z, const double *m,
+                             long long n, int precision, int nan_to_origin, double *cos_out, double *sin_out,
+                             void *workspace, size_t workspace_bytes, void *stream);
+int xt_cyl_eval_sorted(void *handle, const double *x, const double *y, const double *z, long long n, int precision,
+                       int m1, int m2, const double *cos_c, const double *sin_c, double *const *outs,
+                       void *workspace, size_t workspace_bytes, void *stream);
 
 /* Stage timing (diagnostics, no counterpart in the reference): with
  * xt_timing_enable(1), xt_cyl_accumulate_eval records CUDA events on its
@@ -280,6 +322,23 @@ int xt_learned_radial_pass(void *sph, void *mlp, const void *prep, int K, double
 /* Synchronises, then reports (and clears) a tensor-memory pass that gave up
  * waiting for its MMAs: XT_ERR_DEVICE, else XT_OK. */
 int xt_learned_status(void);
+
+/* --------------------------------------------------------------- table generation */
+/* Basis functions of the cylindrical EOF construction at npt points (R, z),
+ * for azimuthal order m: psi = Phi_nl Y_lm and, with derivs != 0,
+ * dpsi/dR, dpsi/dz and rho_nl Y_lm, for l = m, m+2, ..., lmax and n < nmax
+ * (function index ((l - m) / 2) * nmax + n; outputs [nfunc][npt] FP64, device).
+ * No counterpart in the reference, which reads EOF caches but cannot make
+ * them (exptool/basis/eof.py:94-95); the Y_lm normalisation is its
+ * factorial_return (spheresl.py:823-863).  Radial functions from the cubic
+ * spline of u_nl(t = ln r): knots [nseg+1], coef [lmax+1][nseg][nmax][4]
+ * (descending powers of t - knot), Phi_nl = u Phi0 inv_sqrt_ev,
+ * rho_nl = u rho0 sqrt_ev ([lmax+1][nmax] each); phi0, dphi0, rho0: the
+ * background model at r = max(sqrt(R^2 + z^2), rmin).  All arrays device. */
+int xt_eof_basis(int m, int lmax, int nmax, int nseg, const double *knots, const double *coef,
+                 const double *inv_sqrt_ev, const double *sqrt_ev, const double *R, const double *z,
+                 const double *phi0, const double *dphi0, const double *rho0, double rmin, long long npt, int derivs,
+                 double *psi, double *dR, double *dz, double *rho, void *stream);
 
 /* --------------------------------------------------------------- snapshot records */
 /* Column kinds of xt_records_to_columns: source field -> column element. */

@@ -2,7 +2,14 @@
 reference (imported from its source tree through ``refshim``) on small,
 seeded inputs.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root, naming the exptool source tree root (the
+directory holding the ``exptool`` package):
+
+  python tests/golden/make_golden.py --reference <root> [snapshots | run_time]
+
+or set EXPTOOL_REFERENCE instead of --reference.  ``snapshots`` makes only the
+snapshot-reader, coefficient-file and orbit-frequency fixtures, ``run_time``
+only run_time.npz.
 
 Outputs (all small):
   sl_c{0,1,2}.cache / .model  SL basis tables (reference file formats)
@@ -15,6 +22,8 @@ Outputs (all small):
                               print_orbit_array(_3D) text of the reference
   centering.npz               Fields.total_coefficients centring (centres and the
                               centred particles handed to the accumulators)
+  run_time.npz                Fields.total_coefficients() reading a PSP snapshot,
+                              get_fields and run_time_mod (orbit text, field file)
   coef_files.npz              bytes of SL / EOF coefficient files written by the
                               reference (two dumps each), the SHA-256 and size of
                               a Fields.save_field file, rotation_curve and
@@ -567,10 +576,71 @@ def frequencies_case(ref):
     np.savez_compressed(P("frequencies.npz"), **out)
 
 
-def main(only_snapshots=False):
+def run_time_case(ref):
+    """potential.Fields.total_coefficients() reading its snapshot file itself
+    (components 'star' and 'dark' through the reference's particle.Input and
+    psp_io; yaml.safe_load supplied by exptool_gb300.io.yaml_lite), with and
+    without centring; potential.get_fields; and integrate.run_time_mod, whose
+    orbit text file and saved field are recorded.  eof.compute_coefficients
+    goes through refshim shim 5 (numpy 2)."""
+    import hashlib
+    import tempfile
+    import types
+    import run_time_input
+    from exptool_gb300.io import coefficients, yaml_lite
+    shim = types.ModuleType("yaml")
+    shim.safe_load = yaml_lite.load
+    sys.modules["yaml"] = shim
+    from exptool.io import psp_io, spl_io
+    psp_io.yaml = spl_io.yaml = shim
+    keep = refshim.patch_eof_compute_coefficients(ref)
+    refshim.set_log_bounds(ref, 1e-3, 100.0)
+    eof_path, cache, model = P("eof_c1.cache"), P("sl_c2.cache"), P("sl_c2.model")
+    out = {}
+    try:
+        with tempfile.TemporaryDirectory() as d:
+            d = d + "/"
+            infile = d + "OUT.run0.00003"
+            run_time_input.write_snapshot(infile)
+            out["snapshot_sha256"] = np.array(hashlib.sha256(open(infile, "rb").read()).hexdigest())
+            for tag, centering, mutual in (("plain", False, False), ("separate", True, False)):
+                F = ref.potential.Fields(infile, eof_path, cache, model, centering=centering,
+                                         mutual_center=mutual, verbose=0)
+                F.total_coefficients()
+                out[tag + "_cos"], out[tag + "_sin"] = (np.array(F.EOF.cos, dtype=np.float64), np.array(F.EOF.sin, dtype=np.float64))
+                out[tag + "_expcoef"] = np.array(F.SL.expcoef, dtype=np.float64)
+                out[tag + "_meta"] = np.array([F.time, F.halofac, F.xcen_disk, F.ycen_disk, F.zcen_disk,
+                                               F.xcen_halo, F.ycen_halo, F.zcen_halo], dtype=np.float64)
+            F, patt, rotfreq = ref.potential.get_fields(d, "run0", 3, eof_path, cache, model, transform=False)
+            out["get_fields_cos"], out["get_fields_sin"] = (np.array(F.EOF.cos, dtype=np.float64), np.array(F.EOF.sin, dtype=np.float64))
+            out["get_fields_expcoef"] = np.array(F.SL.expcoef, dtype=np.float64)
+            out["get_fields_meta"] = np.array([patt, rotfreq, F.time, F.halofac, F.xcen_disk, F.ycen_disk,
+                                               F.zcen_disk, F.xcen_halo, F.ycen_halo, F.zcen_halo])
+            g = run_time_input.GRID
+            ref.integrate.run_time_mod(d, "run0", eof_path, cache, model, 3, g["rads"], g["vels"], g["nint"],
+                                       g["dt"], False, -1, -1, 100., 1000, 0, nprocs=2, omegap=g["omegap"],
+                                       orbitfile=d + "omap.txt", save_field=True, field_file_name=d + "field.dat")
+            out["omap_text"] = np.array(open(d + "omap.txt").read())
+            rec = coefficients.read_field_record(d + "field.dat")
+            out["field_size"] = np.int64(os.path.getsize(d + "field.dat"))
+            for k in ("cos", "sin", "expcoef", "eof_f", "sl_f", "eof_i", "sl_i", "flags", "time"):
+                out["field_" + k] = np.asarray(rec[k])
+            # file names only: the recorded paths are those of the machine that ran this
+            out["field_files"] = np.array([os.path.basename(bytes(v).decode().rstrip("\x00")) for v in rec["files"]])
+    finally:
+        ref.eof.compute_coefficients = keep
+    np.savez_compressed(P("run_time.npz"), **out)
+    print("run_time done")
+
+
+def main(only_snapshots=False, only_run_time=False, reference=None):
     """All fixtures, or (argument ``snapshots``) only the snapshot-reader,
-    coefficient-file and orbit-frequency ones."""
-    ref = refshim.load()
+    coefficient-file and orbit-frequency ones, or (``run_time``) only
+    run_time.npz."""
+    ref = refshim.load(reference)
+    if only_run_time:
+        run_time_case(ref)
+        return
     snapshot_case()
     outcoef_case(ref)
     frequencies_case(ref)
@@ -590,4 +660,9 @@ def main(only_snapshots=False):
 
 
 if __name__ == "__main__":
-    main(only_snapshots=sys.argv[1:] == ["snapshots"])
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="exptool source tree root (default: $EXPTOOL_REFERENCE)")
+    ap.add_argument("which", nargs="?", choices=["all", "snapshots", "run_time"], default="all")
+    a = ap.parse_args()
+    main(only_snapshots=a.which == "snapshots", only_run_time=a.which == "run_time", reference=a.reference)

@@ -18,12 +18,15 @@ Shims (each one names the reference line it works around):
 """
 from __future__ import annotations
 
+import os
 import sys
 import types
 
 import numpy as np
 
-REF_ROOT = "/root/reference"
+# root of the exptool source tree (the directory holding the ``exptool``
+# package): EXPTOOL_REFERENCE, or the argument of load()
+REF_ROOT = os.environ.get("EXPTOOL_REFERENCE", "")
 
 
 class _Stub(types.ModuleType):
@@ -36,10 +39,15 @@ class _Stub(types.ModuleType):
         return _Stub("call")
 
 
-def load():
+def load(root=None):
+    """Import the reference from ``root`` (default: the EXPTOOL_REFERENCE
+    environment variable) with the shims above; returns its modules."""
+    root = root or REF_ROOT
+    if not root or not os.path.isdir(os.path.join(root, "exptool")):
+        raise RuntimeError("set EXPTOOL_REFERENCE (or pass --reference) to the exptool source tree root")
     sys.dont_write_bytecode = True
-    if REF_ROOT not in sys.path:
-        sys.path.insert(0, REF_ROOT)
+    if root not in sys.path:
+        sys.path.insert(0, root)
     for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.cm", "matplotlib.colors",
                  "matplotlib.colorbar", "yaml", "mpl_toolkits", "mpl_toolkits.mplot3d"]:
         sys.modules.setdefault(name, _Stub(name))
@@ -81,3 +89,42 @@ def set_log_bounds(ref, rmin, rmax):
     """Shim 4: the cmap=2 clamps read module globals xmin/xmax."""
     ref.spheresl.xmin = float(np.log(rmin))
     ref.spheresl.xmax = float(np.log(rmax))
+
+
+def patch_eof_compute_coefficients(ref):
+    """Shim 5: eof.compute_coefficients tests ``if nanvals > 0`` on an index
+    array (eof.py:1194), which numpy 2 refuses for an empty array.  The
+    replacement takes the function's own steps with that test written
+    ``nanvals.size > 0``: the EOF_Object fields of eof.py:1207-1216 and
+    :1250-1251, the tables through the reference's parse_eof / eof_params /
+    set_table_params, and the coefficients from its single-process
+    ``accumulate`` branch (eof.py:1236-1243)."""
+    eof = ref.eof
+
+    def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max=-1, VAR=False,
+                             nanblock=False):
+        d = PSPInput.data
+        nanvals = np.where(np.isnan(d['x']) | np.isnan(d['y']) | np.isnan(d['z']))[0]
+        if nanvals.size > 0 and not nanblock:
+            d['x'][nanvals] = 0.
+            d['y'][nanvals] = 0.
+            d['z'][nanvals] = 0.
+        out = eof.EOF_Object()
+        out.time = PSPInput.time
+        out.filename = PSPInput.filename
+        out.comp = PSPInput.comp
+        out.nbodies = d['m'].size
+        out.eof_file = eof_file
+        potC, rforceC, zforceC, densC, potS, rforceS, zforceS, densS = eof.parse_eof(eof_file)
+        rmin, rmax, numx, numy, mmax, norder, ascale, hscale, cmap, dens = eof.eof_params(eof_file)
+        XMIN, XMAX, dX, YMIN, YMAX, dY = eof.set_table_params(RMAX=rmax, RMIN=rmin, ASCALE=ascale, HSCALE=hscale,
+                                                              NUMX=numx, NUMY=numy, CMAP=cmap)
+        out.mmax = mmax
+        out.nmax = norder
+        out.cos, out.sin = eof.accumulate(PSPInput, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy, ascale,
+                                          hscale, cmap, verbose=verbose, no_odd=no_odd)
+        return out
+
+    keep = eof.compute_coefficients
+    eof.compute_coefficients = compute_coefficients
+    return keep

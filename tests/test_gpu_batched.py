@@ -74,3 +74,63 @@ def test_batched_vs_fp64_per_snapshot(l6_table, tmp_path, monkeypatch):
         if sizes[i]:
             assert norm_err(again[i], got[i]) < 2e-6
     assert torch.cuda.is_available()
+
+
+def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch):
+    """Tensor-core engine (tcgen05, BF16 operands, FP32 accumulation in tensor
+    memory, FP64 window sums and contraction) against the FP64 single-snapshot
+    path on the same FP32-rounded particles, and against the oracle on a small
+    snapshot.  BF16 rounds each operand to 2^-9 relative, so one particle's
+    contribution carries up to ~4e-3 relative error: normwise <= 5e-3 for any
+    snapshot, and <= 5e-4 for snapshots of 1e4 particles or more, where the
+    independent roundings average out.  Empty and one-particle snapshots,
+    work items of several K-tiles, both stage counts and repeated calls
+    (the operand tiles keep the last call's contents) are covered; the
+    kernels' error flag stays clear."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import spheresl
+    from exptool_gb300.tables.samplers import hernquist_sample
+    from oracle import sl as osl
+    monkeypatch.setenv("XT_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    cache, model = l6_table
+    sizes = [10000, 3000, 250000, 77777, 1, 0, 120000, 40000]
+    snaps = [hernquist_sample(n, 700 + i) for i, n in enumerate(sizes)]
+    xyzm = np.concatenate([np.stack(s, axis=1) for s in snaps], axis=0).astype(np.float32)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    table = spheresl.table_from_files(cache, model)
+    xd = torch.from_numpy(xyzm).cuda().contiguous()
+    refs = []
+    for i in range(len(sizes)):
+        blk = xd[int(offs[i]):int(offs[i + 1])].double()
+        refs.append(dev.to_host(table.accumulate(*(blk[:, k].contiguous() for k in range(4)))) if sizes[i] else None)
+    results = []
+    for chunk, stages in ((16384, 2), (512, 3), (128, 2)):
+        got = dev.to_host(table.accumulate_batched_tc(xd, offs, chunk=chunk, stages=stages))
+        dev.batched_tc_status()
+        results.append(got)
+        for i, n in enumerate(sizes):
+            if n == 0:
+                assert not np.any(got[i]), (chunk, i)
+                continue
+            e = norm_err(got[i], refs[i])
+            assert e <= 5e-3, (chunk, stages, i, e)
+            if n >= 10000:
+                assert e <= 5e-4, (chunk, stages, i, e)
+    # the same sums whatever the work-item size (FP32 order and BF16 operands alike)
+    for i, n in enumerate(sizes):
+        if n >= 10000:
+            assert norm_err(results[1][i], results[0][i]) <= 1e-5
+    # against the oracle on a small snapshot (FP32-rounded inputs)
+    t = osl.load_table(cache, model)
+    x, y, z, m = (xyzm[offs[1]:offs[2], k].astype(np.float64) for k in range(4))
+    assert norm_err(results[0][1], osl.compute_coefficients_solitary(x, y, z, m, t)) <= 5e-3
+    # the public entry point with autotuned item size and stages; no_odd zeroes odd-l rows
+    pub = spheresl.compute_coefficients_batched((xyzm, offs), cache, model, engine="tensor")
+    assert norm_err(pub[2], refs[2]) <= 5e-4
+    assert os.path.exists(tmp_path / "tune.json")
+    odd = spheresl.compute_coefficients_batched((xyzm, offs), cache, model, engine="tensor", no_odd=True,
+                                                autotune=False)
+    for l in (1, 3, 5):
+        assert not np.any(odd[:, l * l:(l + 1) * (l + 1)])
+    assert norm_err(odd[2][0:1], refs[2][0:1]) <= 5e-4

@@ -185,3 +185,45 @@ def test_disc_fused_nan_particles(disc):
     assert np.all(np.isfinite(E2.cos))
     for mm in range(t["mmax"] + 1):
         assert rel(E2.cos[mm], E.cos[mm]) <= 1e-11
+
+
+def test_sorted_calls_match_particle_order_calls(disc):
+    """The drop-in accumulate and evaluate run through the sorted pipeline
+    (xt_cyl_accumulate_sorted / xt_cyl_eval_sorted) where the table fits it;
+    the particle-order kernels (xt_cyl_accumulate, xt_cyl_eval_points) remain
+    for other tables.  Both agree on the full disc, from device and from
+    page-locked host particle arrays, for the full m range and m in [1, 2]."""
+    import torch
+    from exptool_gb300 import _lib, device as dev
+    from exptool_gb300.basis import eof
+    path, (x, y, z, m), t = disc
+    table = eof.table_from_file(path)
+    assert table.sorted_ok()
+    xd, yd, zd, md = (dev.to_dev(a) for a in (x, y, z, m))
+    c_po, s_po = table.accumulate(xd, yd, zd, md)
+    coef = table.accumulate_sorted(xd, yd, zd, md)
+    pinned = [torch.from_numpy(a).pin_memory() for a in (x, y, z, m)]
+    coef_h = table.accumulate_sorted(*pinned)
+    for mm in range(t["mmax"] + 1):
+        assert rel(coef[0, mm].cpu(), c_po[mm].cpu()) <= 1e-11, mm
+        assert rel(coef_h[0, mm].cpu(), c_po[mm].cpu()) <= 1e-11, mm
+        if mm:
+            assert rel(coef[1, mm].cpu(), s_po[mm].cpu()) <= 1e-11, mm
+    for m1, m2 in ((0, 1000), (1, 2)):
+        field = table.prepare(c_po, s_po)
+        want = table.eval_points(field, xd, yd, zd, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART,
+                                 m1=m1, m2=m2, want=[1, 1, 1, 1, 1, 1, 0, 0])
+        got = table.eval_sorted(xd, yd, zd, c_po, s_po, m1=m1, m2=m2)
+        got_h = table.eval_sorted(*pinned[:3], c_po, s_po, m1=m1, m2=m2)
+        for k in range(6):
+            assert rel(got[k].cpu(), want[k].cpu()) <= 1e-10, (m1, k)
+            assert torch.equal(got_h[k], got[k]), (m1, k)
+    # mixed precision through the sorted calls, against FP64
+    coef32 = table.accumulate_sorted(xd, yd, zd, md, precision="f32")
+    assert rel(coef32[0, 0].cpu(), c_po[0].cpu()) < 1e-5
+    r32 = table.eval_sorted(xd, yd, zd, c_po, s_po, precision="f32")
+    r64 = table.eval_sorted(xd, yd, zd, c_po, s_po)
+    F = torch.stack([r64[2], r64[4]])
+    G = torch.stack([r32[2], r32[4]])
+    err = (torch.linalg.norm(G - F, dim=0) / torch.linalg.norm(F, dim=0)).cpu().numpy()
+    assert np.median(err) < 1e-5

@@ -61,7 +61,7 @@ def test_host_readers_match_oracle():
 
 
 def test_eof_builder_roundtrip(tmp_path):
-    t = EOFTables(mmax=2, norder=3, numx=10, numy=10, lmax_sph=8, nmax_sph=6, nsample=5000)
+    t = EOFTables(mmax=2, norder=3, numx=10, numy=10, lmax_sph=8, nmax_sph=6, nsample=5000, engine="numpy")
     p = str(tmp_path / "eof.cache")
     t.write(p, dens=True)
     tabs = geof.parse_eof(p)
