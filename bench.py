@@ -55,6 +55,15 @@ STAGE_TRAFFIC_F64 = {
 }
 
 
+# FP32 (FMA) pipe activity and instructions per cycle of the FP64 launch of each
+# fused stage, from the same ncu capture: the double-float stages are bound by
+# FP32 issue, so the HBM fraction alone understates how busy they are
+STAGE_PIPE_F64 = {
+    "k_cyl_binrec": (51.9, 2.9), "k_cyl_scatter": (1.3, 0.16), "k_cyl_deposit_sorted": (38.5, 2.4),
+    "k_cyl_contract_partial+final": (37.0, 2.6), "k_cyl_field": (36.6, 2.5), "k_cyl_eval_sorted": (53.4, 2.5),
+}
+
+
 def cache_dir():
     d = os.environ.get("XT_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "xt_bench_tables"))
     os.makedirs(d, exist_ok=True)
@@ -673,7 +682,19 @@ def gpu_arm(args, rank, world):
                                        "launch at this workload (one launch)",
                      "bound_note": STAGE_TRAFFIC_F64[st_names[dom]][1],
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg64[dom],
-                     "launch_ms": round(float(stages64[dom]), 4)},
+                     "launch_ms": round(float(stages64[dom]), 4),
+                     "pipe": {"fma_pipe_active_pct": STAGE_PIPE_F64[st_names[dom]][0],
+                              "ipc_per_sm": STAGE_PIPE_F64[st_names[dom]][1], "ipc_max": 4,
+                              "source": "ncu --set full, FP64 launch at this workload "
+                                        "(profiles/cyl_fused_kernels_disc1e6.md)"}},
+        "rooflines_other": {
+            "config0_sph_eval_f64": "k_sph_eval<double,4>/<double,6>: FP64-pipe bound, 89 % FP64 pipe at lmax 6 "
+                                    "(profiles/sph_eval_f64_l6_1e6pts.md); deposit k_sph_deposit<double,4> 65 % "
+                                    "FP64 pipe (profiles/sph_deposit_f64_l4_halo1e5.md)",
+            "config2_leapfrog": "k_leapfrog<float,4>: L2-resident field gathers (99.6 % L2 hit, long-scoreboard "
+                                "stalls), FP64 kick/drift (profiles/leapfrog_orbits_65536x100.md)",
+            "config3_tensor_core": "k_sph_batched_tc: see batched_spherical.tensor_core and "
+                                   "profiles/sph_batched_tc_16snap.md"},
         "fused_stages": fused_stages,
         "separate_calls_f64": {"ms_per_step": stot64 / K, "value": world * N1 / (stot64 / K * 1e-3),
                                "what": "the drop-in eof.compute_coefficients + eof.compute_forces on device arrays: "
@@ -1052,7 +1073,8 @@ def profile_case(args):
     reader      a 1e6-particle PSP snapshot (double precision) read into device
                 columns (k_records_to_columns);
     batched_tc  the first 16 batched snapshots through the tensor-core engine
-                (k_bt_*, k_sph_batched_tc, k_bt_reduce);
+                (k_bt_*, k_sph_batched_tc, k_bt_reduce); batched_tc_full: all 256
+                (for launch lists only: 2.5 GB of particles, a ~4 GB workspace);
     eof_tables  a GPU EOF build (mmax 2, norder 6, 64^2 grid, lmax 16; k_eof_basis)."""
     import tempfile
     import torch
@@ -1107,12 +1129,12 @@ def profile_case(args):
         snapshot.write_psp(path, 0.0, {"star": comp}, float_len=8)
         for _ in range(reps):
             psp_io.Input(path, comp="star", device=True)
-    elif case == "batched_tc":
+    elif case in ("batched_tc", "batched_tc_full"):
         c6, m6 = sl6_table_paths()
         t6 = spheresl.table_from_files(c6, m6)
-        xyzm, offs = batched_snapshots(16)
+        xyzm, offs = batched_snapshots(16 if case == "batched_tc" else 256)
         for _ in range(reps):
-            t6.accumulate_batched_tc(xyzm, offs, chunk=16384, stages=2)
+            t6.accumulate_batched_tc(xyzm, offs, chunk=16384, stages=1)
         dev.batched_tc_status()
     elif case == "eof_tables":
         from exptool_gb300.tables.eof_builder import EOFTables
@@ -1141,7 +1163,7 @@ def main():
                     help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
                          "(a short, fixed launch sequence for ncu captures)")
     ap.add_argument("--profile-case", default=None,
-                    choices=["spherical", "orbits", "reader", "batched_tc", "eof_tables"],
+                    choices=["spherical", "orbits", "reader", "batched_tc", "batched_tc_full", "eof_tables"],
                     help="a short launch sequence of one workload for ncu captures (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:

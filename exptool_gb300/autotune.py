@@ -105,15 +105,15 @@ def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
     xt_sph_accumulate_batched_tc for this table, tuned on (up to) the first
     ``sample_snaps`` snapshots of the batch.  The tile shape itself is fixed
     by the table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16,
-    K = 128 particles per stage; stages = 2 lets two CTAs share an SM, 3
-    keeps one with a deeper pipeline."""
+    K = 128 particles per stage; with 1, 2 or 3 stages 4, 2 or 1 CTAs share
+    an SM (48 KB of shared memory per stage at lmax 6)."""
     import numpy as np
     offs = np.asarray(offsets, dtype=np.int64)
     ns = min(len(offs) - 1, sample_snaps)
     sub_offs = offs[:ns + 1]
     sub = xyzm[:int(sub_offs[-1])]
-    k = key("sph_batched_tc_v1", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
-    cands = [{"chunk": c, "stages": st} for c in (4096, 8192, 16384, 32768, 65536) for st in (2, 3)]
+    k = key("sph_batched_tc_v2", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
+    cands = [{"chunk": c, "stages": st} for c in (4096, 8192, 16384, 32768, 65536) for st in (1, 2, 3)]
     ws = {}
 
     def run(cfg):

@@ -22,6 +22,7 @@
 
 #include "xt_internal.cuh"
 #include "xt_launch.cuh"
+#include "xt_df.cuh"
 
 namespace xt {
 
@@ -116,38 +117,83 @@ __global__ void k_sph_batched(SphTab<float> T, const float4* __restrict__ xyzm, 
   }
 }
 
-// expcoef[s, row, n] = sum_i efp[l, n, i] * G[s, row, i]: one warp per output.
-__global__ void __launch_bounds__(256) k_sph_contract_batched(const double* __restrict__ efp,
-                                                              const double* __restrict__ G, int nsnap, int lmax,
-                                                              int nmax, int numr, double* __restrict__ out) {
-  const int nrow = (lmax + 1) * (lmax + 1);
-  const long long nout = (long long)nsnap * nrow * nmax;
-  const int lane = threadIdx.x & 31;
-  for (long long o = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; o < nout;
-       o += ((long long)gridDim.x * blockDim.x) >> 5) {
-    const int n = (int)(o % nmax);
-    const long long sr = o / nmax;
-    const int row = (int)(sr % nrow);
-    int l = 0;
-    while ((l + 1) * (l + 1) <= row) ++l;
-    const double* e = efp + ((size_t)l * nmax + n) * numr;
-    const double* g = G + (size_t)sr * numr;
-    double acc = 0.0;
-    for (int i = lane; i < numr; i += 32) acc += e[i] * g[i];
+// expcoef[s, row, n] = sum_node efp[l, n, node] G[s, row, node] in double-float
+// arithmetic on the FP32 pipe (the FP64 pipe of GB300 issues at a small
+// fraction of the FP32 rate).  One block per (snapshot, l): tiles of 256
+// nodes of the 2l+1 grid rows (split into FP32 pairs on loading) and of the
+// split table rows of this l are staged in shared memory, each thread keeps
+// lazily renormalised df sums for its outputs (row, n).  Error ~numr 2^-47 of
+// the sum of |terms|.
+constexpr int kCbTile = 256;
+constexpr int kCbPitch = kCbTile + 1;      // float2 pitch: rows of the table tile fall in distinct banks
+constexpr int kCbOut = 3;                  // outputs per thread: (2l+1) nmax <= 3 * 256
+
+__global__ void __launch_bounds__(256) k_sph_contract_batched_df(const float2* __restrict__ efp_df,
+                                                                 const double* __restrict__ G, int lmax, int nmax,
+                                                                 int numr, double* __restrict__ out) {
+  extern __shared__ float2 cb_sm[];
+  const int s = blockIdx.x, l = blockIdx.y;
+  const int nrow = (lmax + 1) * (lmax + 1), r0 = l * l, nr = 2 * l + 1;
+  const int nout = nr * nmax;
+  float2* Gt = cb_sm;                       // [nr][kCbPitch]
+  float2* Et = cb_sm + nr * kCbPitch;       // [nmax][kCbPitch]
+  const double* g = G + ((size_t)s * nrow + r0) * numr;
+  const float2* e = efp_df + (size_t)l * nmax * numr;
+  dacc acc[kCbOut];
+  for (int t0 = 0; t0 < numr; t0 += kCbTile) {
+    const int tn = min(kCbTile, numr - t0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nr * kCbTile; k += blockDim.x) {
+      const int r = k / kCbTile, j = k - r * kCbTile;
+      float2 v = make_float2(0.f, 0.f);
+      if (j < tn) {
+        const df d = df_from(g[(size_t)r * numr + t0 + j]);
+        v = make_float2(d.h, d.l);
+      }
+      Gt[r * kCbPitch + j] = v;
+    }
+    for (int k = threadIdx.x; k < nmax * kCbTile; k += blockDim.x) {
+      const int n = k / kCbTile, j = k - n * kCbTile;
+      Et[n * kCbPitch + j] = j < tn ? e[(size_t)n * numr + t0 + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) out[o] = acc;
+    for (int q = 0; q < kCbOut; ++q) {
+      const int o = threadIdx.x + q * blockDim.x;
+      if (o >= nout) break;
+      const int r = o / nmax, n = o - r * nmax;
+      const float2* gr = Gt + r * kCbPitch;
+      const float2* er = Et + n * kCbPitch;
+      for (int j = 0; j < tn; ++j) {
+        const float2 a = gr[j], b = er[j];
+        acc[q].fma(df{a.x, a.y}, df{b.x, b.y});
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kCbOut; ++q) {
+    const int o = threadIdx.x + q * blockDim.x;
+    if (o >= nout) break;
+    const int r = o / nmax, n = o - r * nmax;
+    out[((size_t)s * nrow + r0 + r) * nmax + n] = (double)acc[q].s + (double)acc[q].e;
   }
 }
 
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-int launch_sph_contract_batched(const double* efp, const double* G, int nsnap, int lmax, int nmax, int numr,
+int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
                                 double* out, cudaStream_t st) {
-  const long long nout = (long long)nsnap * (lmax + 1) * (lmax + 1) * nmax;
-  const int cgrid = (int)std::min<long long>((nout * 32 + 255) / 256, 152LL * 64);
-  k_sph_contract_batched<<<cgrid, 256, 0, st>>>(efp, G, nsnap, lmax, nmax, numr, out);
-  XT_CHECK_LAUNCH("k_sph_contract_batched");
+  XT_REQUIRE((2 * lmax + 1) * nmax <= kCbOut * 256, "the batched contraction supports (2 lmax + 1) nmax <= %d",
+             kCbOut * 256);
+  const size_t smem = (size_t)(2 * lmax + 1 + nmax) * kCbPitch * sizeof(float2);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    XT_CUDA(cudaFuncSetAttribute(k_sph_contract_batched_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
+  }
+  k_sph_contract_batched_df<<<dim3((unsigned)nsnap, (unsigned)(lmax + 1)), 256, smem, st>>>(efp_df, G, lmax, nmax,
+                                                                                          numr, out);
+  XT_CHECK_LAUNCH("k_sph_contract_batched_df");
   return XT_OK;
 }
 
@@ -245,9 +291,9 @@ int xt_sph_accumulate_batched(void* handle, const float* xyzm, const long long* 
     if (rc) return rc;
     XT_CHECK_LAUNCH("k_sph_batched");
   }
-  const double* efp = nullptr;
-  XT_REQUIRE(sph_efp(handle, &efp), "NULL table handle");
-  return launch_sph_contract_batched(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
+  const float2* efp_df = nullptr;
+  XT_REQUIRE(sph_efp_df(handle, &efp_df), "NULL table handle");
+  return launch_sph_contract_batched(efp_df, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
 }
 
 }  // extern "C"

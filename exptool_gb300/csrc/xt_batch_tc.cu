@@ -26,13 +26,14 @@
 //   3. k_bt_scatter: counting sort of the particles by (snapshot, window);
 //   4. k_sph_batched_tc: persistent; a CTA takes an item, builds the W^T and
 //      A tiles of 128 particles per K-tile in shared memory (one particle per
-//      thread, BF16, canonical K-major layout), one thread issues the MMAs
+//      thread, BF16; W^T K-major, A MN-major), one thread issues the MMAs
 //      and commits them to the stage's mbarrier while the next stage is
 //      built; at the item's end the accumulator (128 nodes x rows, FP32) is
 //      read from tensor memory into a per-item partial;
 //   5. k_bt_reduce: FP64 sum of the partials per (snapshot, row, node), in a
 //      fixed order (the window boundary node takes both windows' shares);
-//   6. k_sph_contract_batched: FP64 contraction with the radial tables.
+//   6. k_sph_contract_batched_df: contraction with the radial tables in
+//      double-float arithmetic (FP64-level accuracy on the FP32 pipe).
 // Waits are bounded: a timeout sets the error flag read by
 // xt_sph_batched_tc_status, waits once more for the MMAs in flight, frees the
 // tensor memory and returns.
@@ -93,18 +94,6 @@ __device__ __forceinline__ void bt_st(unsigned char* tile, int row, int k, float
 __device__ __forceinline__ float bt_radius(float4 q) {
   float r = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
   return (r >= 1.0e-10f) ? r : 1.0e-10f;
-}
-
-// Interpolation weights x1 plerp, x2 plerp of radius r on interval i (the
-// FP32 weights of sph_bins, spheresl.py:121-143, for a given interval; used
-// when the interval recomputed here differs from the one the sort stored).
-__device__ __noinline__ float2 bt_weights_at(const SphTab<float>& T, float r, int i) {
-  float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
-  if (T.cmap == 1) x = fminf(fmaxf(x, -1.f), 1.f - 1.0e-8f);
-  if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
-  const float x2 = (x - T.xi[i]) * T.inv_dxi, x1 = 1.f - x2;
-  const float plerp = x1 * T.p0[i] + x2 * T.p0[i + 1];
-  return make_float2(x1 * plerp, x2 * plerp);
 }
 
 // Interpolation interval of radius r: the node index of sph_bins
@@ -270,14 +259,59 @@ __global__ void __launch_bounds__(256) k_bt_scatter(const float4* __restrict__ x
 }
 
 // ------------------------------------------------------------------ tensor-core products
+// Operand tiles of one stage (K = 128 particles, one per thread):
+//  * the angular values A^T (N = NPAD rows x K particles) first, in the
+//    MN-major canonical layout: element (n, k) at (k >> 3) * BSK + (n >> 3) * 128
+//    + (k & 7) * 16 + (n & 7) * 2, so a thread stores 8 consecutive rows of its
+//    particle as one 16-byte word (conflict-free across the warp);
+//  * the weights W^T (M = 128 nodes x K particles) after it, K-major: element
+//    (node, k) at bt_off(node, k).
+// A wrongly read stride could only reach into the stage's own W^T tile: the
+// angular tile comes first.
+template <int NPAD>
+struct BtTile {
+  static constexpr int BSK = (NPAD / 8) * 128;        // bytes between 8-particle groups (K direction)
+  static constexpr int B_BYTES = NPAD * BT_KT * 2;
+  static constexpr int STAGE = B_BYTES + BT_A_BYTES;
+};
+
+// Associated Legendre P_l^m(x) by the recurrences of legendre() (spheresl.py:
+// 664-700) for a finite x in [-1, 1], where every value is finite.
+template <int LCAP>
+__device__ __forceinline__ void bt_legendre(float x, float* P) {
+  const float somx2 = sqrtf((1.f - x) * (1.f + x));
+  P[0] = 1.f;
+  float pll = 1.f, fact = 1.f;
+#pragma unroll
+  for (int m = 1; m <= LCAP; ++m) {
+    pll *= -fact * somx2;
+    P[tri(m, m)] = pll;
+    fact += 2.f;
+  }
+#pragma unroll
+  for (int m = 0; m < LCAP; ++m) {
+    float pl2 = P[tri(m, m)];
+    float pl1 = x * (float)(2 * m + 1) * pl2;
+    P[tri(m + 1, m)] = pl1;
+#pragma unroll
+    for (int l = m + 2; l <= LCAP; ++l) {
+      const float v = (x * (float)(2 * l - 1) * pl1 - (float)(l + m - 1) * pl2) * (1.f / (float)(l - m));
+      P[tri(l, m)] = v;
+      pl2 = pl1;
+      pl1 = v;
+    }
+  }
+}
+
 template <int LCAP, int NPAD, int STAGES>
 __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
-  constexpr int B_BYTES = NPAD * BT_KT * 2;
-  constexpr int STAGE_BYTES = BT_A_BYTES + B_BYTES;
+  using TL = BtTile<NPAD>;
   constexpr int NCOLS = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
   constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
+  constexpr int NROW = (LCAP + 1) * (LCAP + 1);
+  static_assert(NROW <= NPAD, "rows exceed the padded tile");
   extern __shared__ __align__(1024) unsigned char sm[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + STAGES * STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + STAGES * TL::STAGE);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + STAGES);
   int* s_item = reinterpret_cast<int*>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -291,17 +325,20 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid < STAGES) mbar_init(smem_u32(bars + tid));
-  // operand tiles start at zero: padded rows of A and the rows of W^T that no
+  // operand tiles start at zero: padded angular rows and the weight rows no
   // particle touches stay zero
-  for (int o = tid * 16; o < STAGES * STAGE_BYTES; o += BT_THREADS * 16)
+  for (int o = tid * 16; o < STAGES * TL::STAGE; o += BT_THREADS * 16)
     *reinterpret_cast<uint4*>(sm + o) = make_uint4(0u, 0u, 0u, 0u);
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t idesc = tc_idesc(BT_M, NPAD);
+  // kind::f16, D F32, A (weights) K-major, B (angular) MN-major (bit 16)
+  const uint32_t idesc = tc_idesc(BT_M, NPAD) | (1u << 16);
   const int nitems = *a.nitems;
+  // byte offset of this thread's angular column in a stage's angular tile
+  const int kofs = (tid >> 3) * TL::BSK + (tid & 7) * 16;
   int prev_row[STAGES];
 #pragma unroll
   for (int s = 0; s < STAGES; ++s) prev_row[s] = -1;
@@ -326,21 +363,72 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
     for (long long t = 0; t < ntile; ++t, ++g) {
       const float4 q = qn;
       const int i = in;
+      const bool have = I.begin + t * BT_KT + tid < I.end;
       const long long pn = I.begin + (t + 1) * BT_KT + tid;
       if (pn < I.end) {
         qn = a.sorted[pn];
         in = a.sidx[pn];
       }
+      // this particle's values, computed before its stage is free
+      uint32_t pk[NPAD / 2];
+#pragma unroll
+      for (int k = 0; k < NPAD / 2; ++k) pk[k] = 0u;
+      float w0 = 0.f, w1 = 0.f;
+      int li = -1;
+      if (have) {
+        const float r = bt_radius(q);
+        // interpolation weights on the stored interval (spheresl.py:121-143)
+        float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
+        if (T.cmap == 1) x = fminf(fmaxf(x, -1.f), 1.f - 1.0e-8f);
+        if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
+        const float x2 = (x - T.xi[i]) * T.inv_dxi, x1 = 1.f - x2;
+        const float plerp = x1 * T.p0[i] + x2 * T.p0[i + 1];
+        const float base = -BT_FOUR_PI * q.w * plerp;
+        w0 = x1 * base;
+        w1 = x2 * base;
+        li = i - wbase;
+        const float costh = q.z / r;
+        float c1, s1;
+        unit_phi(q.x, q.y, c1, s1);
+        float P[NT];
+        bt_legendre<LCAP>(costh, P);
+        float cm[LCAP + 1], sn[LCAP + 1];
+        multiples<float, LCAP>(c1, s1, LCAP, cm, sn);
+        float v[NPAD];
+#pragma unroll
+        for (int k = 0; k < NPAD; ++k) v[k] = 0.f;
+        // the normalisation fact[l][m] is applied in FP64 by k_bt_reduce: a
+        // BF16 rounding of it would bias every particle alike
+#pragma unroll
+        for (int l = 0; l <= LCAP; ++l) {
+          const bool on = l <= lmax && !(a.no_odd && (l & 1));   // rows of odd l stay zero under no_odd
+#pragma unroll
+          for (int m = 0; m <= l; ++m) {
+            const float pv = on ? P[tri(l, m)] : 0.f;
+            if (m == 0) {
+              v[l * l] = pv;
+            } else {
+              v[l * l + 2 * m - 1] = pv * cm[m];
+              v[l * l + 2 * m] = pv * sn[m];
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < NPAD / 2; ++k) {
+          __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+          pk[k] = *reinterpret_cast<uint32_t*>(&b2);
+        }
+      }
       const int st = (int)(g % STAGES);
-      unsigned char* At = sm + st * STAGE_BYTES;
-      unsigned char* Bt = At + BT_A_BYTES;
+      unsigned char* Bt = sm + st * TL::STAGE;
+      unsigned char* At = Bt + TL::B_BYTES;
       // the MMAs that last read this stage (K-tile g - STAGES) must be done
-      bool lf = g >= STAGES && !mbar_wait(smem_u32(bars + st), (uint32_t)(((g / STAGES) - 1) & 1));
+      bool lf = false;
+      if (tid == 0 && g >= STAGES) lf = !mbar_wait(smem_u32(bars + st), (uint32_t)(((g / STAGES) - 1) & 1));
       if (__syncthreads_or(lf)) {
         ok = false;
         break;
       }
-      // column `tid` of this stage: clear the weights the last particle here left
       int pr = -1;
 #pragma unroll
       for (int s = 0; s < STAGES; ++s)
@@ -350,53 +438,22 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
         *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr + 1, tid)) = __float2bfloat16_rn(0.f);
       }
       int nr = -1;
-      const long long p = I.begin + t * BT_KT + tid;
-      if (p < I.end) {
-        const float r = bt_radius(q);
-        const SphBins<float> B = sph_bins(T, r, false, false);
-        float2 lw = make_float2(B.lw0, B.lw1);
-        if (B.i != i) lw = bt_weights_at(T, r, i);
-        const int li = i - wbase;
+      if (have) {
         if (li >= 0 && li < BT_NODES) {
-          const float base = -BT_FOUR_PI * q.w;
-          bt_st(At, li, tid, lw.x * base);
-          bt_st(At, li + 1, tid, lw.y * base);
+          bt_st(At, li, tid, w0);
+          bt_st(At, li + 1, tid, w1);
           nr = li;
         } else {
           atomicExch(a.err, 3);
         }
-        const float costh = q.z / r;
-        float c1, s1;
-        unit_phi(q.x, q.y, c1, s1);
-        float P[NT];
-#pragma unroll
-        for (int k = 0; k < NT; ++k) P[k] = 0.f;
-        legendre<float, LCAP>(costh, lmax, P);
-        float cm[LCAP + 1], sn[LCAP + 1];
-        multiples<float, LCAP>(c1, s1, lmax, cm, sn);
-#pragma unroll
-        for (int l = 0; l <= LCAP; ++l) {
-          if (l > lmax) break;
-          if (a.no_odd && (l & 1)) continue;     // rows of odd l stay zero
-          const int loff = l * l;
-#pragma unroll
-          for (int m = 0; m <= l; ++m) {
-            // the normalisation fact[l][m] is applied in FP64 by k_bt_reduce:
-            // a BF16 rounding of it would be the same for every particle
-            const float v = P[tri(l, m)];
-            if (m == 0) {
-              bt_st(Bt, loff, tid, v);
-            } else {
-              bt_st(Bt, loff + 2 * m - 1, tid, v * cm[m]);
-              bt_st(Bt, loff + 2 * m, tid, v * sn[m]);
-            }
-          }
-        }
-      } else {
-        // no particle: a zero angular column (a stale non-finite value would
-        // survive the zero weights)
-        for (int row = 0; row < a.nrow; ++row) bt_st(Bt, row, tid, 0.f);
       }
+      // the angular column: (NROW + 7) / 8 chunks of 8 rows (rows past NROW are
+      // zero from the start and never written); zeros for a missing particle
+      // (a stale non-finite value would survive zero weights)
+#pragma unroll
+      for (int c = 0; c < (NROW + 7) / 8; ++c)
+        *reinterpret_cast<uint4*>(Bt + kofs + c * 128) =
+            make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
 #pragma unroll
       for (int s = 0; s < STAGES; ++s)
         if (s == st) prev_row[s] = nr;
@@ -408,15 +465,16 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
         const uint32_t ab = smem_u32(At), bb = smem_u32(Bt);
 #pragma unroll
         for (int kk = 0; kk < BT_KT / 16; ++kk)
-          tc_mma(tmem, tc_desc(ab + kk * 2 * BT_LBO, BT_LBO, BT_SBO), tc_desc(bb + kk * 2 * BT_LBO, BT_LBO, BT_SBO),
-                 idesc, (t > 0 || kk > 0) ? 1u : 0u);
+          tc_mma(tmem, tc_desc(ab + kk * 2 * BT_LBO, BT_LBO, BT_SBO),
+                 tc_desc(bb + kk * 2 * TL::BSK, TL::BSK, 128), idesc, (t > 0 || kk > 0) ? 1u : 0u);
         tc_commit(smem_u32(bars + st));
       }
     }
     if (!ok) break;
     // the item's sums: wait for its last MMAs, read the accumulator rows
     const int lst = (int)((g - 1) % STAGES);
-    const bool lf = !mbar_wait(smem_u32(bars + lst), (uint32_t)(((g - 1) / STAGES) & 1));
+    bool lf = false;
+    if (tid == 0) lf = !mbar_wait(smem_u32(bars + lst), (uint32_t)(((g - 1) / STAGES) & 1));
     if (__syncthreads_or(lf)) {
       ok = false;
       break;
@@ -439,7 +497,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
   }
   // after a wait gave up, the MMAs still in flight finish (bounded) before the
   // tensor memory is released
-  if (!ok && g > 0) mbar_wait(smem_u32(bars + (int)((g - 1) % STAGES)), (uint32_t)(((g - 1) / STAGES) & 1));
+  if (!ok && g > 0 && tid == 0) mbar_wait(smem_u32(bars + (int)((g - 1) % STAGES)), (uint32_t)(((g - 1) / STAGES) & 1));
   tc_fence_before();
   __syncthreads();
   if (tid == 0 && !ok) atomicExch(a.err, 1);
@@ -526,9 +584,12 @@ static long long bt_nchunk(const long long* off, int nsnap) {
 
 template <int LC, int NPAD, int STAGES>
 static int bt_launch_gemm(const BtArgs& A, cudaStream_t st) {
-  constexpr size_t smem = (size_t)STAGES * (BT_A_BYTES + NPAD * BT_KT * 2) + STAGES * 8 + 8;
+  constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
   auto kern = k_sph_batched_tc<LC, NPAD, STAGES>;
   XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // all of the unified L1/shared storage as shared memory, so that as many
+  // CTAs as fit are resident (the default carveout left one per SM)
+  XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
   XT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT_THREADS, smem));
   XT_REQUIRE(per_sm >= 1, "k_sph_batched_tc does not fit on an SM with %zu bytes of shared memory", smem);
@@ -562,7 +623,7 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
   XT_REQUIRE(sph_tabs(handle, &d, &f), "NULL table handle");
   XT_REQUIRE(nsnap > 0 && offsets_host && expcoef_out, "need nsnap > 0, host offsets and an output");
   XT_REQUIRE(chunk >= BT_KT && chunk <= (1 << 30), "chunk must be in [%d, 2^30] particles", BT_KT);
-  XT_REQUIRE(stages == 2 || stages == 3, "stages must be 2 or 3");
+  XT_REQUIRE(stages >= 1 && stages <= 3, "stages must be 1, 2 or 3");
   XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
   XT_REQUIRE(d.numr >= 2 && (d.numr - 2) / BT_NODES + 1 <= BT_MAXWIN, "numr must be in [2, %d]",
              BT_MAXWIN * BT_NODES + 1);
@@ -638,6 +699,7 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
     int rc = with_lcap(d.lmax, [&](auto lc) -> int {
       constexpr int LC = decltype(lc)::value;
       constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
+      if (stages == 1) return bt_launch_gemm<LC, NPAD, 1>(A, st);
       return stages == 2 ? bt_launch_gemm<LC, NPAD, 2>(A, st) : bt_launch_gemm<LC, NPAD, 3>(A, st);
     });
     if (rc) return rc;
@@ -646,9 +708,9 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
         A.partial, ifirst, d.fact, d.lmax, nsnap, nrow, d.numr, L.nwin, G);
     XT_CHECK_LAUNCH("k_bt_reduce");
   }
-  const double* efp = nullptr;
-  XT_REQUIRE(sph_efp(handle, &efp), "NULL table handle");
-  return launch_sph_contract_batched(efp, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
+  const float2* efp_df = nullptr;
+  XT_REQUIRE(sph_efp_df(handle, &efp_df), "NULL table handle");
+  return launch_sph_contract_batched(efp_df, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
 }
 
 int xt_sph_batched_tc_status(void) {

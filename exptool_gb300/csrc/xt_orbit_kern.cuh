@@ -118,9 +118,10 @@ __global__ void __launch_bounds__(128) k_leapfrog(SphTab<R> ST, const R* __restr
       x = x + (vx * dt) + (0.5 * fx * dt2);
       y = y + (vy * dt) + (0.5 * fy * dt2);
       z = z + (vz * dt) + (0.5 * fz * dt2);
-      const double rp = A.rotc * ((double)k * dt);
-      double srd, crd;
-      sincos(rp, &srd, &crd);
+      // rotation of the field frame (integrate.py:131); without rotation the
+      // angle is zero at every step and its FP64 sine and cosine are skipped
+      double srd = 0.0, crd = 1.0;
+      if (A.rotc != 0.0) sincos(A.rotc * ((double)k * dt), &srd, &crd);
       fields_point<R, LCAP>(ST, GH, CT, F, fo, (R)x, (R)y, (R)z, (R)crd, (R)srd, v);
       const double nfx = (double)v[0] + (double)v[1];
       const double nfy = (double)v[2] + (double)v[3];

@@ -105,6 +105,7 @@ struct SphHandle {
   // FP64 arrays
   double *xi = nullptr, *p0 = nullptr, *d0 = nullptr, *fact = nullptr, *rnode = nullptr;
   double *efp = nullptr, *efd = nullptr;   // [(L+1)][K][numr]
+  float2* efp_df = nullptr;                 // efp split into FP32 leading part and remainder
   // FP32 copies for the mixed path
   float *xi_f = nullptr, *p0_f = nullptr, *d0_f = nullptr, *fact_f = nullptr, *rnode_f = nullptr;
   SphTab<double> tab_d;
@@ -114,7 +115,7 @@ struct SphHandle {
 static void free_handle(SphHandle* h) {
   if (!h) return;
   void* ptrs[] = {h->xi, h->p0, h->d0, h->fact, h->efp, h->efd, h->xi_f, h->p0_f, h->d0_f, h->fact_f,
-                  h->rnode, h->rnode_f};
+                  h->rnode, h->rnode_f, h->efp_df};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -222,6 +223,13 @@ __global__ void __launch_bounds__(256) k_sph_field32(const double* __restrict__ 
     GA[t] = a;
     GD[t] = d;
   }
+}
+
+bool sph_efp_df(void* handle, const float2** efp_df) {
+  SphHandle* h = static_cast<SphHandle*>(handle);
+  if (!h) return false;
+  *efp_df = h->efp_df;
+  return true;
 }
 
 bool sph_efp(void* handle, const double** efp) {
@@ -374,6 +382,19 @@ int xt_sph_table_create(int lmax, int nmax, int numr, int cmap, double rmin, dou
       (rc = upload(&h->efd, efd.data(), efd.size()))) {
     free_handle(h);
     return rc;
+  }
+  // the same table as FP32 pairs (hi, lo = rounding of the remainder) for the
+  // double-float batched contraction
+  {
+    std::vector<float2> e2(efp.size());
+    for (size_t k = 0; k < efp.size(); ++k) {
+      const float hi = (float)efp[k];
+      e2[k] = make_float2(hi, (float)(efp[k] - (double)hi));
+    }
+    if ((rc = upload(&h->efp_df, e2.data(), e2.size()))) {
+      free_handle(h);
+      return rc;
+    }
   }
   // node radii xi_to_r(xi) (compatibility.py:54-62)
   std::vector<double> rn(numr);

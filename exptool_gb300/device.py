@@ -238,8 +238,8 @@ class SphTable:
         tcgen05 product of the interpolation weights and the angular basis
         values with FP32 accumulation, FP64 sums of the window partials and an
         FP64 contraction.  Arguments as for accumulate_batched; ``chunk`` is
-        the most particles of one work item, ``stages`` the operand buffers in
-        flight (2 or 3).  Returns a (nsnap, (lmax+1)^2, nmax) float64 tensor."""
+        the most particles of one work item, ``stages`` the operand buffers per
+        CTA (1 to 3).  Returns a (nsnap, (lmax+1)^2, nmax) float64 tensor."""
         offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
         nsnap = offs.size - 1
         if xyzm.dtype != torch.float32 or xyzm.dim() != 2 or xyzm.shape[1] != 4 or not xyzm.is_contiguous():

@@ -147,7 +147,7 @@ int xt_sph_accumulate_batched(void *handle, const float *xyzm, const long long *
  * K = particles); window partials are summed in FP64 and contracted with the
  * radial tables in FP64.  Same arguments as xt_sph_accumulate_batched, with
  * chunk = the most particles of one work item (>= 128) and stages = operand
- * buffers in flight (2 or 3).  numr <= 8129, lmax <= 8, at most 2^31 - 1
+ * buffers per CTA (1 to 3; fewer buffers let more CTAs share an SM).  numr <= 8129, lmax <= 8, at most 2^31 - 1
  * particles.  The workspace size depends on the snapshot sizes.
  * xt_sph_batched_tc_status synchronises the device and reports (and clears)
  * an error flag a launch set: XT_ERR_DEVICE, else XT_OK. */

@@ -84,7 +84,7 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
     contribution carries up to ~4e-3 relative error: normwise <= 5e-3 for any
     snapshot, and <= 5e-4 for snapshots of 1e4 particles or more, where the
     independent roundings average out.  Empty and one-particle snapshots,
-    work items of several K-tiles, both stage counts and repeated calls
+    work items of several K-tiles, every stage count and repeated calls
     (the operand tiles keep the last call's contents) are covered; the
     kernels' error flag stays clear."""
     import torch
@@ -105,7 +105,7 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
         blk = xd[int(offs[i]):int(offs[i + 1])].double()
         refs.append(dev.to_host(table.accumulate(*(blk[:, k].contiguous() for k in range(4)))) if sizes[i] else None)
     results = []
-    for chunk, stages in ((16384, 2), (512, 3), (128, 2)):
+    for chunk, stages in ((16384, 2), (512, 3), (128, 2), (4096, 1)):
         got = dev.to_host(table.accumulate_batched_tc(xd, offs, chunk=chunk, stages=stages))
         dev.batched_tc_status()
         results.append(got)
