@@ -196,12 +196,14 @@ def batched_tc_extra(table, xyzm, offs, K=5, fp64_ms=None, refs=None):
     ntot = int(offs[-1])
     cfg, tune_ms = at.sph_batched_tc_config(table, xyzm, offs)
     ws = torch.empty(table.batched_tc_workspace(offs, cfg["chunk"]), dtype=torch.uint8, device="cuda")
-    out = table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws)
+    out = table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"],
+                                      ctas_per_sm=cfg["ctas_per_sm"], workspace=ws)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(K):
-        table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws)
+        table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"],
+                                    ctas_per_sm=cfg["ctas_per_sm"], workspace=ws)
     e1.record()
     torch.cuda.synchronize()
     dev.batched_tc_status()
@@ -215,6 +217,7 @@ def batched_tc_extra(table, xyzm, offs, K=5, fp64_ms=None, refs=None):
         errs.append((float(np.max(np.abs(a - b)) / np.max(np.abs(b))), _block_err(a, b, table.lmax)))
     errs = np.array(errs)
     res = {"ms": ms, "particles_per_s": ntot / (ms * 1e-3), "autotuned": cfg,
+           "resident_ctas_per_sm": {st: table.batched_tc_residency(st) for st in (1, 2, 3)},
            "autotune_candidates_ms": {k: round(v, 3) for k, v in tune_ms.items()},
            "tile": "M = 128 radial nodes, N = 64 (49 rows), K = 128 particles per stage, BF16 in, FP32 in TMEM",
            "tensor_flop_per_particle": 2 * 128 * 64,
@@ -813,6 +816,21 @@ def frequencies_extra(no=16384, nt=2048, sample=512, order=4):
     t0 = time.perf_counter()
     fq.find_fundamental_frequency_map(O, order=order)
     t_gpu = time.perf_counter() - t0
+    # the kernel alone on resident signals (537 MB of x and vx: larger than L2)
+    xd = torch.from_numpy(X).cuda()
+    vd = torch.from_numpy(VX).cuda()
+    win = torch.from_numpy(np.hanning(nt)).cuda()
+    for _ in range(3):
+        fq.spectra_device(0, xd, vd, win, order)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        fq.spectra_device(0, xd, vd, win, order)
+    e1.record()
+    torch.cuda.synchronize()
+    k_ms = e0.elapsed_time(e1) / reps
+    del xd, vd
 
     def numpy_map(x, v):
         freq = np.fft.fftfreq(x.shape[0], d=T[1] - T[0])
@@ -830,7 +848,10 @@ def frequencies_extra(no=16384, nt=2048, sample=512, order=4):
     numpy_map(X[:, :sample], VX[:, :sample])
     t_np = (time.perf_counter() - t0) * no / sample
     return {"workload": f"{no} orbits x {nt} steps, fundamental frequencies (order {order}), host map in and out",
-            "gpu_s": t_gpu, "orbits_per_s": no / t_gpu, "numpy_vectorised_s_scaled": t_np,
+            "gpu_s": t_gpu, "orbits_per_s": no / t_gpu, "kernel_ms": k_ms,
+            "kernel_orbits_per_s": no / (k_ms * 1e-3),
+            "kernel_achieved_gbs": 2 * 8 * nt * no / (k_ms * 1e-3) / 1e9,
+            "numpy_vectorised_s_scaled": t_np,
             "numpy_sample_orbits": sample}
 
 
@@ -1075,7 +1096,10 @@ def profile_case(args):
     batched_tc  the first 16 batched snapshots through the tensor-core engine
                 (k_bt_*, k_sph_batched_tc, k_bt_reduce); batched_tc_full: all 256
                 (for launch lists only: 2.5 GB of particles, a ~4 GB workspace);
-    eof_tables  a GPU EOF build (mmax 2, norder 6, 64^2 grid, lmax 16; k_eof_basis)."""
+    eof_tables  a GPU EOF build (mmax 2, norder 6, 64^2 grid, lmax 16; k_eof_basis);
+    frequencies fundamental frequencies of 4096 orbits x 2048 steps (x and vx
+                resident, 134 MB), then of the same orbits over 1500 steps
+                (Bluestein) (k_orbit_spectra)."""
     import tempfile
     import torch
     from exptool_gb300 import _lib, device as dev
@@ -1140,6 +1164,19 @@ def profile_case(args):
         from exptool_gb300.tables.eof_builder import EOFTables
         for _ in range(reps):
             EOFTables(mmax=2, norder=6, numx=64, numy=64, lmax_sph=16, nmax_sph=10, nsample=50000, engine="gpu")
+    elif case == "frequencies":
+        from exptool_gb300.orbits import frequencies as fq
+        rng = np.random.default_rng(41)
+        T = np.arange(2048) * 0.01
+        w = 6.0 * (1.0 + 0.5 * rng.random((3, 4096)))
+        X = sum(a * np.cos(w[k] * T[:, None]) for k, a in enumerate((1.0, 0.45, 0.2)))
+        V = sum(-a * w[k] * np.sin(w[k] * T[:, None]) for k, a in enumerate((1.0, 0.45, 0.2)))
+        xd, vd = dev.to_dev(X), dev.to_dev(V)
+        win = dev.to_dev(np.hanning(2048))
+        for _ in range(reps):
+            fq.spectra_device(0, xd, vd, win, 4)
+        xs, vs = xd[:1500].contiguous(), vd[:1500].contiguous()
+        fq.spectra_device(0, xs, vs, dev.to_dev(np.hanning(1500)), 4)
     else:
         raise SystemExit(f"unknown profile case {case!r}")
     torch.cuda.synchronize()
@@ -1163,7 +1200,7 @@ def main():
                     help="run warm-up steps then one FP64 and one FP32 step of the headline workload and exit "
                          "(a short, fixed launch sequence for ncu captures)")
     ap.add_argument("--profile-case", default=None,
-                    choices=["spherical", "orbits", "reader", "batched_tc", "batched_tc_full", "eof_tables"],
+                    choices=["spherical", "orbits", "reader", "batched_tc", "batched_tc_full", "eof_tables", "frequencies"],
                     help="a short launch sequence of one workload for ncu captures (see profile_case)")
     args = ap.parse_args()
     if args.profile_case:

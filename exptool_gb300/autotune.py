@@ -101,19 +101,21 @@ def sph_batched_config(table, xyzm, offsets, force=False, sample_snaps=32):
 
 
 def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
-    """Work-item size (particles) and operand stages of
+    """Work-item size (particles), operand stages and CTAs per SM of
     xt_sph_accumulate_batched_tc for this table, tuned on (up to) the first
-    ``sample_snaps`` snapshots of the batch.  The tile shape itself is fixed
-    by the table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16,
-    K = 128 particles per stage; with 1, 2 or 3 stages 4, 2 or 1 CTAs share
-    an SM (48 KB of shared memory per stage at lmax 6)."""
+    ``sample_snaps`` snapshots of the batch.  The MMA tile is fixed by the
+    table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16, K = 128
+    particles per stage (48 KB of shared memory per stage at lmax 6); the
+    candidates are every chunk x depth x residency from one CTA per SM up to
+    as many as fit at that depth."""
     import numpy as np
     offs = np.asarray(offsets, dtype=np.int64)
     ns = min(len(offs) - 1, sample_snaps)
     sub_offs = offs[:ns + 1]
     sub = xyzm[:int(sub_offs[-1])]
-    k = key("sph_batched_tc_v2", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
-    cands = [{"chunk": c, "stages": st} for c in (4096, 8192, 16384, 32768, 65536) for st in (1, 2, 3)]
+    k = key("sph_batched_tc_v3", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
+    cands = [{"chunk": c, "stages": st, "ctas_per_sm": cp} for c in (4096, 8192, 16384, 32768, 65536)
+             for st in (1, 2, 3) for cp in range(1, table.batched_tc_residency(st) + 1)]
     ws = {}
 
     def run(cfg):
@@ -121,6 +123,7 @@ def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
         if ws.get("n", 0) < need:
             ws["t"] = torch.empty(need, dtype=torch.uint8, device=xyzm.device)
             ws["n"] = need
-        table.accumulate_batched_tc(sub, sub_offs, chunk=cfg["chunk"], stages=cfg["stages"], workspace=ws["t"])
+        table.accumulate_batched_tc(sub, sub_offs, chunk=cfg["chunk"], stages=cfg["stages"],
+                                    ctas_per_sm=cfg["ctas_per_sm"], workspace=ws["t"])
 
     return tune(k, cands, run, force=force)

@@ -158,10 +158,13 @@ def compute_coefficients_batched(snapshots, sph_file, mod_file, no_odd=False, au
                 from .. import autotune as at
                 cfg, _ = at.sph_batched_tc_config(table, xyzm, offsets)
             else:
-                cfg = {"chunk": 16384, "stages": 2}
+                cfg = {"chunk": 16384, "stages": 1, "ctas_per_sm": 0}
             chunk = cfg["chunk"] if chunk is None else chunk
             stages = cfg["stages"] if stages is None else stages
-        out = table.accumulate_batched_tc(xyzm, offsets, no_odd=no_odd, chunk=chunk, stages=stages)
+            ctas = cfg["ctas_per_sm"]
+        else:
+            ctas = 0
+        out = table.accumulate_batched_tc(xyzm, offsets, no_odd=no_odd, chunk=chunk, stages=stages, ctas_per_sm=ctas)
         host = dev.to_host(out)
         dev.batched_tc_status()
         return host

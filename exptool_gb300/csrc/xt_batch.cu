@@ -119,31 +119,52 @@ __global__ void k_sph_batched(SphTab<float> T, const float4* __restrict__ xyzm, 
 
 // expcoef[s, row, n] = sum_node efp[l, n, node] G[s, row, node] in double-float
 // arithmetic on the FP32 pipe (the FP64 pipe of GB300 issues at a small
-// fraction of the FP32 rate).  One block per (snapshot, l): tiles of 256
+// fraction of the FP32 rate).  One block per (snapshot, l): tiles of 128
 // nodes of the 2l+1 grid rows (split into FP32 pairs on loading) and of the
-// split table rows of this l are staged in shared memory, each thread keeps
-// lazily renormalised df sums for its outputs (row, n).  Error ~numr 2^-47 of
-// the sum of |terms|.
-constexpr int kCbTile = 256;
+// split table rows of this l are staged in shared memory.  The (2l+1) nmax
+// outputs share the 256 threads evenly: each output's nodes are split over
+// S = 256 / outputs slices (node j to slice j mod S), each slice keeping a
+// lazily renormalised df sum, and the slices are merged in shared memory at
+// the end (for 2l+1 = 13, nmax = 20, S = 1 and four threads take a second
+// output).  Error ~numr 2^-47 of the sum of |terms|.
+constexpr int kCbTile = 128;
 constexpr int kCbPitch = kCbTile + 1;      // float2 pitch: rows of the table tile fall in distinct banks
-constexpr int kCbOut = 3;                  // outputs per thread: (2l+1) nmax <= 3 * 256
+constexpr int kCbOut = 3;                  // outputs per thread when S = 1: (2l+1) nmax <= 3 * 256
+constexpr int kCbThreads = 256;
 
-__global__ void __launch_bounds__(256) k_sph_contract_batched_df(const float2* __restrict__ efp_df,
-                                                                 const double* __restrict__ G, int lmax, int nmax,
-                                                                 int numr, double* __restrict__ out) {
+__global__ void __launch_bounds__(kCbThreads) k_sph_contract_batched_df(const float2* __restrict__ efp_df,
+                                                                       const double* __restrict__ G, int lmax,
+                                                                       int nmax, int numr,
+                                                                       double* __restrict__ out) {
   extern __shared__ float2 cb_sm[];
+  __shared__ float2 red[kCbThreads];
   const int s = blockIdx.x, l = blockIdx.y;
   const int nrow = (lmax + 1) * (lmax + 1), r0 = l * l, nr = 2 * l + 1;
   const int nout = nr * nmax;
+  const int S = nout >= kCbThreads ? 1 : kCbThreads / nout;    // node slices per output
   float2* Gt = cb_sm;                       // [nr][kCbPitch]
   float2* Et = cb_sm + nr * kCbPitch;       // [nmax][kCbPitch]
   const double* g = G + ((size_t)s * nrow + r0) * numr;
   const float2* e = efp_df + (size_t)l * nmax * numr;
+  const int tid = threadIdx.x;
+  const int sl = tid % S, o0 = tid / S;     // slice and first output of this thread
   dacc acc[kCbOut];
+  // outputs o0 + q * (256 / S), as (row offset, order offset) into the tiles
+  int go[kCbOut], eo[kCbOut];
+  int nq = 0;
+#pragma unroll
+  for (int q = 0; q < kCbOut; ++q) {
+    const int o = o0 + q * (kCbThreads / S);
+    const bool have = o < nout && (q == 0 || S == 1);
+    const int r = have ? o / nmax : 0, n = have ? o - r * nmax : 0;
+    go[q] = r * kCbPitch;
+    eo[q] = n * kCbPitch;
+    if (have) nq = q + 1;
+  }
   for (int t0 = 0; t0 < numr; t0 += kCbTile) {
     const int tn = min(kCbTile, numr - t0);
     __syncthreads();
-    for (int k = threadIdx.x; k < nr * kCbTile; k += blockDim.x) {
+    for (int k = tid; k < nr * kCbTile; k += kCbThreads) {
       const int r = k / kCbTile, j = k - r * kCbTile;
       float2 v = make_float2(0.f, 0.f);
       if (j < tn) {
@@ -152,30 +173,53 @@ __global__ void __launch_bounds__(256) k_sph_contract_batched_df(const float2* _
       }
       Gt[r * kCbPitch + j] = v;
     }
-    for (int k = threadIdx.x; k < nmax * kCbTile; k += blockDim.x) {
+    for (int k = tid; k < nmax * kCbTile; k += kCbThreads) {
       const int n = k / kCbTile, j = k - n * kCbTile;
       Et[n * kCbPitch + j] = j < tn ? e[(size_t)n * numr + t0 + j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < kCbOut; ++q) {
-      const int o = threadIdx.x + q * blockDim.x;
-      if (o >= nout) break;
-      const int r = o / nmax, n = o - r * nmax;
-      const float2* gr = Gt + r * kCbPitch;
-      const float2* er = Et + n * kCbPitch;
+    if (nq == 1) {
+#pragma unroll 4
+      for (int j = sl; j < tn; j += S) {
+        const float2 a = Gt[go[0] + j], b = Et[eo[0] + j];
+        acc[0].fma(df{a.x, a.y}, df{b.x, b.y});
+      }
+    } else if (nq > 1) {
       for (int j = 0; j < tn; ++j) {
-        const float2 a = gr[j], b = er[j];
-        acc[q].fma(df{a.x, a.y}, df{b.x, b.y});
+#pragma unroll
+        for (int q = 0; q < kCbOut; ++q) {
+          if (q < nq) {
+            const float2 a = Gt[go[q] + j], b = Et[eo[q] + j];
+            acc[q].fma(df{a.x, a.y}, df{b.x, b.y});
+          }
+        }
       }
     }
   }
+  // merge the slices of each output (slice 0 adds the others' sums)
+  if (S > 1) {
+    __syncthreads();
+    red[tid] = make_float2(acc[0].s, acc[0].e);
+    __syncthreads();
+    if (sl == 0 && nq > 0) {
+      df v = acc[0].value();
+      for (int k = 1; k < S; ++k) {
+        const float2 w = red[tid + k];
+        v = df_add(v, df{w.x, w.y});
+      }
+      acc[0].s = v.h;
+      acc[0].e = v.l;
+    }
+  }
+  if (sl == 0) {
 #pragma unroll
-  for (int q = 0; q < kCbOut; ++q) {
-    const int o = threadIdx.x + q * blockDim.x;
-    if (o >= nout) break;
-    const int r = o / nmax, n = o - r * nmax;
-    out[((size_t)s * nrow + r0 + r) * nmax + n] = (double)acc[q].s + (double)acc[q].e;
+    for (int q = 0; q < kCbOut; ++q) {
+      if (q < nq) {
+        const int o = o0 + q * (kCbThreads / S);
+        const int r = o / nmax, n = o - r * nmax;
+        out[((size_t)s * nrow + r0 + r) * nmax + n] = (double)acc[q].s + (double)acc[q].e;
+      }
+    }
   }
 }
 
@@ -183,16 +227,16 @@ static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
                                 double* out, cudaStream_t st) {
-  XT_REQUIRE((2 * lmax + 1) * nmax <= kCbOut * 256, "the batched contraction supports (2 lmax + 1) nmax <= %d",
-             kCbOut * 256);
+  XT_REQUIRE((2 * lmax + 1) * nmax <= kCbOut * kCbThreads,
+             "the batched contraction supports (2 lmax + 1) nmax <= %d", kCbOut * kCbThreads);
   const size_t smem = (size_t)(2 * lmax + 1 + nmax) * kCbPitch * sizeof(float2);
   static size_t attr = 0;
   if (smem > 48 * 1024 && smem > attr) {
     XT_CUDA(cudaFuncSetAttribute(k_sph_contract_batched_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = smem;
   }
-  k_sph_contract_batched_df<<<dim3((unsigned)nsnap, (unsigned)(lmax + 1)), 256, smem, st>>>(efp_df, G, lmax, nmax,
-                                                                                          numr, out);
+  k_sph_contract_batched_df<<<dim3((unsigned)nsnap, (unsigned)(lmax + 1)), kCbThreads, smem, st>>>(
+      efp_df, G, lmax, nmax, numr, out);
   XT_CHECK_LAUNCH("k_sph_contract_batched_df");
   return XT_OK;
 }
@@ -275,9 +319,7 @@ int xt_sph_accumulate_batched(void* handle, const float* xyzm, const long long* 
     int rc = with_lcap(d.lmax, [&](auto lc) -> int {
       constexpr int LC = decltype(lc)::value;
       {
-        XT_CUDA(cudaFuncSetAttribute(k_sph_batched<LC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 0;
-        XT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sph_batched<LC>, threads, smem));
+        const int per_sm = resident_blocks_full_carveout((const void*)k_sph_batched<LC>, threads, smem);
         if (per_sm < 1) {
           set_error("k_sph_batched cannot run %d threads with %zu bytes of shared memory", threads, smem);
           return XT_ERR_ARG;

@@ -39,6 +39,7 @@
 // tensor memory and returns.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -507,34 +508,39 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
   }
 }
 
-// G[s, row, node] = fact[l][m] times the FP64 sum of the partials of the
-// windows holding the node, in item order.  Node 127 w (w >= 1) is lane 0 of
-// window w and lane 127 of window w - 1.
+// G[s, row, node] = fact[l][m] times the sum of the partials of the windows
+// holding the node, in item order.  Node 127 w (w >= 1) is lane 0 of window w
+// and lane 127 of window w - 1.  The FP32 partials are summed exactly into a
+// double-float (TwoSum on the FP32 pipe; GB300's FP64 pipe is slow) and
+// widened once.  One block per (snapshot, row), threads over the nodes.
 __global__ void __launch_bounds__(256) k_bt_reduce(const float* __restrict__ partial, const int* __restrict__ ifirst,
                                                    const double* __restrict__ fact, int lmax, int nsnap, int nrow,
                                                    int numr, int nwin, double* __restrict__ G) {
-  const long long total = (long long)nsnap * nrow * numr;
-  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
-       o += (long long)gridDim.x * blockDim.x) {
-    const int node = (int)(o % numr);
-    const long long sr = o / numr;
+  for (long long sr = blockIdx.x; sr < (long long)nsnap * nrow; sr += gridDim.x) {
     const int row = (int)(sr % nrow), s = (int)(sr / nrow);
-    const int w = node / BT_NODES, lane = node - w * BT_NODES;
-    double acc = 0.0;
-    if (w < nwin) {
-      const int b = s * nwin + w;
-      for (int it = ifirst[b]; it < ifirst[b + 1]; ++it)
-        acc += (double)partial[((size_t)it * nrow + row) * BT_M + lane];
-    }
-    if (lane == 0 && w >= 1) {
-      const int b = s * nwin + w - 1;
-      for (int it = ifirst[b]; it < ifirst[b + 1]; ++it)
-        acc += (double)partial[((size_t)it * nrow + row) * BT_M + BT_NODES];
-    }
     int l = 0;
     while ((l + 1) * (l + 1) <= row) ++l;
     const int m = (row - l * l + 1) >> 1;            // row l^2 (m = 0), l^2 + 2m - 1 (cos), l^2 + 2m (sin)
-    G[o] = fact[l * (lmax + 1) + m] * acc;
+    const double f = fact[l * (lmax + 1) + m];
+    for (int node = threadIdx.x; node < numr; node += blockDim.x) {
+      const int w = node / BT_NODES, lane = node - w * BT_NODES;
+      float hi = 0.f, lo = 0.f;
+      auto add = [&](float x) {
+        const float t = __fadd_rn(hi, x);
+        const float v = __fsub_rn(t, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(t, v)), __fsub_rn(x, v)));
+        hi = t;
+      };
+      if (w < nwin) {
+        const int b = s * nwin + w;
+        for (int it = ifirst[b]; it < ifirst[b + 1]; ++it) add(partial[((size_t)it * nrow + row) * BT_M + lane]);
+      }
+      if (lane == 0 && w >= 1) {
+        const int b = s * nwin + w - 1;
+        for (int it = ifirst[b]; it < ifirst[b + 1]; ++it) add(partial[((size_t)it * nrow + row) * BT_M + BT_NODES]);
+      }
+      G[sr * numr + node] = f * ((double)hi + (double)lo);
+    }
   }
 }
 
@@ -582,23 +588,35 @@ static long long bt_nchunk(const long long* off, int nsnap) {
   return n;
 }
 
+// CTAs of k_sph_batched_tc<LC, NPAD, STAGES> resident per SM: as many as the
+// whole unified L1/shared storage holds as shared memory (the default carveout
+// leaves one per SM) and the SM's 512 tensor-memory columns allow; 0 if none.
 template <int LC, int NPAD, int STAGES>
-static int bt_launch_gemm(const BtArgs& A, cudaStream_t st) {
+static int bt_residency() {
   constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
-  auto kern = k_sph_batched_tc<LC, NPAD, STAGES>;
-  XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // all of the unified L1/shared storage as shared memory, so that as many
-  // CTAs as fit are resident (the default carveout left one per SM)
-  XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  int per_sm = 0;
-  XT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT_THREADS, smem));
-  XT_REQUIRE(per_sm >= 1, "k_sph_batched_tc does not fit on an SM with %zu bytes of shared memory", smem);
-  // tensor memory: every resident CTA holds NCOLS of the SM's 512 columns
+  const int per_sm = resident_blocks_full_carveout((const void*)k_sph_batched_tc<LC, NPAD, STAGES>, BT_THREADS, smem);
   const int ncols = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
-  per_sm = std::min(per_sm, 512 / ncols);
-  kern<<<sm_count() * per_sm, BT_THREADS, smem, st>>>(A);
+  return std::min(per_sm, 512 / ncols);
+}
+
+// Persistent launch of ctas_per_sm CTAs per SM (0: as many as are resident).
+template <int LC, int NPAD, int STAGES>
+static int bt_launch_gemm(const BtArgs& A, int ctas_per_sm, cudaStream_t st) {
+  constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
+  int per_sm = bt_residency<LC, NPAD, STAGES>();
+  XT_REQUIRE(per_sm >= 1, "k_sph_batched_tc does not fit on an SM with %zu bytes of shared memory", smem);
+  if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
+  k_sph_batched_tc<LC, NPAD, STAGES><<<sm_count() * per_sm, BT_THREADS, smem, st>>>(A);
   XT_CHECK_LAUNCH("k_sph_batched_tc");
   return XT_OK;
+}
+
+// Dispatch on the pipeline depth.
+template <int LC, int NPAD, typename F>
+static int bt_with_stages(int stages, F&& f) {
+  if (stages == 1) return f(std::integral_constant<int, 1>{});
+  if (stages == 2) return f(std::integral_constant<int, 2>{});
+  return f(std::integral_constant<int, 3>{});
 }
 
 }  // namespace xt
@@ -616,14 +634,15 @@ size_t xt_sph_batched_tc_workspace(void* handle, int nsnap, const long long* off
 }
 
 int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long long* offsets_host, int nsnap,
-                                 int no_odd, int chunk, int stages, double* expcoef_out, void* workspace,
-                                 size_t workspace_bytes, void* stream) {
+                                 int no_odd, int chunk, int stages, int ctas_per_sm, double* expcoef_out,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
   SphTab<double> d;
   SphTab<float> f;
   XT_REQUIRE(sph_tabs(handle, &d, &f), "NULL table handle");
   XT_REQUIRE(nsnap > 0 && offsets_host && expcoef_out, "need nsnap > 0, host offsets and an output");
   XT_REQUIRE(chunk >= BT_KT && chunk <= (1 << 30), "chunk must be in [%d, 2^30] particles", BT_KT);
   XT_REQUIRE(stages >= 1 && stages <= 3, "stages must be 1, 2 or 3");
+  XT_REQUIRE(ctas_per_sm >= 0, "ctas_per_sm must be >= 0 (0: as many as are resident)");
   XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
   XT_REQUIRE(d.numr >= 2 && (d.numr - 2) / BT_NODES + 1 <= BT_MAXWIN, "numr must be in [2, %d]",
              BT_MAXWIN * BT_NODES + 1);
@@ -699,18 +718,39 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
     int rc = with_lcap(d.lmax, [&](auto lc) -> int {
       constexpr int LC = decltype(lc)::value;
       constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
-      if (stages == 1) return bt_launch_gemm<LC, NPAD, 1>(A, st);
-      return stages == 2 ? bt_launch_gemm<LC, NPAD, 2>(A, st) : bt_launch_gemm<LC, NPAD, 3>(A, st);
+      return bt_with_stages<LC, NPAD>(stages, [&](auto sc) -> int {
+        return bt_launch_gemm<LC, NPAD, decltype(sc)::value>(A, ctas_per_sm, st);
+      });
     });
     if (rc) return rc;
-    const long long nred = (long long)nsnap * nrow * d.numr;
-    k_bt_reduce<<<(int)std::min<long long>((nred + 255) / 256, (long long)sm_count() * 16), 256, 0, st>>>(
+    const long long nred = (long long)nsnap * nrow;
+    k_bt_reduce<<<(int)std::min<long long>(nred, (long long)sm_count() * 32), 256, 0, st>>>(
         A.partial, ifirst, d.fact, d.lmax, nsnap, nrow, d.numr, L.nwin, G);
     XT_CHECK_LAUNCH("k_bt_reduce");
   }
   const float2* efp_df = nullptr;
   XT_REQUIRE(sph_efp_df(handle, &efp_df), "NULL table handle");
   return launch_sph_contract_batched(efp_df, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
+}
+
+int xt_sph_batched_tc_residency(void* handle, int stages, int* ctas_per_sm) {
+  SphTab<double> d;
+  XT_REQUIRE(sph_tabs(handle, &d, nullptr), "NULL table handle");
+  XT_REQUIRE(stages >= 1 && stages <= 3, "stages must be 1, 2 or 3");
+  XT_REQUIRE(ctas_per_sm, "NULL output");
+  XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
+  int v = 0;
+  with_lcap(d.lmax, [&](auto lc) -> int {
+    constexpr int LC = decltype(lc)::value;
+    constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
+    return bt_with_stages<LC, NPAD>(stages, [&](auto sc) -> int {
+      v = bt_residency<LC, NPAD, decltype(sc)::value>();
+      return XT_OK;
+    });
+  });
+  *ctas_per_sm = v;
+  XT_REQUIRE(v >= 1, "k_sph_batched_tc does not fit on an SM at %d stages", stages);
+  return XT_OK;
 }
 
 int xt_sph_batched_tc_status(void) {

@@ -47,6 +47,16 @@ int sm_count();   // multiprocessors of the current device (cached)
 // dynamic shared memory (cudaOccupancyMaxActiveBlocksPerMultiprocessor, cached).
 int resident_blocks_per_sm(const void* fn, int block, size_t smem);
 
+// For a kernel with large dynamic shared memory: asks for the whole unified
+// L1/shared storage as shared memory (carveout 100) and returns the blocks
+// resident per SM under that carveout.  The occupancy API counts shared memory
+// against the default carveout, not the preference, so the shared-memory limit
+// is computed here from the SM's shared memory, the per-block reservation and
+// the 128-byte allocation granularity; registers, warps and the block limit
+// come from the occupancy API without dynamic shared memory.  Returns 0 when a
+// block does not fit.
+int resident_blocks_full_carveout(const void* fn, int block, size_t smem);
+
 // Grid of at most one full wave: as many blocks as stay resident together, or
 // fewer when `units` (one per thread) needs fewer.  Grid-stride kernels launched
 // this way balance their work over every resident block instead of leaving a

@@ -73,6 +73,27 @@ int resident_blocks_per_sm(const void* fn, int block, size_t smem) {
   return v;
 }
 
+int resident_blocks_full_carveout(const void* fn, int block, size_t smem) {
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0, per_sm_smem = 0, reserved = 0, other = 0;
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, fn) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&other, fn, block, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const size_t per_block = (smem + fa.sharedSizeBytes + (size_t)reserved + 127) / 128 * 128;
+  const int by_smem = (int)((size_t)per_sm_smem / per_block);
+  return by_smem < other ? by_smem : other;
+}
+
 int grid_for(long long n, int block, int blocks_per_sm) {
   const int nsm = sm_count();
   long long need = (n + block - 1) / block;

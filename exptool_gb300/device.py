@@ -232,14 +232,17 @@ class SphTable:
                    "xt_sph_accumulate_batched")
         return out
 
-    def accumulate_batched_tc(self, xyzm, offsets, no_odd=False, chunk=16384, stages=2, workspace=None):
+    def accumulate_batched_tc(self, xyzm, offsets, no_odd=False, chunk=16384, stages=2, ctas_per_sm=0,
+                              workspace=None):
         """Coefficients of many snapshots on the tensor cores: particles
         counting-sorted by (snapshot, radial window), then per window a BF16
         tcgen05 product of the interpolation weights and the angular basis
         values with FP32 accumulation, FP64 sums of the window partials and an
         FP64 contraction.  Arguments as for accumulate_batched; ``chunk`` is
         the most particles of one work item, ``stages`` the operand buffers per
-        CTA (1 to 3).  Returns a (nsnap, (lmax+1)^2, nmax) float64 tensor."""
+        CTA (1 to 3), ``ctas_per_sm`` the CTAs of the persistent launch per SM
+        (0: as many as are resident).  Returns a (nsnap, (lmax+1)^2, nmax)
+        float64 tensor."""
         offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
         nsnap = offs.size - 1
         if xyzm.dtype != torch.float32 or xyzm.dim() != 2 or xyzm.shape[1] != 4 or not xyzm.is_contiguous():
@@ -251,10 +254,19 @@ class SphTable:
         ws = workspace if (workspace is not None and workspace.numel() >= need) else \
             torch.empty(need, dtype=torch.uint8, device=xyzm.device)
         _lib.check(self._lib.xt_sph_accumulate_batched_tc(self.handle, dptr(xyzm), offs.ctypes.data, nsnap,
-                                                          int(bool(no_odd)), int(chunk), int(stages), dptr(out),
-                                                          dptr(ws), ws.numel(), stream_ptr()),
+                                                          int(bool(no_odd)), int(chunk), int(stages),
+                                                          int(ctas_per_sm), dptr(out), dptr(ws), ws.numel(),
+                                                          stream_ptr()),
                    "xt_sph_accumulate_batched_tc")
         return out
+
+    def batched_tc_residency(self, stages):
+        """CTAs of the tensor-core accumulation resident per SM at this
+        pipeline depth (the largest useful ``ctas_per_sm``)."""
+        v = ctypes.c_int(0)
+        _lib.check(self._lib.xt_sph_batched_tc_residency(self.handle, int(stages), ctypes.byref(v)),
+                   "xt_sph_batched_tc_residency")
+        return int(v.value)
 
     def batched_tc_workspace(self, offsets, chunk=16384):
         offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))

@@ -1,86 +1,144 @@
 """Orbit frequencies with the interface of ``exptool/orbits/frequencies.py``,
-computed for whole orbit maps at once on the GPU: the spectra of all orbits
-(columns) are one batched FFT (cuFFT through torch.fft), the relative maxima
-and the strongest peaks of every spectrum are found with tensor operations,
-in chunks of orbits that bound device memory.  The reference loops over
+computed for whole orbit maps at once on the GPU by one kernel of this library
+(``xt_orbit_spectra``): one CTA per orbit takes the N-point DFT of its signal
+in double-float arithmetic in shared memory (radix-2 FFT for N a power of two,
+Bluestein's transform otherwise) and searches the spectrum for its peaks in
+place, so only indices and powers leave the device.  The reference loops over
 orbits with numpy.fft.
 
 Conventions followed (frequencies.py):
 * frequencies are numpy.fft.fftfreq(N, d = T[1] - T[0]) of the window;
-* fundamental frequencies: the spectrum of pos + i vel (Hann window
-  0.5 - 0.5 cos(2 pi n / (N - 1)) when hanning), relative maxima of
-  |Re spectrum| that beat `order` neighbours on each side (edges clipped, as
-  numpy.take with mode='clip'), positive frequencies only, sorted by that
-  power (frequencies.py:94-132);
+* fundamental frequencies: the spectrum of pos + i vel (numpy.hanning window
+  when hanning), relative maxima of |Re spectrum| that beat `order`
+  neighbours on each side (edges clipped, as numpy.take with mode='clip'),
+  positive frequencies only, sorted by that power (frequencies.py:94-132);
 * radial / azimuthal / vertical frequencies: |frequency| of the largest
   |spectrum| of R, phi, z with the zero-frequency term of R (and, for maps,
   of z) removed (frequencies.py:135-217).
 Where a spectrum has fewer than three qualifying maxima the missing
 fundamental frequencies are NaN (the reference raises IndexError).  The
-reference's mutable default ``window`` list is not modified here.
+reference's mutable default ``window`` list is not modified here.  Signals are
+limited to 4096 samples for a power-of-two length and 2048 otherwise (the
+transform of one signal lives in shared memory).
 """
 from __future__ import annotations
 
 import numpy as np
 import torch
 
+from .. import _lib
 from .. import device as dev
 
-_CHUNK_BYTES = 1 << 31          # complex spectra per chunk of orbits
+_CHUNK_BYTES = 1 << 31          # device bytes of signal columns per chunk of orbits
+_MAX_M = 4096
+_TABLES = {}
 
 
 def _window(n, lo, hi):
     return lo, (n if hi > n else hi)
 
 
-def _chunks(norb, nt):
-    per = max(1, int(_CHUNK_BYTES // (16 * max(nt, 1))))
+def _chunks(norb, nt, arrays=1):
+    per = max(1, int(_CHUNK_BYTES // (8 * arrays * max(nt, 1))))
     for a in range(0, norb, per):
         yield a, min(norb, a + per)
 
 
-def _relmax(a, order):
-    """Strict relative maxima along dim 0 against `order` neighbours each
-    side, indices clipped at the ends."""
-    n = a.shape[0]
-    idx = torch.arange(n, device=a.device)
-    mask = torch.ones_like(a, dtype=torch.bool)
-    for k in range(1, int(order) + 1):
-        mask &= a > a[(idx + k).clamp(max=n - 1)]
-        mask &= a > a[(idx - k).clamp(min=0)]
-    return mask
+def _split(z):
+    """Complex FP64 values -> (k, 4) float32 (re hi, re lo, im hi, im lo)."""
+    z = np.asarray(z, dtype=np.complex128)
+    rh = z.real.astype(np.float32)
+    ih = z.imag.astype(np.float32)
+    out = np.empty((z.size, 4), dtype=np.float32)
+    out[:, 0] = rh
+    out[:, 1] = (z.real - rh.astype(np.float64)).astype(np.float32)
+    out[:, 2] = ih
+    out[:, 3] = (z.imag - ih.astype(np.float64)).astype(np.float32)
+    return out
 
 
-def _hann(n, device):
-    if n == 1:
-        return torch.ones(1, dtype=torch.float64, device=device)
-    k = torch.arange(n, dtype=torch.float64, device=device)
-    return 0.5 - 0.5 * torch.cos(2.0 * np.pi * k / (n - 1))
+def _tables(n):
+    """(m, twiddles, chirp, chirp transform) device tables for signals of n
+    samples, cached per n.  Chirp angles are reduced exactly in integers
+    before the FP64 exponentials."""
+    if n in _TABLES:
+        return _TABLES[n]
+    if n < 2:
+        raise ValueError(f"orbit signals need at least 2 samples, got {n}")
+    pow2 = n & (n - 1) == 0
+    m = n if pow2 else 1 << int(np.ceil(np.log2(2 * n - 1)))
+    if m > _MAX_M:
+        raise ValueError(f"orbit signals of {n} samples exceed the transform limit ({_MAX_M} for powers of two, "
+                         f"{_MAX_M // 2} otherwise)")
+    t = np.arange(m // 2, dtype=np.int64)
+    tw = np.exp(-2j * np.pi * (t / m))
+    chirp = chirp_f = None
+    if not pow2:
+        j = np.arange(n, dtype=np.int64)
+        w = np.exp(-1j * np.pi * ((j * j) % (2 * n)) / n)          # exp(-i pi j^2 / n)
+        b = np.zeros(m, dtype=np.complex128)
+        b[:n] = np.conj(w)
+        b[m - n + 1:] = np.conj(w[1:])[::-1]
+        chirp = dev.to_dev(_split(w), dtype=torch.float32)
+        chirp_f = dev.to_dev(_split(np.fft.fft(b)), dtype=torch.float32)
+    out = (m, dev.to_dev(_split(tw), dtype=torch.float32), chirp, chirp_f)
+    _TABLES[n] = out
+    return out
 
 
-def _fundamental(pos, vel, freq, hanning, order, nkeep=3):
-    """pos, vel: (N, B) float64 host arrays -> (omega (nkeep, B), power (nkeep, B))."""
+def spectra_device(mode, re, im, win=None, order=4, zero_first=False, freq_sign=1, want_spec=False):
+    """One xt_orbit_spectra launch over device signals: re, im (None for a
+    real signal) are (N, B) float64 CUDA tensors, column b one orbit's
+    samples; win a device window of N values or None.  mode 0 returns the
+    three strongest relative maxima of |Re X| at frequencies of sign
+    freq_sign beating `order` neighbours on each side, mode 1 the index of
+    the largest |X| (the zero-frequency term dropped when zero_first).
+    Returns device (idx (B, 3) int32, value (B, 3) float64, spectra (B, N, 2)
+    float64 or None); unused slots hold index -1."""
+    lib = _lib.load()
+    N, B = re.shape
+    m, tw, chirp, chirp_f = _tables(N)
+    io = torch.empty((B, 3), dtype=torch.int32, device=re.device)
+    vo = torch.empty((B, 3), dtype=torch.float64, device=re.device)
+    so = torch.empty((B, N, 2), dtype=torch.float64, device=re.device) if want_spec else None
+    _lib.check(lib.xt_orbit_spectra(int(mode), B, N, dev.dptr(re), dev.dptr(im), B, dev.dptr(win), int(order),
+                                    int(bool(zero_first)), int(freq_sign), m, dev.dptr(tw), dev.dptr(chirp),
+                                    dev.dptr(chirp_f), dev.dptr(io), dev.dptr(vo), dev.dptr(so),
+                                    dev.stream_ptr()), "xt_orbit_spectra")
+    return io, vo, so
+
+
+def _spectra(mode, re, im, win, order, zero_first, freq_sign, want_spec=False):
+    """spectra_device over (N, B) host arrays in chunks of orbits that bound
+    the device memory.  Returns host (idx (B, 3), val (B, 3), spectra (B, N)
+    complex or None)."""
+    N, B = re.shape
+    idx = np.empty((B, 3), dtype=np.int32)
+    val = np.empty((B, 3))
+    spec = np.empty((B, N), dtype=np.complex128) if want_spec else None
+    w = dev.to_dev(np.asarray(win, dtype=np.float64)) if win is not None else None
+    for a, b in _chunks(B, N, 1 if im is None else 2):
+        rd = dev.to_dev(np.ascontiguousarray(re[:, a:b]))
+        idd = dev.to_dev(np.ascontiguousarray(im[:, a:b])) if im is not None else None
+        io, vo, so = spectra_device(mode, rd, idd, w, order, zero_first, freq_sign, want_spec)
+        idx[a:b] = dev.to_host(io)
+        val[a:b] = dev.to_host(vo)
+        if want_spec:
+            sh = dev.to_host(so)
+            spec[a:b] = sh[..., 0] + 1j * sh[..., 1]
+    return idx, val, spec
+
+
+def _fundamental(pos, vel, freq, hanning, order, nkeep=3, want_spec=False):
+    """pos, vel: (N, B) float64 host arrays -> (omega (nkeep, B), power (nkeep, B)[, spectra (B, N)])."""
     N, B = pos.shape
-    fr = torch.as_tensor(freq, dtype=torch.float64, device=dev.device())
-    om = np.full((nkeep, B), np.nan)
-    pw = np.full((nkeep, B), np.nan)
-    w = _hann(N, dev.device())[:, None] if hanning else None
-    for a, b in _chunks(B, N):
-        p = dev.to_dev(np.ascontiguousarray(pos[:, a:b]))
-        v = dev.to_dev(np.ascontiguousarray(vel[:, a:b]))
-        ft = torch.complex(p, v)
-        if w is not None:
-            ft = ft * w
-        spec = torch.fft.fft(ft, dim=0)
-        amp = spec.real.abs()
-        mask = _relmax(amp, order) & (fr > 0)[:, None]
-        vals = torch.where(mask, amp, torch.full_like(amp, -np.inf))
-        k = min(nkeep, N)
-        tv, ti = torch.topk(vals, k, dim=0)
-        ok = torch.isfinite(tv)
-        om[:k, a:b] = dev.to_host(torch.where(ok, fr[ti], torch.full_like(tv, np.nan)))
-        pw[:k, a:b] = dev.to_host(torch.where(ok, tv, torch.full_like(tv, np.nan)))
-    return om, pw
+    win = np.hanning(N) if hanning else None
+    sign = 1 if (N < 2 or freq[1] > 0) else -1
+    idx, val, spec = _spectra(0, pos, vel, win, order, False, sign, want_spec)
+    ok = idx[:, :nkeep] >= 0
+    om = np.where(ok, np.asarray(freq)[np.clip(idx[:, :nkeep], 0, None)], np.nan).T
+    pw = np.where(ok, val[:, :nkeep], np.nan).T
+    return (om, pw, spec) if want_spec else (om, pw)
 
 
 def find_fundamental_frequency_map(OrbitInstance, time="T", pos="X", vel="VX", hanning=True, window=(0, 10000),
@@ -105,26 +163,29 @@ def find_fundamental_frequency(OrbitInstance, time="T", pos="X", vel="VX", hanni
     freq = np.fft.fftfreq(T[lo:hi].shape[-1], d=(T[1] - T[0]))
     P = np.asarray(OrbitInstance[pos], dtype=np.float64)[lo:hi][:, None]
     V = np.asarray(OrbitInstance[vel], dtype=np.float64)[lo:hi][:, None]
-    om, _pw = _fundamental(P, V, freq, hanning, order)
+    om, _pw, spec = _fundamental(P, V, freq, hanning, order, want_spec=True)
     for i in range(3):
         OrbitInstance["O" + pos + str(i + 1)] = om[i, 0]
     if retall:
-        ft = torch.complex(dev.to_dev(P[:, 0]), dev.to_dev(V[:, 0]))
-        if hanning:
-            ft = ft * _hann(ft.shape[0], dev.device())
-        return OrbitInstance, freq, dev.to_host(torch.fft.fft(ft))
+        return OrbitInstance, freq, spec[0]
     return OrbitInstance
 
 
 def organize_frequencies(freq, fftarr, order=4):
     """frequencies.py:94-132: (positive-frequency relative maxima of
-    |Re fftarr|, their power), strongest first."""
-    a = torch.as_tensor(np.abs(np.asarray(fftarr).real), dtype=torch.float64, device=dev.device())
-    mask = dev.to_host(_relmax(a[:, None], order)[:, 0])
+    |Re fftarr|, their power), strongest first.  A host utility on a given
+    spectrum, as in the reference."""
+    amp = np.abs(np.asarray(fftarr).real)
+    n = amp.size
+    k = np.arange(n)
+    mask = np.ones(n, dtype=bool)
+    for j in range(1, int(order) + 1):
+        mask &= amp > amp[np.clip(k + j, 0, n - 1)]
+        mask &= amp > amp[np.clip(k - j, 0, n - 1)]
     vals = np.where(mask)[0]
     g = np.where(np.asarray(freq)[vals] > 0.0)[0]
     gomegas = np.asarray(freq)[vals[g]]
-    gvals = np.abs(np.asarray(fftarr).real)[vals[g]]
+    gvals = amp[vals[g]]
     o = (-1.0 * gvals).argsort()
     return gomegas[o], gvals[o]
 
@@ -132,16 +193,10 @@ def organize_frequencies(freq, fftarr, order=4):
 def _peak_freqs(cols, freq, zero_first):
     """|freq| of the largest |spectrum| of each column of each array; the
     zero-frequency term removed where zero_first[i]."""
-    fr = torch.as_tensor(freq, dtype=torch.float64, device=dev.device())
-    N, B = cols[0].shape
-    outs = [np.empty(B) for _ in cols]
-    for a, b in _chunks(B, N):
-        for i, c in enumerate(cols):
-            sp = torch.fft.fft(dev.to_dev(np.ascontiguousarray(c[:, a:b])).to(torch.complex128), dim=0)
-            mag = sp.abs()
-            if zero_first[i]:
-                mag[0] = 0.0
-            outs[i][a:b] = dev.to_host(fr[mag.argmax(dim=0)].abs())
+    outs = []
+    for i, c in enumerate(cols):
+        idx, _val, _ = _spectra(1, c, None, None, 0, zero_first[i], 1)
+        outs.append(np.abs(np.asarray(freq)[idx[:, 0]]))
     return outs
 
 

@@ -146,15 +146,19 @@ int xt_sph_accumulate_batched(void *handle, const float *xyzm, const long long *
  * accumulation in tensor memory (M = 128 nodes, N = rows padded to 16,
  * K = particles); window partials are summed in FP64 and contracted with the
  * radial tables in FP64.  Same arguments as xt_sph_accumulate_batched, with
- * chunk = the most particles of one work item (>= 128) and stages = operand
- * buffers per CTA (1 to 3; fewer buffers let more CTAs share an SM).  numr <= 8129, lmax <= 8, at most 2^31 - 1
- * particles.  The workspace size depends on the snapshot sizes.
+ * chunk = the most particles of one work item (>= 128), stages = operand
+ * buffers per CTA (1 to 3; fewer buffers let more CTAs share an SM) and
+ * ctas_per_sm = CTAs of the persistent launch per SM (0: as many as are
+ * resident; xt_sph_batched_tc_residency gives that number for a depth).
+ * numr <= 8129, lmax <= 8, at most 2^31 - 1 particles.  The workspace size
+ * depends on the snapshot sizes.
  * xt_sph_batched_tc_status synchronises the device and reports (and clears)
  * an error flag a launch set: XT_ERR_DEVICE, else XT_OK. */
 size_t xt_sph_batched_tc_workspace(void *handle, int nsnap, const long long *offsets_host, int chunk);
 int xt_sph_accumulate_batched_tc(void *handle, const float *xyzm, const long long *offsets_host, int nsnap,
-                                 int no_odd, int chunk, int stages, double *expcoef_out, void *workspace,
-                                 size_t workspace_bytes, void *stream);
+                                 int no_odd, int chunk, int stages, int ctas_per_sm, double *expcoef_out,
+                                 void *workspace, size_t workspace_bytes, void *stream);
+int xt_sph_batched_tc_residency(void *handle, int stages, int *ctas_per_sm);
 int xt_sph_batched_tc_status(void);
 
 /* --------------------------------------------------------------- cylindrical (EOF) */
@@ -322,6 +326,28 @@ int xt_learned_radial_pass(void *sph, void *mlp, const void *prep, int K, double
 /* Synchronises, then reports (and clears) a tensor-memory pass that gave up
  * waiting for its MMAs: XT_ERR_DEVICE, else XT_OK. */
 int xt_learned_status(void);
+
+/* --------------------------------------------------------------- orbit frequencies */
+/* Spectra and peaks of nsig orbit signals of n samples: signal s, sample t at
+ * a[t * ld + s] (+ i b[t * ld + s] when b != NULL), times win[t] when win !=
+ * NULL (numpy.hanning values); device arrays.  The n-point DFT of
+ * numpy.fft.fft in double-float arithmetic, one CTA per signal: a radix-2
+ * FFT of size m = n for n a power of two, else Bluestein's transform with
+ * m = 2^p >= 2n - 1 (m <= 4096).  Tables as complex double-float quadruples
+ * (re hi, re lo, im hi, im lo; float32, 16-byte aligned, device): tw[m/2] =
+ * exp(-2 pi i t/m); chirp[n] = exp(-i pi t^2/n) and chirp_f[m] = the m-point
+ * FFT of the chirp's conjugate wrapped circularly (Bluestein only, else NULL).
+ * mode 0: exptool/orbits/frequencies.py:94-132 organize_frequencies on the
+ * spectrum: idx_out[s][0..2] = the three strongest strict relative maxima of
+ * |Re X| (order neighbours each side, ends clipped) at positive frequencies
+ * (freq_sign = sign of the time step), -1 when missing, val_out = their
+ * |Re X|.  mode 1: frequencies.py:135-217: idx_out[s][0] = first index of the
+ * largest |X| with bin 0 set to zero when zero_first.  spec_out (may be NULL):
+ * [nsig][n] complex doubles. */
+int xt_orbit_spectra(int mode, long long nsig, int n, const double *a, const double *b, long long ld,
+                     const double *win, int order, int zero_first, int freq_sign, int m, const float *tw,
+                     const float *chirp, const float *chirp_f, int *idx_out, double *val_out, double *spec_out,
+                     void *stream);
 
 /* --------------------------------------------------------------- table generation */
 /* Basis functions of the cylindrical EOF construction at npt points (R, z),
