@@ -132,8 +132,15 @@ constexpr int kCbPitch = kCbTile + 1;      // float2 pitch: rows of the table ti
 constexpr int kCbOut = 3;                  // outputs per thread when S = 1: (2l+1) nmax <= 3 * 256
 constexpr int kCbThreads = 256;
 
+__device__ __forceinline__ float2 cb_pair(double v) {
+  const df d = df_from(v);
+  return make_float2(d.h, d.l);
+}
+__device__ __forceinline__ float2 cb_pair(float2 v) { return v; }
+
+template <typename GT>
 __global__ void __launch_bounds__(kCbThreads) k_sph_contract_batched_df(const float2* __restrict__ efp_df,
-                                                                       const double* __restrict__ G, int lmax,
+                                                                       const GT* __restrict__ G, int lmax,
                                                                        int nmax, int numr,
                                                                        double* __restrict__ out) {
   extern __shared__ float2 cb_sm[];
@@ -144,7 +151,7 @@ __global__ void __launch_bounds__(kCbThreads) k_sph_contract_batched_df(const fl
   const int S = nout >= kCbThreads ? 1 : kCbThreads / nout;    // node slices per output
   float2* Gt = cb_sm;                       // [nr][kCbPitch]
   float2* Et = cb_sm + nr * kCbPitch;       // [nmax][kCbPitch]
-  const double* g = G + ((size_t)s * nrow + r0) * numr;
+  const GT* g = G + ((size_t)s * nrow + r0) * numr;
   const float2* e = efp_df + (size_t)l * nmax * numr;
   const int tid = threadIdx.x;
   const int sl = tid % S, o0 = tid / S;     // slice and first output of this thread
@@ -166,12 +173,7 @@ __global__ void __launch_bounds__(kCbThreads) k_sph_contract_batched_df(const fl
     __syncthreads();
     for (int k = tid; k < nr * kCbTile; k += kCbThreads) {
       const int r = k / kCbTile, j = k - r * kCbTile;
-      float2 v = make_float2(0.f, 0.f);
-      if (j < tn) {
-        const df d = df_from(g[(size_t)r * numr + t0 + j]);
-        v = make_float2(d.h, d.l);
-      }
-      Gt[r * kCbPitch + j] = v;
+      Gt[r * kCbPitch + j] = j < tn ? cb_pair(g[(size_t)r * numr + t0 + j]) : make_float2(0.f, 0.f);
     }
     for (int k = tid; k < nmax * kCbTile; k += kCbThreads) {
       const int n = k / kCbTile, j = k - n * kCbTile;
@@ -225,20 +227,32 @@ __global__ void __launch_bounds__(kCbThreads) k_sph_contract_batched_df(const fl
 
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
-                                double* out, cudaStream_t st) {
+template <typename GT>
+static int contract_batched(const float2* efp_df, const GT* G, int nsnap, int lmax, int nmax, int numr, double* out,
+                            cudaStream_t st) {
   XT_REQUIRE((2 * lmax + 1) * nmax <= kCbOut * kCbThreads,
              "the batched contraction supports (2 lmax + 1) nmax <= %d", kCbOut * kCbThreads);
   const size_t smem = (size_t)(2 * lmax + 1 + nmax) * kCbPitch * sizeof(float2);
   static size_t attr = 0;
   if (smem > 48 * 1024 && smem > attr) {
-    XT_CUDA(cudaFuncSetAttribute(k_sph_contract_batched_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    XT_CUDA(cudaFuncSetAttribute(k_sph_contract_batched_df<GT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
     attr = smem;
   }
-  k_sph_contract_batched_df<<<dim3((unsigned)nsnap, (unsigned)(lmax + 1)), kCbThreads, smem, st>>>(
+  k_sph_contract_batched_df<GT><<<dim3((unsigned)nsnap, (unsigned)(lmax + 1)), kCbThreads, smem, st>>>(
       efp_df, G, lmax, nmax, numr, out);
   XT_CHECK_LAUNCH("k_sph_contract_batched_df");
   return XT_OK;
+}
+
+int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
+                                double* out, cudaStream_t st) {
+  return contract_batched(efp_df, G, nsnap, lmax, nmax, numr, out, st);
+}
+
+int launch_sph_contract_batched(const float2* efp_df, const float2* G, int nsnap, int lmax, int nmax, int numr,
+                                double* out, cudaStream_t st) {
+  return contract_batched(efp_df, G, nsnap, lmax, nmax, numr, out, st);
 }
 
 }  // namespace xt

@@ -18,8 +18,9 @@
 // of 16), K = particles, BF16 operands and FP32 accumulation in tensor memory.
 //
 // Pipeline (one call, all snapshots):
-//   1. k_bt_hist: the node interval i of every particle (kept), counts per
-//      (sorting chunk, window of 127 intervals);
+//   1. k_bt_hist: counts per (sorting chunk, window of 127 intervals) of the
+//      particles' node intervals (recomputed bit for bit by the scatter and
+//      the products, so nothing per particle is stored);
 //   2. k_bt_offsets, k_bt_buckets, k_bt_items: per-chunk offsets inside each
 //      (snapshot, window) bucket, bucket bases, and work items (bucket pieces
 //      of at most `chunk` particles);
@@ -30,8 +31,9 @@
 //      and commits them to the stage's mbarrier while the next stage is
 //      built; at the item's end the accumulator (128 nodes x rows, FP32) is
 //      read from tensor memory into a per-item partial;
-//   5. k_bt_reduce: FP64 sum of the partials per (snapshot, row, node), in a
-//      fixed order (the window boundary node takes both windows' shares);
+//   5. k_bt_reduce: exact double-float sum of the partials per (snapshot,
+//      row, node), in a fixed order (the window boundary node takes both
+//      windows' shares), times fact[l][m];
 //   6. k_sph_contract_batched_df: contraction with the radial tables in
 //      double-float arithmetic (FP64-level accuracy on the FP32 pipe).
 // Waits are bounded: a timeout sets the error flag read by
@@ -44,6 +46,7 @@
 
 #include <cuda_bf16.h>
 
+#include "xt_df.cuh"
 #include "xt_internal.cuh"
 #include "xt_launch.cuh"
 #include "xt_tc.cuh"
@@ -75,7 +78,6 @@ struct BtItem {
 struct BtArgs {
   SphTab<float> T;
   const float4* sorted;
-  const int* sidx;
   const BtItem* items;
   const int* nitems;
   int* counter;
@@ -92,21 +94,37 @@ __device__ __forceinline__ void bt_st(unsigned char* tile, int row, int k, float
   *reinterpret_cast<__nv_bfloat16*>(tile + bt_off(row, k)) = __float2bfloat16_rn(v);
 }
 
+// Radius, mapped radius and interpolation interval of a particle.  The
+// counting sort (k_bt_hist, k_bt_scatter) and the products (k_sph_batched_tc)
+// each compute them from the particle, so every operation is an explicitly
+// rounded intrinsic (no multiply-add contraction left to the compiler) and
+// the three kernels get the same bits: the interval that put a particle into
+// a window is the one its weights are taken on.
 __device__ __forceinline__ float bt_radius(float4 q) {
-  float r = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z);
+  const float r = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(q.x, q.x), __fmul_rn(q.y, q.y)), __fmul_rn(q.z, q.z)));
   return (r >= 1.0e-10f) ? r : 1.0e-10f;
 }
 
-// Interpolation interval of radius r: the node index of sph_bins
-// (spheresl.py:121-131) without its weights (no table reads).
-__device__ __forceinline__ int bt_interval(const SphTab<float>& T, float r) {
-  float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
+// compatibility.r_to_xi (compatibility.py:16-36) for r > 0, clamped to the
+// table as sph_bins does (spheresl.py:121-131).
+__device__ __forceinline__ float bt_xi(const SphTab<float>& T, float r) {
+  float x;
   if (T.cmap == 1) {
-    if (x < -1.f) x = -1.f;
-    if (x >= 1.f) x = 1.f - 1.0e-08f;
+    const float u = __fmul_rn(r, T.inv_scale);
+    x = __fdiv_rn(__fsub_rn(u, 1.f), __fadd_rn(u, 1.f));
+    x = fminf(fmaxf(x, -1.f), 1.f - 1.0e-8f);
+  } else if (T.cmap == 2) {
+    x = fminf(fmaxf(logf(r), T.lo), T.hi);
+  } else {
+    x = r;
   }
-  if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
-  float fi = floorf((x - T.xi0) * T.inv_dxi);
+  return x;
+}
+
+// Interpolation interval of mapped radius x: the node index of sph_bins
+// (spheresl.py:121-131).
+__device__ __forceinline__ int bt_interval(const SphTab<float>& T, float x) {
+  float fi = floorf(__fmul_rn(__fsub_rn(x, T.xi0), T.inv_dxi));
   if (!(fi >= 0.f)) fi = 0.f;
   if (fi > (float)(T.numr - 2)) fi = (float)(T.numr - 2);
   return (int)fi;
@@ -144,15 +162,14 @@ __device__ __forceinline__ int bt_block_scan(int v, int* wsum, int* total) {
 
 __global__ void __launch_bounds__(256) k_bt_hist(SphTab<float> T, const float4* __restrict__ xyzm,
                                                  const BtChunk* __restrict__ chunks, int nchunk, int nwin,
-                                                 int* __restrict__ pidx, int* __restrict__ ccount) {
+                                                 int* __restrict__ ccount) {
   __shared__ int cnt[BT_MAXWIN];
   for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
     for (int w = threadIdx.x; w < nwin; w += blockDim.x) cnt[w] = 0;
     __syncthreads();
     const BtChunk C = chunks[c];
     for (long long p = C.begin + threadIdx.x; p < C.end; p += blockDim.x) {
-      const int i = bt_interval(T, bt_radius(xyzm[p]));
-      pidx[p] = i;
+      const int i = bt_interval(T, bt_xi(T, bt_radius(xyzm[p])));
       atomicAdd(&cnt[i / BT_NODES], 1);
     }
     __syncthreads();
@@ -233,24 +250,23 @@ __global__ void k_bt_items(const long long* __restrict__ bsize, const long long*
   }
 }
 
-__global__ void __launch_bounds__(256) k_bt_scatter(const float4* __restrict__ xyzm, const BtChunk* __restrict__ chunks,
-                                                    int nchunk, int nwin, const int* __restrict__ pidx,
+__global__ void __launch_bounds__(256) k_bt_scatter(SphTab<float> T, const float4* __restrict__ xyzm,
+                                                    const BtChunk* __restrict__ chunks, int nchunk, int nwin,
                                                     const int* __restrict__ coff, const long long* __restrict__ bbase,
                                                     long long n_total, float4* __restrict__ sorted,
-                                                    int* __restrict__ sidx, int* __restrict__ err) {
+                                                    int* __restrict__ err) {
   __shared__ int cnt[BT_MAXWIN];
   for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
     for (int w = threadIdx.x; w < nwin; w += blockDim.x) cnt[w] = 0;
     __syncthreads();
     const BtChunk C = chunks[c];
     for (long long p = C.begin + threadIdx.x; p < C.end; p += blockDim.x) {
-      const int i = pidx[p];
-      const int w = i / BT_NODES;
+      const float4 q = xyzm[p];
+      const int w = bt_interval(T, bt_xi(T, bt_radius(q))) / BT_NODES;
       const int slot = atomicAdd(&cnt[w], 1);
       const long long dst = bbase[(size_t)C.snap * nwin + w] + coff[(size_t)c * nwin + w] + slot;
       if (dst >= 0 && dst < n_total) {
-        sorted[dst] = xyzm[p];
-        sidx[dst] = i;
+        sorted[dst] = q;
       } else {
         atomicExch(err, 2);
       }
@@ -356,20 +372,12 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
     const long long ntile = (I.end - I.begin + BT_KT - 1) / BT_KT;
     // this thread's particle of the next K-tile is loaded one tile ahead
     float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
-    int in = 0;
-    if (I.begin + tid < I.end) {
-      qn = a.sorted[I.begin + tid];
-      in = a.sidx[I.begin + tid];
-    }
+    if (I.begin + tid < I.end) qn = a.sorted[I.begin + tid];
     for (long long t = 0; t < ntile; ++t, ++g) {
       const float4 q = qn;
-      const int i = in;
       const bool have = I.begin + t * BT_KT + tid < I.end;
       const long long pn = I.begin + (t + 1) * BT_KT + tid;
-      if (pn < I.end) {
-        qn = a.sorted[pn];
-        in = a.sidx[pn];
-      }
+      if (pn < I.end) qn = a.sorted[pn];
       // this particle's values, computed before its stage is free
       uint32_t pk[NPAD / 2];
 #pragma unroll
@@ -378,10 +386,10 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
       int li = -1;
       if (have) {
         const float r = bt_radius(q);
-        // interpolation weights on the stored interval (spheresl.py:121-143)
-        float x = r_to_xi_inv(r, T.cmap, T.inv_scale);
-        if (T.cmap == 1) x = fminf(fmaxf(x, -1.f), 1.f - 1.0e-8f);
-        if (T.cmap == 2) x = fminf(fmaxf(x, T.lo), T.hi);
+        // interpolation weights on the interval that sorted the particle
+        // into this window (spheresl.py:121-143)
+        const float x = bt_xi(T, r);
+        const int i = bt_interval(T, x);
         const float x2 = (x - T.xi[i]) * T.inv_dxi, x1 = 1.f - x2;
         const float plerp = x1 * T.p0[i] + x2 * T.p0[i + 1];
         const float base = -BT_FOUR_PI * q.w * plerp;
@@ -511,17 +519,19 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
 // G[s, row, node] = fact[l][m] times the sum of the partials of the windows
 // holding the node, in item order.  Node 127 w (w >= 1) is lane 0 of window w
 // and lane 127 of window w - 1.  The FP32 partials are summed exactly into a
-// double-float (TwoSum on the FP32 pipe; GB300's FP64 pipe is slow) and
-// widened once.  One block per (snapshot, row), threads over the nodes.
+// double-float (TwoSum on the FP32 pipe; GB300's FP64 pipe is slow), times
+// fact as a double-float product, and stored as the (hi, lo) pair the
+// double-float contraction reads.  One block per (snapshot, row), threads
+// over the nodes.
 __global__ void __launch_bounds__(256) k_bt_reduce(const float* __restrict__ partial, const int* __restrict__ ifirst,
                                                    const double* __restrict__ fact, int lmax, int nsnap, int nrow,
-                                                   int numr, int nwin, double* __restrict__ G) {
+                                                   int numr, int nwin, float2* __restrict__ G) {
   for (long long sr = blockIdx.x; sr < (long long)nsnap * nrow; sr += gridDim.x) {
     const int row = (int)(sr % nrow), s = (int)(sr / nrow);
     int l = 0;
     while ((l + 1) * (l + 1) <= row) ++l;
     const int m = (row - l * l + 1) >> 1;            // row l^2 (m = 0), l^2 + 2m - 1 (cos), l^2 + 2m (sin)
-    const double f = fact[l * (lmax + 1) + m];
+    const df f = df_from(fact[l * (lmax + 1) + m]);
     for (int node = threadIdx.x; node < numr; node += blockDim.x) {
       const int w = node / BT_NODES, lane = node - w * BT_NODES;
       float hi = 0.f, lo = 0.f;
@@ -539,7 +549,8 @@ __global__ void __launch_bounds__(256) k_bt_reduce(const float* __restrict__ par
         const int b = s * nwin + w - 1;
         for (int it = ifirst[b]; it < ifirst[b + 1]; ++it) add(partial[((size_t)it * nrow + row) * BT_M + BT_NODES]);
       }
-      G[sr * numr + node] = f * ((double)hi + (double)lo);
+      const df v = df_mul(fast_two_sum(hi, lo), f);
+      G[sr * numr + node] = make_float2(v.h, v.l);
     }
   }
 }
@@ -549,7 +560,7 @@ static __device__ int g_bt_err;
 static size_t bt_al(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct BtLayout {
-  size_t G, pidx, sorted, sidx, chunks, cfirst, ccount, coff, bsize, bbase, ifirst, items, partial, ctr, total;
+  size_t G, sorted, chunks, cfirst, ccount, coff, bsize, bbase, ifirst, items, partial, ctr, total;
   long long max_items;
   int nwin, nb;
   long long nchunk;
@@ -564,10 +575,8 @@ static BtLayout bt_layout(const SphTab<double>& d, int nsnap, long long n_total,
   L.max_items = n_total / chunk + L.nb + 1;
   size_t o = 0;
   auto take = [&](size_t b) { const size_t at = o; o += bt_al(b); return at; };
-  L.G = take((size_t)nsnap * nrow * d.numr * sizeof(double));
-  L.pidx = take((size_t)n_total * sizeof(int));
+  L.G = take((size_t)nsnap * nrow * d.numr * sizeof(float2));
   L.sorted = take((size_t)n_total * sizeof(float4));
-  L.sidx = take((size_t)n_total * sizeof(int));
   L.chunks = take((size_t)nchunk * sizeof(BtChunk));
   L.cfirst = take((size_t)(nsnap + 1) * sizeof(int));
   L.ccount = take((size_t)nchunk * L.nwin * sizeof(int));
@@ -589,14 +598,14 @@ static long long bt_nchunk(const long long* off, int nsnap) {
 }
 
 // CTAs of k_sph_batched_tc<LC, NPAD, STAGES> resident per SM: as many as the
-// whole unified L1/shared storage holds as shared memory (the default carveout
-// leaves one per SM) and the SM's 512 tensor-memory columns allow; 0 if none.
+// registers, the whole unified L1/shared storage as shared memory (the default
+// carveout leaves one per SM) and the SM's 512 tensor-memory columns allow; 0
+// if none.
 template <int LC, int NPAD, int STAGES>
 static int bt_residency() {
   constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
-  const int per_sm = resident_blocks_full_carveout((const void*)k_sph_batched_tc<LC, NPAD, STAGES>, BT_THREADS, smem);
-  const int ncols = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
-  return std::min(per_sm, 512 / ncols);
+  constexpr int ncols = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
+  return resident_blocks_tmem((const void*)k_sph_batched_tc<LC, NPAD, STAGES>, BT_THREADS, smem, ncols);
 }
 
 // Persistent launch of ctas_per_sm CTAs per SM (0: as many as are resident).
@@ -661,13 +670,13 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
   const int nrow = (d.lmax + 1) * (d.lmax + 1);
   cudaStream_t st = as_stream(stream);
   char* ws = static_cast<char*>(workspace);
-  double* G = reinterpret_cast<double*>(ws + L.G);
+  float2* G = reinterpret_cast<float2*>(ws + L.G);
   int* ctr = reinterpret_cast<int*>(ws + L.ctr);      // [0] items, [1] item counter
   int* err = nullptr;
   XT_CUDA(cudaGetSymbolAddress((void**)&err, g_bt_err));
   XT_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st));
   if (n_total == 0) {
-    XT_CUDA(cudaMemsetAsync(G, 0, (size_t)nsnap * nrow * d.numr * sizeof(double), st));
+    XT_CUDA(cudaMemsetAsync(G, 0, (size_t)nsnap * nrow * d.numr * sizeof(float2), st));
   } else {
     std::vector<BtChunk> chunks;
     std::vector<int> cfirst(nsnap + 1);
@@ -682,7 +691,6 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
     int* dcfirst = reinterpret_cast<int*>(ws + L.cfirst);
     XT_CUDA(cudaMemcpyAsync(dchunks, chunks.data(), chunks.size() * sizeof(BtChunk), cudaMemcpyHostToDevice, st));
     XT_CUDA(cudaMemcpyAsync(dcfirst, cfirst.data(), cfirst.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    int* pidx = reinterpret_cast<int*>(ws + L.pidx);
     int* ccount = reinterpret_cast<int*>(ws + L.ccount);
     int* coff = reinterpret_cast<int*>(ws + L.coff);
     long long* bsize = reinterpret_cast<long long*>(ws + L.bsize);
@@ -690,10 +698,9 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
     int* ifirst = reinterpret_cast<int*>(ws + L.ifirst);
     BtItem* items = reinterpret_cast<BtItem*>(ws + L.items);
     float4* sorted = reinterpret_cast<float4*>(ws + L.sorted);
-    int* sidx = reinterpret_cast<int*>(ws + L.sidx);
     const float4* q = reinterpret_cast<const float4*>(xyzm);
     const int cgrid = (int)std::min<long long>(nchunk, (long long)sm_count() * 8);
-    k_bt_hist<<<cgrid, 256, 0, st>>>(f, q, dchunks, (int)nchunk, L.nwin, pidx, ccount);
+    k_bt_hist<<<cgrid, 256, 0, st>>>(f, q, dchunks, (int)nchunk, L.nwin, ccount);
     XT_CHECK_LAUNCH("k_bt_hist");
     k_bt_offsets<<<nsnap, 256, 0, st>>>(dcfirst, L.nwin, ccount, coff, bsize);
     XT_CHECK_LAUNCH("k_bt_offsets");
@@ -701,13 +708,12 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
     XT_CHECK_LAUNCH("k_bt_buckets");
     k_bt_items<<<(L.nb + 255) / 256, 256, 0, st>>>(bsize, bbase, ifirst, L.nb, L.nwin, chunk, items);
     XT_CHECK_LAUNCH("k_bt_items");
-    k_bt_scatter<<<cgrid, 256, 0, st>>>(q, dchunks, (int)nchunk, L.nwin, pidx, coff, bbase, n_total, sorted, sidx,
+    k_bt_scatter<<<cgrid, 256, 0, st>>>(f, q, dchunks, (int)nchunk, L.nwin, coff, bbase, n_total, sorted,
                                         err);
     XT_CHECK_LAUNCH("k_bt_scatter");
     BtArgs A;
     A.T = f;
     A.sorted = sorted;
-    A.sidx = sidx;
     A.items = items;
     A.nitems = ctr;
     A.counter = ctr + 1;

@@ -57,6 +57,16 @@ int resident_blocks_per_sm(const void* fn, int block, size_t smem);
 // block does not fit.
 int resident_blocks_full_carveout(const void* fn, int block, size_t smem);
 
+// Blocks of a kernel that allocates `tmem_cols` tensor-memory columns per
+// block, resident per SM, from the SM's own limits: registers (per-thread
+// count rounded to 8, per warp to 256), threads, blocks, shared memory under
+// the full carveout (as above) and the 512 tensor-memory columns.  The
+// occupancy API answers 1 for kernels that contain tcgen05.alloc whatever
+// their resources (measured on GB300: four 128-thread CTAs of 49 KB run
+// together and take 6.4 ms where one per SM takes 12.3 ms), so it is not
+// asked.  Returns 0 when a block does not fit.
+int resident_blocks_tmem(const void* fn, int block, size_t smem, int tmem_cols);
+
 // Grid of at most one full wave: as many blocks as stay resident together, or
 // fewer when `units` (one per thread) needs fewer.  Grid-stride kernels launched
 // this way balance their work over every resident block instead of leaving a

@@ -918,9 +918,11 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
 // Double-float evaluation of the binned records (FP64 path,
 // accumulated_eval_particles); SORTED as for k_cyl_eval_sorted.
 // Launch bounds and the twice-unrolled m loop were measured on 1e6 disc
-// particles: 0.129 ms with up to ~127 registers, against 0.135 ms at 72.
+// particles: 0.129 ms with up to ~127 registers, against 0.135 ms at 72;
+// asking for 5 resident blocks (at most 102 registers) gives 0.121 ms, 6
+// blocks or a rolled m loop 0.127 ms.
 template <bool SORTED>
-__global__ void __launch_bounds__(128, 1) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
+__global__ void __launch_bounds__(128, 5) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
                                                             const BinRec<df>* __restrict__ recs, int m1, int m2,
                                                             double* o0, double* o1, double* o2, double* o3,
                                                             double* o4) {

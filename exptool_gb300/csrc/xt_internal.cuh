@@ -10,7 +10,10 @@ bool sph_efp(void* handle, const double** efp);   // ef/sqrt(ev) table [l][n][no
 bool sph_efp_df(void* handle, const float2** efp_df);   // the same as FP32 (hi, lo) pairs
 bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f);
 // expcoef[s, row, n] = sum_node efp[l, n, node] G[s, row, node] for nsnap
-// snapshot grids G, in double-float from the split table efp_df (xt_batch.cu)
+// snapshot grids G (FP64, or double-float (hi, lo) pairs), in double-float
+// from the split table efp_df (xt_batch.cu)
 int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
+                                double* out, cudaStream_t st);
+int launch_sph_contract_batched(const float2* efp_df, const float2* G, int nsnap, int lmax, int nmax, int numr,
                                 double* out, cudaStream_t st);
 }  // namespace xt

@@ -14,6 +14,7 @@
 // nmax-long dot products.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
@@ -92,6 +93,36 @@ int resident_blocks_full_carveout(const void* fn, int block, size_t smem) {
   const size_t per_block = (smem + fa.sharedSizeBytes + (size_t)reserved + 127) / 128 * 128;
   const int by_smem = (int)((size_t)per_sm_smem / per_block);
   return by_smem < other ? by_smem : other;
+}
+
+int resident_blocks_tmem(const void* fn, int block, size_t smem, int tmem_cols) {
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0, per_sm_smem = 0, reserved = 0, regs_sm = 0, threads_sm = 0, blocks_sm = 0;
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&blocks_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (block < 1 || block > fa.maxThreadsPerBlock || tmem_cols < 1 || tmem_cols > 512) return 0;
+  const int warps = (block + 31) / 32;
+  const int regs_warp = ((((fa.numRegs > 0 ? fa.numRegs : 1) + 7) / 8 * 8) * 32 + 255) / 256 * 256;
+  int v = regs_sm / (regs_warp * warps);
+  v = std::min(v, threads_sm / (warps * 32));
+  v = std::min(v, blocks_sm);
+  const size_t per_block = (smem + fa.sharedSizeBytes + (size_t)reserved + 127) / 128 * 128;
+  v = std::min(v, (int)((size_t)per_sm_smem / per_block));
+  v = std::min(v, 512 / tmem_cols);
+  return v < 0 ? 0 : v;
 }
 
 int grid_for(long long n, int block, int blocks_per_sm) {
