@@ -920,7 +920,10 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
 // Launch bounds and the twice-unrolled m loop were measured on 1e6 disc
 // particles: 0.129 ms with up to ~127 registers, against 0.135 ms at 72;
 // asking for 5 resident blocks (at most 102 registers) gives 0.121 ms, 6
-// blocks or a rolled m loop 0.127 ms.
+// blocks or a rolled m loop 0.127 ms.  Two threads per record (orders split
+// between the lanes of a pair, sums exchanged by shuffles; 64 registers, twice
+// the warps) took 0.152 ms: the kernel is bound by its double-float
+// instruction count, not by latency.
 template <bool SORTED>
 __global__ void __launch_bounds__(128, 5) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
                                                             const BinRec<df>* __restrict__ recs, int m1, int m2,
