@@ -31,10 +31,6 @@ template <typename R, int LC>
 void launch_sph_eval(const SphTab<R>& T, const R* GH, int coord_mode, const double* a, const double* b,
                      const double* c, long long n, const SphEvalOpts& o, double* const* outs, int grid, int block,
                      cudaStream_t st);
-// FP64 spherical evaluation in double-float arithmetic (xt_sph_df.cu)
-template <int LC>
-void launch_sph_eval_df(const SphTab<double>& T, const double* GH, int coord_mode, const double* a, const double* b,
-                        const double* c, long long n, const SphEvalOpts& o, double* const* outs, cudaStream_t st);
 template <typename R, int LC>
 void launch_fields_forces(const SphTab<R>& ST, const R* GH, const CylTab<R>& CT, const R* F, const FieldOpts& fo,
                           const double* x, const double* y, const double* z, const double* rot, double rot_scalar,

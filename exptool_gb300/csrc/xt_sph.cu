@@ -209,15 +209,11 @@ __global__ void __launch_bounds__(256) k_sph_contract(const double* __restrict__
   }
 }
 
-// FP64 field (drop-in path), SphFieldLayout<double>:
-// GH[(node*nrow + row)*4 + {0,1}] = sum_{n<nuse} s*c[row,n]*{efp,efd}[l,n,node]
-// for rows with l <= luse (others 0), and + {2,3} the differences D1, D2 of
-// H = p0 G centred on the node (its neighbours' G recomputed by the same sums,
-// so bit-identical to theirs).
+// FP64 field (drop-in path): GH[(node*nrow + row)*2 + {0,1}] =
+// sum_{n<nuse} s*c[row,n]*{efp,efd}[l,n,node] for rows with l <= luse (others 0).
 __global__ void __launch_bounds__(256) k_sph_field(const double* __restrict__ efp, const double* __restrict__ efd,
-                                                   const double* __restrict__ p0, const double* __restrict__ coef,
-                                                   double scale, int lmax, int nmax, int numr, int luse, int nuse,
-                                                   double* __restrict__ GH) {
+                                                   const double* __restrict__ coef, double scale, int lmax, int nmax,
+                                                   int numr, int luse, int nuse, double* __restrict__ GH) {
   const int nrow = (lmax + 1) * (lmax + 1);
   const long long total = (long long)numr * nrow;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -226,30 +222,17 @@ __global__ void __launch_bounds__(256) k_sph_field(const double* __restrict__ ef
     const int row = (int)(t % nrow);
     int l = 0;
     while ((l + 1) * (l + 1) <= row) ++l;
-    double g = 0.0, h = 0.0, gm = 0.0, gp = 0.0;
-    const bool inner = node >= 1 && node <= numr - 2;
+    double g = 0.0, h = 0.0;
     if (l <= luse) {
       for (int n = 0; n < nuse; ++n) {
         const double c = scale * coef[(size_t)row * nmax + n];
         const size_t ix = ((size_t)l * nmax + n) * numr + node;
         g += c * efp[ix];
         h += c * efd[ix];
-        if (inner) {
-          gm += c * efp[ix - 1];
-          gp += c * efp[ix + 1];
-        }
       }
     }
-    double d1 = 0.0, d2 = 0.0;
-    if (inner) {
-      const double hm = p0[node - 1] * gm, h0 = p0[node] * g, hp = p0[node + 1] * gp;
-      d1 = 0.5 * (hp - hm);
-      d2 = hm - 2.0 * h0 + hp;
-    }
-    GH[4 * t] = g;
-    GH[4 * t + 1] = h;
-    GH[4 * t + 2] = d1;
-    GH[4 * t + 3] = d2;
+    GH[2 * t] = g;
+    GH[2 * t + 1] = h;
   }
 }
 
@@ -603,8 +586,8 @@ int xt_sph_prepare(void* handle, const double* expcoef, double coef_scale, int l
   const long long total = (long long)h->numr * sph_nrow(h->lmax);
   const int grid = grid_for(total, 256, 4);
   if (precision == XT_F64) {
-    k_sph_field<<<grid, 256, 0, st>>>(h->efp, h->efd, h->p0, expcoef, coef_scale, h->lmax, h->nmax, h->numr,
-                                      lmax_use, nmax_use, static_cast<double*>(field));
+    k_sph_field<<<grid, 256, 0, st>>>(h->efp, h->efd, expcoef, coef_scale, h->lmax, h->nmax, h->numr, lmax_use,
+                                      nmax_use, static_cast<double*>(field));
   } else {
     float* f = static_cast<float*>(field);
     k_sph_field32<<<grid, 256, 0, st>>>(h->efp, h->efd, h->p0, expcoef, coef_scale, h->lmax, h->nmax, h->numr,
@@ -636,7 +619,8 @@ int xt_sph_eval_points(void* handle, const void* field, int precision, int coord
   int rc = with_lcap(h->lmax, [&](auto lc) {
     constexpr int LC = decltype(lc)::value;
     if (precision == XT_F64)
-      launch_sph_eval_df<LC>(h->tab_d, static_cast<const double*>(field), coord_mode, a, b, c, n, o, outs, st);
+      launch_sph_eval<double, LC>(h->tab_d, static_cast<const double*>(field), coord_mode, a, b, c, n, o, outs, grid,
+                                  block, st);
     else
       launch_sph_eval<float, LC>(h->tab_f, static_cast<const float*>(field), coord_mode, a, b, c, n, o, outs, grid,
                                  block, st);

@@ -49,11 +49,7 @@ struct SphBins {
 };
 
 // Coefficient-contracted SL fields.  FP64 (the drop-in path): per node, per
-// row, (G, Gd, D1, D2): (G, Gd) = sum_n c[row,n] ef[l,n,node] {1/sqrt(ev),
-// sqrt(ev)} and, centred on the node j (1 <= j <= numr-2, else 0), the
-// differences D1 = (H[j+1]-H[j-1])/2, D2 = H[j-1]-2H[j]+H[j+1] of H = p0 G,
-// formed in FP64 (the double-float evaluation takes the force from them
-// instead of differencing nearly equal products).
+// row, (G, Gd) = sum_n c[row,n] ef[l,n,node] {1/sqrt(ev), sqrt(ev)}.
 // FP32 (the mixed path), laid out for one 16-byte gather per row: a float4
 // array [numr][nrow] of (G[i], G[i+1], D1[j], D2[j]) with j = max(i, 1),
 // D1 = (H[j+1]-H[j-1])/2, D2 = H[j-1]-2H[j]+H[j+1], H = p0 G (all from FP64
@@ -62,7 +58,7 @@ template <typename R>
 struct SphFieldLayout {
   static constexpr bool f32 = std::is_same<R, float>::value;
   // elements of R per (node, row)
-  static constexpr int per_row = f32 ? 6 : 4;
+  static constexpr int per_row = f32 ? 6 : 2;
 };
 
 template <typename R>
@@ -240,10 +236,9 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
   dlegendre<R, LCAP>(costh, lmax, P, dP);
   R cm[LCAP + 1], sm[LCAP + 1];
   multiples<R, LCAP>(c1, s1, lmax, cm, sm);
-  constexpr int PR = SphFieldLayout<R>::per_row;
-  const R* g0 = GH + (size_t)(B.j - 1) * nrow * PR;
-  const R* g1 = g0 + nrow * PR;
-  const R* g2 = g1 + nrow * PR;
+  const R* g0 = GH + (size_t)(B.j - 1) * nrow * 2;
+  const R* g1 = g0 + nrow * 2;
+  const R* g2 = g1 + nrow * 2;
 
   auto rowvals = [&](int row, R& pot, R& frc, R& den) {
     if constexpr (SphFieldLayout<R>::f32) {
@@ -257,11 +252,11 @@ __device__ __forceinline__ void sph_eval_point(const SphTab<R>& T, const R* __re
         den = R(0);
       }
     } else {
-      R a0 = g0[PR * row], a1 = g1[PR * row], a2 = g2[PR * row];
+      R a0 = g0[2 * row], a1 = g1[2 * row], a2 = g2[2 * row];
       pot = B.wp[0] * a0 + B.wp[1] * a1 + B.wp[2] * a2;
       frc = B.wf[0] * a0 + B.wf[1] * a1 + B.wf[2] * a2;
       if (dens) {
-        R b0 = g0[PR * row + 1], b1 = g1[PR * row + 1], b2 = g2[PR * row + 1];
+        R b0 = g0[2 * row + 1], b1 = g1[2 * row + 1], b2 = g2[2 * row + 1];
         den = B.wd[0] * b0 + B.wd[1] * b1 + B.wd[2] * b2;
       } else {
         den = R(0);
