@@ -197,13 +197,15 @@ def batched_tc_extra(table, xyzm, offs, K=5, fp64_ms=None, refs=None):
     cfg, tune_ms = at.sph_batched_tc_config(table, xyzm, offs)
     ws = torch.empty(table.batched_tc_workspace(offs, cfg["chunk"]), dtype=torch.uint8, device="cuda")
     out = table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"],
-                                      ctas_per_sm=cfg["ctas_per_sm"], workspace=ws)
+                                      ctas_per_sm=cfg["ctas_per_sm"],
+                                      threads_per_particle=cfg["threads_per_particle"], workspace=ws)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(K):
         table.accumulate_batched_tc(xyzm, offs, chunk=cfg["chunk"], stages=cfg["stages"],
-                                    ctas_per_sm=cfg["ctas_per_sm"], workspace=ws)
+                                    ctas_per_sm=cfg["ctas_per_sm"], threads_per_particle=cfg["threads_per_particle"],
+                                    workspace=ws)
     e1.record()
     torch.cuda.synchronize()
     dev.batched_tc_status()
@@ -217,7 +219,8 @@ def batched_tc_extra(table, xyzm, offs, K=5, fp64_ms=None, refs=None):
         errs.append((float(np.max(np.abs(a - b)) / np.max(np.abs(b))), _block_err(a, b, table.lmax)))
     errs = np.array(errs)
     res = {"ms": ms, "particles_per_s": ntot / (ms * 1e-3), "autotuned": cfg,
-           "resident_ctas_per_sm": {st: table.batched_tc_residency(st) for st in (1, 2, 3)},
+           "resident_ctas_per_sm": {f"stages{st}_split{sp}": table.batched_tc_residency(st, sp) for st in (1, 2, 3)
+                                    for sp in (1, 2)},
            "autotune_candidates_ms": {k: round(v, 3) for k, v in tune_ms.items()},
            "tile": "M = 128 radial nodes, N = 64 (49 rows), K = 128 particles per stage, BF16 in, FP32 in TMEM",
            "tensor_flop_per_particle": 2 * 128 * 64,

@@ -61,9 +61,9 @@ _SIGS = {
     "xt_sph_batched_workspace": (c_sz, [c_vp, c_int, c_ll, c_int]),
     "xt_sph_accumulate_batched": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_sz, c_vp]),
     "xt_sph_batched_tc_workspace": (c_sz, [c_vp, c_int, c_vp, c_int]),
-    "xt_sph_accumulate_batched_tc": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_sz,
-                                             c_vp]),
-    "xt_sph_batched_tc_residency": (c_int, [c_vp, c_int, c_vp]),
+    "xt_sph_accumulate_batched_tc": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp,
+                                             c_sz, c_vp]),
+    "xt_sph_batched_tc_residency": (c_int, [c_vp, c_int, c_int, c_vp]),
     "xt_sph_batched_tc_status": (c_int, []),
     "xt_cyl_table_create": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl, c_dbl,
                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.POINTER(c_vp)]),

@@ -101,21 +101,27 @@ def sph_batched_config(table, xyzm, offsets, force=False, sample_snaps=32):
 
 
 def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
-    """Work-item size (particles), operand stages and CTAs per SM of
-    xt_sph_accumulate_batched_tc for this table, tuned on (up to) the first
-    ``sample_snaps`` snapshots of the batch.  The MMA tile is fixed by the
-    table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16, K = 128
-    particles per stage (48 KB of shared memory per stage at lmax 6); the
-    candidates are every chunk x depth x residency from one CTA per SM up to
-    as many as fit at that depth."""
+    """Work-item size (particles), operand stages, CTAs per SM and threads per
+    particle of xt_sph_accumulate_batched_tc for this table, tuned on (up to)
+    the first ``sample_snaps`` snapshots of the batch.  The MMA tile is fixed
+    by the table: M = 128 radial nodes, N = (lmax+1)^2 rows padded to 16,
+    K = 128 particles per stage (48 KB of shared memory per stage at lmax 6).
+    Candidates: chunks of 8k, 16k and 32k particles x 1 to 3 stages x one or
+    two threads per particle x the full residency at that shape and one CTA
+    per SM fewer."""
     import numpy as np
     offs = np.asarray(offsets, dtype=np.int64)
     ns = min(len(offs) - 1, sample_snaps)
     sub_offs = offs[:ns + 1]
     sub = xyzm[:int(sub_offs[-1])]
-    k = key("sph_batched_tc_v3", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
-    cands = [{"chunk": c, "stages": st, "ctas_per_sm": cp} for c in (4096, 8192, 16384, 32768, 65536)
-             for st in (1, 2, 3) for cp in range(1, table.batched_tc_residency(st) + 1)]
+    k = key("sph_batched_tc_v4", lmax=table.lmax, nmax=table.nmax, numr=table.numr)
+    cands = []
+    for sp in (1, 2):
+        for st in (1, 2, 3):
+            res = table.batched_tc_residency(st, sp)
+            for cp in sorted({res, max(1, res - 1)}):
+                for c in (8192, 16384, 32768):
+                    cands.append({"chunk": c, "stages": st, "ctas_per_sm": cp, "threads_per_particle": sp})
     ws = {}
 
     def run(cfg):
@@ -124,6 +130,7 @@ def sph_batched_tc_config(table, xyzm, offsets, force=False, sample_snaps=32):
             ws["t"] = torch.empty(need, dtype=torch.uint8, device=xyzm.device)
             ws["n"] = need
         table.accumulate_batched_tc(sub, sub_offs, chunk=cfg["chunk"], stages=cfg["stages"],
-                                    ctas_per_sm=cfg["ctas_per_sm"], workspace=ws["t"])
+                                    ctas_per_sm=cfg["ctas_per_sm"], threads_per_particle=cfg["threads_per_particle"],
+                                    workspace=ws["t"])
 
     return tune(k, cands, run, force=force)

@@ -255,6 +255,7 @@ class LearnedRadialBasis:
         torch.cuda.synchronize()
         self.steps_done = done
         self.train_seconds = time.perf_counter() - t0
+        _lib.check(self._lib.xt_learned_status(), "learned network training")   # tensor-core GEMM waits
         return self.train_seconds
 
     # ------------------------------------------------------------ inference

@@ -158,13 +158,14 @@ def compute_coefficients_batched(snapshots, sph_file, mod_file, no_odd=False, au
                 from .. import autotune as at
                 cfg, _ = at.sph_batched_tc_config(table, xyzm, offsets)
             else:
-                cfg = {"chunk": 16384, "stages": 1, "ctas_per_sm": 0}
+                cfg = {"chunk": 16384, "stages": 1, "ctas_per_sm": 0, "threads_per_particle": 1}
             chunk = cfg["chunk"] if chunk is None else chunk
             stages = cfg["stages"] if stages is None else stages
-            ctas = cfg["ctas_per_sm"]
+            ctas, split = cfg["ctas_per_sm"], cfg["threads_per_particle"]
         else:
-            ctas = 0
-        out = table.accumulate_batched_tc(xyzm, offsets, no_odd=no_odd, chunk=chunk, stages=stages, ctas_per_sm=ctas)
+            ctas, split = 0, 1
+        out = table.accumulate_batched_tc(xyzm, offsets, no_odd=no_odd, chunk=chunk, stages=stages, ctas_per_sm=ctas,
+                                          threads_per_particle=split)
         host = dev.to_host(out)
         dev.batched_tc_status()
         return host

@@ -320,9 +320,77 @@ __device__ __forceinline__ void bt_legendre(float x, float* P) {
   }
 }
 
-template <int LCAP, int NPAD, int STAGES>
-__global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
+// Two threads per particle: the angular rows are ordered by the parity of m,
+// the even orders (m = 0, 2, ...) in the first 8 * G0 columns of the tile and
+// the odd ones after them, each half a whole number of 8-row groups, so each
+// thread of a pair stores its own 16-byte row chunks.  Within a half: for each
+// m, the cosine rows l = m..LCAP, then the sine rows.  row[slot] is the
+// coefficient row l^2 (m = 0), l^2 + 2m - 1 (cos) or l^2 + 2m (sin), -1 for
+// padding.
+template <int LCAP>
+struct BtPerm {
+  static constexpr int count(int parity) {
+    int c = 0;
+    for (int m = parity; m <= LCAP; m += 2) c += m == 0 ? LCAP + 1 : 2 * (LCAP - m + 1);
+    return c;
+  }
+  static constexpr int G0 = (count(0) + 7) / 8, G1 = (count(1) + 7) / 8;
+  int row[8 * (G0 + G1)];
+  constexpr BtPerm() : row() {
+    for (int s = 0; s < 8 * (G0 + G1); ++s) row[s] = -1;
+    for (int h = 0; h < 2; ++h) {
+      int slot = h ? 8 * G0 : 0;
+      for (int m = h; m <= LCAP; m += 2) {
+        for (int l = m; l <= LCAP; ++l) row[slot++] = l * l + (m == 0 ? 0 : 2 * m - 1);
+        if (m > 0)
+          for (int l = m; l <= LCAP; ++l) row[slot++] = l * l + 2 * m;
+      }
+    }
+  }
+};
+
+// The angular values of one half (H = 0: even m, H = 1: odd m) in the slot
+// order of BtPerm, from the recurrences of bt_legendre.
+template <int LCAP, int H>
+__device__ __forceinline__ void bt_half_values(float x, float somx2, const float* cm, const float* sn, int lmax,
+                                               int no_odd, float* v) {
+  float pmm[LCAP + 1];
+  pmm[0] = 1.f;
+  float fact = 1.f;
+#pragma unroll
+  for (int m = 1; m <= LCAP; ++m) {
+    pmm[m] = pmm[m - 1] * (-fact * somx2);
+    fact += 2.f;
+  }
+  int slot = 0;
+#pragma unroll
+  for (int m = H; m <= LCAP; m += 2) {
+    float Pl[LCAP + 2];
+    Pl[m] = pmm[m];
+    if (m + 1 <= LCAP) Pl[m + 1] = x * (float)(2 * m + 1) * pmm[m];
+#pragma unroll
+    for (int l = m + 2; l <= LCAP; ++l)
+      Pl[l] = (x * (float)(2 * l - 1) * Pl[l - 1] - (float)(l + m - 1) * Pl[l - 2]) * (1.f / (float)(l - m));
+#pragma unroll
+    for (int l = m; l <= LCAP; ++l) {
+      const bool on = l <= lmax && !(no_odd && (l & 1));
+      const float pv = on ? Pl[l] : 0.f;
+      if (m == 0) {
+        v[slot + (l - m)] = pv;
+      } else {
+        v[slot + (l - m)] = pv * cm[m];
+        v[slot + (LCAP - m + 1) + (l - m)] = pv * sn[m];
+      }
+    }
+    slot += m == 0 ? LCAP + 1 : 2 * (LCAP - m + 1);
+  }
+}
+
+template <int LCAP, int NPAD, int STAGES, int SPLIT>
+__global__ void __launch_bounds__(BT_THREADS * SPLIT, SPLIT == 2 ? 3 : 1) k_sph_batched_tc(BtArgs a) {
   using TL = BtTile<NPAD>;
+  using PM = BtPerm<LCAP>;
+  static_assert(SPLIT == 1 || 8 * (PM::G0 + PM::G1) <= NPAD, "split rows exceed the padded tile");
   constexpr int NCOLS = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
   constexpr int NT = (LCAP + 1) * (LCAP + 2) / 2;
   constexpr int NROW = (LCAP + 1) * (LCAP + 1);
@@ -332,6 +400,8 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + STAGES);
   int* s_item = reinterpret_cast<int*>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int kp = tid & (BT_KT - 1);          // this thread's particle slot of a K-tile
+  const int half = SPLIT == 2 ? tid / BT_KT : 0;
   const SphTab<float>& T = a.T;
   const int lmax = T.lmax;
 
@@ -344,7 +414,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
   if (tid < STAGES) mbar_init(smem_u32(bars + tid));
   // operand tiles start at zero: padded angular rows and the weight rows no
   // particle touches stay zero
-  for (int o = tid * 16; o < STAGES * TL::STAGE; o += BT_THREADS * 16)
+  for (int o = tid * 16; o < STAGES * TL::STAGE; o += BT_THREADS * SPLIT * 16)
     *reinterpret_cast<uint4*>(sm + o) = make_uint4(0u, 0u, 0u, 0u);
   fence_async_smem();
   tc_fence_before();
@@ -355,7 +425,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
   const uint32_t idesc = tc_idesc(BT_M, NPAD) | (1u << 16);
   const int nitems = *a.nitems;
   // byte offset of this thread's angular column in a stage's angular tile
-  const int kofs = (tid >> 3) * TL::BSK + (tid & 7) * 16;
+  const int kofs = (kp >> 3) * TL::BSK + (kp & 7) * 16;
   int prev_row[STAGES];
 #pragma unroll
   for (int s = 0; s < STAGES; ++s) prev_row[s] = -1;
@@ -372,11 +442,11 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
     const long long ntile = (I.end - I.begin + BT_KT - 1) / BT_KT;
     // this thread's particle of the next K-tile is loaded one tile ahead
     float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (I.begin + tid < I.end) qn = a.sorted[I.begin + tid];
+    if (I.begin + kp < I.end) qn = a.sorted[I.begin + kp];
     for (long long t = 0; t < ntile; ++t, ++g) {
       const float4 q = qn;
-      const bool have = I.begin + t * BT_KT + tid < I.end;
-      const long long pn = I.begin + (t + 1) * BT_KT + tid;
+      const bool have = I.begin + t * BT_KT + kp < I.end;
+      const long long pn = I.begin + (t + 1) * BT_KT + kp;
       if (pn < I.end) qn = a.sorted[pn];
       // this particle's values, computed before its stage is free
       uint32_t pk[NPAD / 2];
@@ -399,33 +469,49 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
         const float costh = q.z / r;
         float c1, s1;
         unit_phi(q.x, q.y, c1, s1);
-        float P[NT];
-        bt_legendre<LCAP>(costh, P);
         float cm[LCAP + 1], sn[LCAP + 1];
         multiples<float, LCAP>(c1, s1, LCAP, cm, sn);
-        float v[NPAD];
+        if constexpr (SPLIT == 1) {
+          float P[NT];
+          bt_legendre<LCAP>(costh, P);
+          float v[NPAD];
 #pragma unroll
-        for (int k = 0; k < NPAD; ++k) v[k] = 0.f;
-        // the normalisation fact[l][m] is applied in FP64 by k_bt_reduce: a
-        // BF16 rounding of it would bias every particle alike
+          for (int k = 0; k < NPAD; ++k) v[k] = 0.f;
+          // the normalisation fact[l][m] is applied in FP64 by k_bt_reduce: a
+          // BF16 rounding of it would bias every particle alike
 #pragma unroll
-        for (int l = 0; l <= LCAP; ++l) {
-          const bool on = l <= lmax && !(a.no_odd && (l & 1));   // rows of odd l stay zero under no_odd
+          for (int l = 0; l <= LCAP; ++l) {
+            const bool on = l <= lmax && !(a.no_odd && (l & 1));   // rows of odd l stay zero under no_odd
 #pragma unroll
-          for (int m = 0; m <= l; ++m) {
-            const float pv = on ? P[tri(l, m)] : 0.f;
-            if (m == 0) {
-              v[l * l] = pv;
-            } else {
-              v[l * l + 2 * m - 1] = pv * cm[m];
-              v[l * l + 2 * m] = pv * sn[m];
+            for (int m = 0; m <= l; ++m) {
+              const float pv = on ? P[tri(l, m)] : 0.f;
+              if (m == 0) {
+                v[l * l] = pv;
+              } else {
+                v[l * l + 2 * m - 1] = pv * cm[m];
+                v[l * l + 2 * m] = pv * sn[m];
+              }
             }
           }
-        }
 #pragma unroll
-        for (int k = 0; k < NPAD / 2; ++k) {
-          __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
-          pk[k] = *reinterpret_cast<uint32_t*>(&b2);
+          for (int k = 0; k < NPAD / 2; ++k) {
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+            pk[k] = *reinterpret_cast<uint32_t*>(&b2);
+          }
+        } else {
+          // this thread's half of the rows (warp-uniform branch)
+          const float somx2 = sqrtf((1.f - costh) * (1.f + costh));
+          constexpr int NV = 8 * (PM::G0 > PM::G1 ? PM::G0 : PM::G1);
+          float v[NV];
+#pragma unroll
+          for (int k = 0; k < NV; ++k) v[k] = 0.f;
+          if (half == 0) bt_half_values<LCAP, 0>(costh, somx2, cm, sn, lmax, a.no_odd, v);
+          else bt_half_values<LCAP, 1>(costh, somx2, cm, sn, lmax, a.no_odd, v);
+#pragma unroll
+          for (int k = 0; k < NV / 2; ++k) {
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+            pk[k] = *reinterpret_cast<uint32_t*>(&b2);
+          }
         }
       }
       const int st = (int)(g % STAGES);
@@ -442,27 +528,38 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
 #pragma unroll
       for (int s = 0; s < STAGES; ++s)
         if (s == st) pr = prev_row[s];
-      if (pr >= 0) {
-        *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr, tid)) = __float2bfloat16_rn(0.f);
-        *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr + 1, tid)) = __float2bfloat16_rn(0.f);
-      }
       int nr = -1;
-      if (have) {
-        if (li >= 0 && li < BT_NODES) {
-          bt_st(At, li, tid, w0);
-          bt_st(At, li + 1, tid, w1);
-          nr = li;
-        } else {
-          atomicExch(a.err, 3);
+      if (half == 0) {                           // the weights: one thread per particle
+        if (pr >= 0) {
+          *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr, kp)) = __float2bfloat16_rn(0.f);
+          *reinterpret_cast<__nv_bfloat16*>(At + bt_off(pr + 1, kp)) = __float2bfloat16_rn(0.f);
+        }
+        if (have) {
+          if (li >= 0 && li < BT_NODES) {
+            bt_st(At, li, kp, w0);
+            bt_st(At, li + 1, kp, w1);
+            nr = li;
+          } else {
+            atomicExch(a.err, 3);
+          }
         }
       }
-      // the angular column: (NROW + 7) / 8 chunks of 8 rows (rows past NROW are
-      // zero from the start and never written); zeros for a missing particle
-      // (a stale non-finite value would survive zero weights)
+      // the angular column: chunks of 8 rows (rows no chunk covers are zero
+      // from the start and never written); zeros for a missing particle (a
+      // stale non-finite value would survive zero weights)
+      if constexpr (SPLIT == 1) {
 #pragma unroll
-      for (int c = 0; c < (NROW + 7) / 8; ++c)
-        *reinterpret_cast<uint4*>(Bt + kofs + c * 128) =
-            make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
+        for (int c = 0; c < (NROW + 7) / 8; ++c)
+          *reinterpret_cast<uint4*>(Bt + kofs + c * 128) =
+              make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
+      } else {
+        const int g0 = half ? PM::G0 : 0, ng = half ? PM::G1 : PM::G0;
+#pragma unroll
+        for (int c = 0; c < (PM::G0 > PM::G1 ? PM::G0 : PM::G1); ++c)
+          if (c < ng)
+            *reinterpret_cast<uint4*>(Bt + kofs + (g0 + c) * 128) =
+                make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
+      }
 #pragma unroll
       for (int s = 0; s < STAGES; ++s)
         if (s == st) prev_row[s] = nr;
@@ -489,16 +586,37 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_sph_batched_tc(BtArgs a) {
       break;
     }
     tc_fence_after();
-    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-    float* dst = a.partial + (size_t)it * a.nrow * BT_M + 32 * warp + (tid & 31);
+    // a warp reads its quarter's lanes; with two threads per particle the
+    // second warpgroup reads the second half of the columns
+    const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    float* dst = a.partial + (size_t)it * a.nrow * BT_M + 32 * (warp & 3) + (tid & 31);
+    if constexpr (SPLIT == 1) {
 #pragma unroll 1
-    for (int c16 = 0; c16 < NPAD / 16; ++c16) {
-      float v[16];
-      tc_ld16(trow + 16 * c16, v);
+      for (int c16 = 0; c16 < NPAD / 16; ++c16) {
+        float v[16];
+        tc_ld16(trow + 16 * c16, v);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int row = 16 * c16 + j;
-        if (row < a.nrow) dst[(size_t)row * BT_M] = v[j];
+        for (int j = 0; j < 16; ++j) {
+          const int row = 16 * c16 + j;
+          if (row < a.nrow) dst[(size_t)row * BT_M] = v[j];
+        }
+      }
+    } else {
+      constexpr PM perm{};
+      constexpr int HALF = NPAD / 2;
+      static_assert(HALF % 16 == 0, "column halves of whole 16-column loads");
+#pragma unroll
+      for (int c16 = 0; c16 < HALF / 16; ++c16) {
+        float v[16];
+        const int col0 = (warp >> 2) * HALF + 16 * c16;
+        tc_ld16(trow + col0, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c0 = 16 * c16 + j;       // column within this warpgroup's half
+          const int row = (warp >> 2) ? (HALF + c0 < 8 * (PM::G0 + PM::G1) ? perm.row[HALF + c0] : -1)
+                                      : (c0 < 8 * (PM::G0 + PM::G1) ? perm.row[c0] : -1);
+          if (row >= 0 && row < a.nrow) dst[(size_t)row * BT_M] = v[j];
+        }
       }
     }
     tc_fence_before();
@@ -597,27 +715,35 @@ static long long bt_nchunk(const long long* off, int nsnap) {
   return n;
 }
 
-// CTAs of k_sph_batched_tc<LC, NPAD, STAGES> resident per SM: as many as the
-// registers, the whole unified L1/shared storage as shared memory (the default
-// carveout leaves one per SM) and the SM's 512 tensor-memory columns allow; 0
-// if none.
-template <int LC, int NPAD, int STAGES>
+// CTAs of k_sph_batched_tc<LC, NPAD, STAGES, SPLIT> resident per SM: as many
+// as the registers, the whole unified L1/shared storage as shared memory (the
+// default carveout leaves one per SM) and the SM's 512 tensor-memory columns
+// allow; 0 if none.
+template <int LC, int NPAD, int STAGES, int SPLIT>
 static int bt_residency() {
   constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
   constexpr int ncols = NPAD <= 32 ? 32 : (NPAD <= 64 ? 64 : (NPAD <= 128 ? 128 : 256));
-  return resident_blocks_tmem((const void*)k_sph_batched_tc<LC, NPAD, STAGES>, BT_THREADS, smem, ncols);
+  return resident_blocks_tmem((const void*)k_sph_batched_tc<LC, NPAD, STAGES, SPLIT>, BT_THREADS * SPLIT, smem,
+                              ncols);
 }
 
 // Persistent launch of ctas_per_sm CTAs per SM (0: as many as are resident).
-template <int LC, int NPAD, int STAGES>
+template <int LC, int NPAD, int STAGES, int SPLIT>
 static int bt_launch_gemm(const BtArgs& A, int ctas_per_sm, cudaStream_t st) {
   constexpr size_t smem = (size_t)STAGES * BtTile<NPAD>::STAGE + STAGES * 8 + 8;
-  int per_sm = bt_residency<LC, NPAD, STAGES>();
+  int per_sm = bt_residency<LC, NPAD, STAGES, SPLIT>();
   XT_REQUIRE(per_sm >= 1, "k_sph_batched_tc does not fit on an SM with %zu bytes of shared memory", smem);
   if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
-  k_sph_batched_tc<LC, NPAD, STAGES><<<sm_count() * per_sm, BT_THREADS, smem, st>>>(A);
+  k_sph_batched_tc<LC, NPAD, STAGES, SPLIT><<<sm_count() * per_sm, BT_THREADS * SPLIT, smem, st>>>(A);
   XT_CHECK_LAUNCH("k_sph_batched_tc");
   return XT_OK;
+}
+
+// Dispatch on the threads per particle.
+template <typename F>
+static int bt_with_split(int split, F&& f) {
+  if (split == 2) return f(std::integral_constant<int, 2>{});
+  return f(std::integral_constant<int, 1>{});
 }
 
 // Dispatch on the pipeline depth.
@@ -643,8 +769,8 @@ size_t xt_sph_batched_tc_workspace(void* handle, int nsnap, const long long* off
 }
 
 int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long long* offsets_host, int nsnap,
-                                 int no_odd, int chunk, int stages, int ctas_per_sm, double* expcoef_out,
-                                 void* workspace, size_t workspace_bytes, void* stream) {
+                                 int no_odd, int chunk, int stages, int ctas_per_sm, int threads_per_particle,
+                                 double* expcoef_out, void* workspace, size_t workspace_bytes, void* stream) {
   SphTab<double> d;
   SphTab<float> f;
   XT_REQUIRE(sph_tabs(handle, &d, &f), "NULL table handle");
@@ -652,6 +778,7 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
   XT_REQUIRE(chunk >= BT_KT && chunk <= (1 << 30), "chunk must be in [%d, 2^30] particles", BT_KT);
   XT_REQUIRE(stages >= 1 && stages <= 3, "stages must be 1, 2 or 3");
   XT_REQUIRE(ctas_per_sm >= 0, "ctas_per_sm must be >= 0 (0: as many as are resident)");
+  XT_REQUIRE(threads_per_particle == 1 || threads_per_particle == 2, "threads_per_particle must be 1 or 2");
   XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
   XT_REQUIRE(d.numr >= 2 && (d.numr - 2) / BT_NODES + 1 <= BT_MAXWIN, "numr must be in [2, %d]",
              BT_MAXWIN * BT_NODES + 1);
@@ -725,7 +852,9 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
       constexpr int LC = decltype(lc)::value;
       constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
       return bt_with_stages<LC, NPAD>(stages, [&](auto sc) -> int {
-        return bt_launch_gemm<LC, NPAD, decltype(sc)::value>(A, ctas_per_sm, st);
+        return bt_with_split(threads_per_particle, [&](auto pc) -> int {
+          return bt_launch_gemm<LC, NPAD, decltype(sc)::value, decltype(pc)::value>(A, ctas_per_sm, st);
+        });
       });
     });
     if (rc) return rc;
@@ -739,10 +868,11 @@ int xt_sph_accumulate_batched_tc(void* handle, const float* xyzm, const long lon
   return launch_sph_contract_batched(efp_df, G, nsnap, d.lmax, d.nmax, d.numr, expcoef_out, st);
 }
 
-int xt_sph_batched_tc_residency(void* handle, int stages, int* ctas_per_sm) {
+int xt_sph_batched_tc_residency(void* handle, int stages, int threads_per_particle, int* ctas_per_sm) {
   SphTab<double> d;
   XT_REQUIRE(sph_tabs(handle, &d, nullptr), "NULL table handle");
   XT_REQUIRE(stages >= 1 && stages <= 3, "stages must be 1, 2 or 3");
+  XT_REQUIRE(threads_per_particle == 1 || threads_per_particle == 2, "threads_per_particle must be 1 or 2");
   XT_REQUIRE(ctas_per_sm, "NULL output");
   XT_REQUIRE(d.lmax <= 8, "the batched path supports lmax <= 8");
   int v = 0;
@@ -750,8 +880,10 @@ int xt_sph_batched_tc_residency(void* handle, int stages, int* ctas_per_sm) {
     constexpr int LC = decltype(lc)::value;
     constexpr int NPAD = ((LC + 1) * (LC + 1) + 15) / 16 * 16;
     return bt_with_stages<LC, NPAD>(stages, [&](auto sc) -> int {
-      v = bt_residency<LC, NPAD, decltype(sc)::value>();
-      return XT_OK;
+      return bt_with_split(threads_per_particle, [&](auto pc) -> int {
+        v = bt_residency<LC, NPAD, decltype(sc)::value, decltype(pc)::value>();
+        return XT_OK;
+      });
     });
   });
   *ctas_per_sm = v;

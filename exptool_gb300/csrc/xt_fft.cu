@@ -5,8 +5,9 @@
 // Fourier transform the reference takes with numpy.fft.fft is computed in
 // double-float complex arithmetic on the FP32 pipe (GB300's FP64 pipe issues
 // at a small fraction of the FP32 rate):
-//  * N a power of two: one radix-2 Stockham FFT of size M = N in shared memory
-//    (two ping-pong buffers, natural-order output, no bit reversal);
+//  * N a power of two: one Stockham FFT of size M = N in shared memory,
+//    radix-4 stages after at most one radix-2 stage (two ping-pong buffers,
+//    natural-order output, no bit reversal);
 //  * other N: Bluestein's chirp-z transform, X[k] = w[k] sum_n x[n] w[n]
 //    conj(w[k - n]) with w[n] = exp(-i pi n^2 / N), as a circular convolution of
 //    size M = 2^p >= 2N - 1 by two FFTs and the precomputed FFT of the chirp.
@@ -46,22 +47,59 @@ __device__ __forceinline__ void c_st(float4* p, cdf a) { *p = make_float4(a.re.h
 __device__ __forceinline__ bool df_gt(df a, df b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
 __device__ __forceinline__ df df_absv(df a) { return a.h < 0.f ? df_neg(a) : a; }
 
-// In-shared-memory radix-2 Stockham FFT of size m (a power of two) from x,
-// using y as the other buffer; returns the buffer holding the result.
-// tw[t] = exp(-2 pi i t / m), t < m/2.  All threads of the CTA take part.
+// exp(-2 pi i t / m) for 0 <= t < m from the half table tw[t] (t < m / 2):
+// W^t = -W^(t - m/2).
+__device__ __forceinline__ cdf twiddle(const float4* __restrict__ tw, int t, int half) {
+  cdf w = c_ld(tw + (t < half ? t : t - half));
+  if (t >= half) {
+    w.re = df_neg(w.re);
+    w.im = df_neg(w.im);
+  }
+  return w;
+}
+
+// In-shared-memory Stockham FFT of size m (a power of two) from x, using y
+// as the other buffer; returns the buffer holding the result (natural
+// order).  Radix-4 stages (a leading radix-2 stage when log2 m is odd): a
+// butterfly at offset j of sub-transform size ns reads x[j + r m/4], r < 4,
+// multiplies by W_{4ns}^{r k} (k = j mod ns) and writes the four outputs of
+// the 4-point DFT (W_4 = -i) to y[(j - k) 4 + k + r ns].  tw[t] =
+// exp(-2 pi i t / m), t < m/2.  All threads of the CTA take part.
 __device__ float4* fft_stockham(float4* x, float4* y, int m, const float4* __restrict__ tw) {
   const int half = m >> 1;
-  for (int ns = 1; ns < m; ns <<= 1) {
-    const int step = m / (2 * ns);                  // W_{2 ns}^k = W_m^{k m / (2 ns)}
-#pragma unroll 4
+  int ns = 1;
+  if ((31 - __clz(m)) & 1) {                   // radix-2 stage, ns = 1: no twiddles
     for (int j = threadIdx.x; j < half; j += blockDim.x) {
+      const cdf v0 = c_ld(x + j), v1 = c_ld(x + j + half);
+      c_st(y + 2 * j, c_add(v0, v1));
+      c_st(y + 2 * j + 1, c_sub(v0, v1));
+    }
+    __syncthreads();
+    float4* t = x;
+    x = y;
+    y = t;
+    ns = 2;
+  }
+  const int q = m >> 2;
+  for (; ns < m; ns <<= 2) {
+    const int step = m / (4 * ns);               // W_{4 ns}^k = W_m^{k m / (4 ns)}
+#pragma unroll 2
+    for (int j = threadIdx.x; j < q; j += blockDim.x) {
       const int k = j & (ns - 1);
-      const cdf v0 = c_ld(x + j);
-      cdf v1 = c_ld(x + j + half);
-      if (k) v1 = c_mul(v1, c_ld(tw + k * step));
-      const int d = ((j - k) << 1) + k;             // (j / ns) * 2 ns + k
-      c_st(y + d, c_add(v0, v1));
-      c_st(y + d + ns, c_sub(v0, v1));
+      const cdf a0 = c_ld(x + j);
+      cdf a1 = c_ld(x + j + q), a2 = c_ld(x + j + 2 * q), a3 = c_ld(x + j + 3 * q);
+      if (k) {
+        a1 = c_mul(a1, twiddle(tw, k * step, half));
+        a2 = c_mul(a2, twiddle(tw, 2 * k * step, half));
+        a3 = c_mul(a3, twiddle(tw, 3 * k * step, half));
+      }
+      const cdf t0 = c_add(a0, a2), t1 = c_sub(a0, a2), t2 = c_add(a1, a3), d13 = c_sub(a1, a3);
+      const cdf t3{d13.im, df_neg(d13.re)};      // -i (a1 - a3)
+      const int d = ((j - k) << 2) + k;
+      c_st(y + d, c_add(t0, t2));
+      c_st(y + d + ns, c_add(t1, t3));
+      c_st(y + d + 2 * ns, c_sub(t0, t2));
+      c_st(y + d + 3 * ns, c_sub(t1, t3));
     }
     __syncthreads();
     float4* t = x;

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "xt_mlp.cuh"
+#include "xt_tc.cuh"
 
 namespace xt {
 
@@ -21,8 +22,8 @@ constexpr int NOP = MLP_NOP;
 // C[M x N] = opA(A) [M x K] * opB(B) [K x N], BF16 operands, FP32 accumulation.
 //   TA = 0: A stored [M][lda] (k contiguous);  TA = 1: A stored [K][lda] (m contiguous)
 //   TB = 0: B stored [N][ldb] (k contiguous);  TB = 1: B stored [K][ldb] (n contiguous)
-// Tile 64 x 64 x 32, 4 warps each computing 32 x 32 with m16n8k16 MMAs.
-// M, N multiples of 64; K a multiple of 32 * ksplit; blockIdx.z = l * ksplit + kpart.
+// blockIdx.z = l * ksplit + kpart (the L networks batched along z, split-K
+// parts accumulated by EPI_ATOMIC).
 enum { EPI_STORE = 0, EPI_BIAS_SILU = 1, EPI_DSILU = 2, EPI_ATOMIC = 3, EPI_BIAS = 4 };
 
 struct GemmArgs {
@@ -38,110 +39,192 @@ struct GemmArgs {
   long long sBias;
   __nv_bfloat16* Hout;       // bf16 activation output (EPI_BIAS_SILU, EPI_DSILU), ld = ldc, stride sC
   const float* Zsaved;       // pre-activations for EPI_DSILU (ld = ldc, stride sC)
+  int* err;                  // set to 1 on an MMA wait timeout (the learned path's flag, xt_learned_status)
 };
 
-template <int TA, int TB, int EPI>
-__global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g) {
-  constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
-  __shared__ __align__(16) __nv_bfloat16 As[BM][BK + PAD];
-  __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + PAD];
+// One CTA per 128 x BN output tile on the 5th-generation tensor cores: K in
+// steps of 64, both operands staged by cp.async (16-byte copies, rows beyond M
+// zero-filled) into the canonical no-swizzle layouts, K-major when the
+// operand is stored k-contiguous (8-row x 16-byte core matrices, 128 bytes
+// apart along K, 1024 apart across 8-row groups) and MN-major when it is
+// stored m- or n-contiguous (8 x 16-byte core matrices along the rows, 128
+// bytes apart, k groups of 8 a full tile width apart; instruction-descriptor
+// bits 15 and 16); two stages, so the copies of step k+1 run while the MMAs
+// of step k do.  One thread issues the four K = 16 MMAs of a step and commits
+// them to the stage's mbarrier; waits are bounded and a timeout sets the
+// learned path's error flag (read by xt_learned_status).  The FP32 accumulator (128 lanes x BN columns of tensor
+// memory) is read by tcgen05.ld for the epilogue and transposed through
+// shared memory, so that the stores (and the bias, Z and atomic accesses) are
+// row segments of 32 consecutive columns per warp instruction.
+constexpr int GT_M = 128, GT_BK = 64, GT_STAGES = 2;
+
+template <int BN>
+struct GtTile {
+  static constexpr int A_BYTES = GT_M * GT_BK * 2;
+  static constexpr int B_BYTES = BN * GT_BK * 2;
+  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int SMEM = GT_STAGES * STAGE + 64;
+};
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Copies of one operand tile (ROWS x 64 of K) into the canonical layout.
+template <int T, int ROWS>
+__device__ __forceinline__ void gt_stage(uint32_t dst, const __nv_bfloat16* src, int ld, int r0, int rmax, int k0) {
+  if (T == 0) {                                   // [rows][ld], k contiguous: K-major
+    for (int c = threadIdx.x; c < ROWS * (GT_BK / 8); c += blockDim.x) {
+      const int row = c >> 3, kc = c & 7;
+      const bool ok = r0 + row < rmax;
+      cp16(dst + (row >> 3) * ((GT_BK / 8) * 128) + kc * 128 + (row & 7) * 16,
+           ok ? src + (size_t)(r0 + row) * ld + k0 + 8 * kc : src, ok);
+    }
+  } else {                                        // [k][ld], rows contiguous: MN-major
+    for (int c = threadIdx.x; c < GT_BK * (ROWS / 8); c += blockDim.x) {
+      const int k = c / (ROWS / 8), rc = c % (ROWS / 8);
+      const bool ok = r0 + 8 * rc < rmax;
+      cp16(dst + (k >> 3) * ((ROWS / 8) * 128) + rc * 128 + (k & 7) * 16,
+           ok ? src + (size_t)(k0 + k) * ld + r0 + 8 * rc : src, ok);
+    }
+  }
+}
+
+template <int T, int ROWS>
+__device__ __forceinline__ uint64_t gt_desc(uint32_t base, int kk) {
+  if (T == 0) return tc_desc(base + kk * 256, 128, (GT_BK / 8) * 128);
+  return tc_desc(base + kk * 2 * ((ROWS / 8) * 128), (ROWS / 8) * 128, 128);
+}
+
+template <int TA, int TB, int EPI, int BN>
+__global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
+  using TL = GtTile<BN>;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + GT_STAGES * TL::STAGE);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + GT_STAGES);
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int l = blockIdx.z / g.ksplit, kpart = blockIdx.z % g.ksplit;
   const __nv_bfloat16* A = g.A + l * g.sA;
   const __nv_bfloat16* B = g.B + l * g.sB;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-  const int kchunk = g.K / g.ksplit;
-  const int kbeg = kpart * kchunk, kend = kbeg + kchunk;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  const int gq = lane >> 2, tq = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    if (TA == 0) {
-      for (int c = tid; c < BM * BK / 8; c += 128) {
-        const int r = c / (BK / 8), cc = (c % (BK / 8)) * 8;
-        *reinterpret_cast<uint4*>(&As[r][cc]) =
-            *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * g.lda + k0 + cc);
-      }
-    } else {
-      for (int c = tid; c < BM * BK; c += 128) {
-        const int kk = c / BM, mm = c % BM;
-        As[mm][kk] = A[(size_t)(k0 + kk) * g.lda + m0 + mm];
-      }
-    }
-    if (TB == 0) {
-      for (int c = tid; c < BN * BK / 8; c += 128) {
-        const int r = c / (BK / 8), cc = (c % (BK / 8)) * 8;
-        *reinterpret_cast<uint4*>(&Bs[r][cc]) =
-            *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * g.ldb + k0 + cc);
-      }
-    } else {
-      for (int c = tid; c < BN * BK; c += 128) {
-        const int kk = c / BN, nn = c % BN;
-        Bs[nn][kk] = B[(size_t)(k0 + kk) * g.ldb + n0 + nn];
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      unsigned af[2][4], bfr[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int mr = wm + i * 16 + gq;
-        af[i][0] = *reinterpret_cast<const unsigned*>(&As[mr][ks + 2 * tq]);
-        af[i][1] = *reinterpret_cast<const unsigned*>(&As[mr + 8][ks + 2 * tq]);
-        af[i][2] = *reinterpret_cast<const unsigned*>(&As[mr][ks + 2 * tq + 8]);
-        af[i][3] = *reinterpret_cast<const unsigned*>(&As[mr + 8][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int nr = wn + j * 8 + gq;
-        bfr[j][0] = *reinterpret_cast<const unsigned*>(&Bs[nr][ks + 2 * tq]);
-        bfr[j][1] = *reinterpret_cast<const unsigned*>(&Bs[nr][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16_16816(acc[i][j], af[i], bfr[j][0], bfr[j][1]);
-    }
-    __syncthreads();
+  const int m0 = blockIdx.x * GT_M, n0 = blockIdx.y * BN;
+  const int kchunk = g.K / g.ksplit, kbeg = kpart * kchunk;
+  const int nk = kchunk / GT_BK;
+  constexpr int NCOLS = BN < 32 ? 32 : BN;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(NCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  // fragment element e of tile (i, j): row m0+wm+16i+gq (+8 for e >= 2), col n0+wn+8j+2tq (+1 for odd e)
-  float* C = g.C + l * g.sC;
-  const float* bias = g.bias ? g.bias + l * g.sBias : nullptr;
-  __nv_bfloat16* H = g.Hout ? g.Hout + l * g.sC : nullptr;
-  const float* Z = g.Zsaved ? g.Zsaved + l * g.sC : nullptr;
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int m = m0 + wm + i * 16 + gq + (e >= 2 ? 8 : 0);
-        const int n = n0 + wn + j * 8 + 2 * tq + (e & 1);
-        const size_t idx = (size_t)m * g.ldc + n;
-        float v = acc[i][j][e];
-        if (EPI == EPI_STORE) {
-          C[idx] = v;
-        } else if (EPI == EPI_BIAS) {
-          C[idx] = v + bias[n];
-        } else if (EPI == EPI_BIAS_SILU) {
-          v += bias[n];
-          C[idx] = v;                                  // pre-activation, kept for the backward pass
-          H[idx] = __float2bfloat16_rn(silu_fast(v));
-        } else if (EPI == EPI_DSILU) {
-          v *= dsilu_fast(Z[idx]);
-          C[idx] = v;                                  // dZ in FP32 (bias gradient)
-          H[idx] = __float2bfloat16_rn(v);             // dZ in BF16 (next products)
-        } else {
-          atomicAdd(C + idx, v);
-        }
+  if (tid < GT_STAGES) mbar_init(smem_u32(bars + tid));
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc_idesc(GT_M, BN) | ((uint32_t)TA << 15) | ((uint32_t)TB << 16);
+  const uint32_t s0 = smem_u32(sm);
+  auto load = [&](int step) {
+    const uint32_t st = s0 + (step % GT_STAGES) * TL::STAGE;
+    const int k0 = kbeg + step * GT_BK;
+    gt_stage<TA, GT_M>(st, A, g.lda, m0, g.M, k0);
+    gt_stage<TB, BN>(st + TL::A_BYTES, B, g.ldb, n0, g.N, k0);
+  };
+  bool ok = true;
+  load(0);
+  cp_commit();
+  for (int ks = 0; ks < nk; ++ks) {
+    if (ks + 1 < nk) {
+      // the next stage's buffer was last read by the MMAs of step ks - 1
+      bool lf = false;
+      if (ks >= 1 && tid == 0)
+        lf = !mbar_wait(smem_u32(bars + (ks - 1) % GT_STAGES), (uint32_t)(((ks - 1) / GT_STAGES) & 1));
+      if (__syncthreads_or(lf)) {
+        ok = false;
+        break;
       }
+      load(ks + 1);
+    }
+    cp_commit();
+    cp_wait1();                                   // this thread's copies of step ks have landed
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      const uint32_t st = s0 + (ks % GT_STAGES) * TL::STAGE;
+#pragma unroll
+      for (int kk = 0; kk < GT_BK / 16; ++kk)
+        tc_mma(tmem, gt_desc<TA, GT_M>(st, kk), gt_desc<TB, BN>(st + TL::A_BYTES, kk), idesc,
+               (ks > 0 || kk > 0) ? 1u : 0u);
+      tc_commit(smem_u32(bars + ks % GT_STAGES));
+    }
+  }
+  if (ok && nk > 0) {
+    bool lf = false;
+    if (tid == 0) lf = !mbar_wait(smem_u32(bars + (nk - 1) % GT_STAGES), (uint32_t)(((nk - 1) / GT_STAGES) & 1));
+    if (__syncthreads_or(lf)) ok = false;
+  }
+  if (ok) {
+    tc_fence_after();
+    asm volatile("cp.async.wait_all;" ::: "memory");   // no copy in flight into the reused stage memory
+    __syncthreads();
+    float* C = g.C + l * g.sC;
+    const float* bias = g.bias ? g.bias + l * g.sBias : nullptr;
+    __nv_bfloat16* H = g.Hout ? g.Hout + l * g.sC : nullptr;
+    const float* Z = g.Zsaved ? g.Zsaved + l * g.sC : nullptr;
+    // each warp's 32 rows x 32 columns pass through shared memory (the
+    // stage buffers, free now) so that every global access below is one
+    // contiguous row segment per warp instruction
+    float* T = reinterpret_cast<float*>(sm) + warp * (32 * 33);
+    const int lane = tid & 31;
+    const int mw = m0 + 32 * warp;
+#pragma unroll 1
+    for (int c = 0; c < BN / 32; ++c) {
+      float v[32];
+      tc_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32 * c, v);   // row mw + lane, all lanes (.sync.aligned)
+#pragma unroll
+      for (int i = 0; i < 32; ++i) T[lane * 33 + i] = v[i];
+      __syncwarp();
+      const int n = n0 + 32 * c + lane;
+      const float b = (EPI == EPI_BIAS || EPI == EPI_BIAS_SILU) ? bias[n] : 0.f;
+      const int rows = nk > 0 ? min(32, g.M - mw) : 0;
+      // the saved pre-activations of the 32 rows, all in flight at once
+      float zv[32];
+      if (EPI == EPI_DSILU) {
+#pragma unroll
+        for (int r = 0; r < 32; ++r) zv[r] = r < rows ? Z[(size_t)(mw + r) * g.ldc + n] : 0.f;
+      }
+#pragma unroll
+      for (int r = 0; r < 32; ++r) {
+        if (r >= rows) break;
+        const size_t idx = (size_t)(mw + r) * g.ldc + n;
+        float q = T[r * 33 + lane];
+        if (EPI == EPI_ATOMIC) {
+          atomicAdd(C + idx, q);
+          continue;
+        }
+        q += b;
+        if (EPI == EPI_DSILU) q *= dsilu_fast(zv[r]);
+        C[idx] = q;                          // pre-activation (SILU) / dZ in FP32 (DSILU)
+        if (EPI == EPI_BIAS_SILU) H[idx] = __float2bfloat16_rn(silu_fast(q));
+        else if (EPI == EPI_DSILU) H[idx] = __float2bfloat16_rn(q);
+      }
+      __syncwarp();
+    }
+  } else if (tid == 0) {
+    atomicExch(g.err, 1);
+    // MMAs possibly in flight finish (bounded) before the tensor memory is released
+    if (nk > 0) mbar_wait(smem_u32(bars + (nk - 1) % GT_STAGES), (uint32_t)(((nk - 1) / GT_STAGES) & 1));
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS) : "memory");
+  }
 }
 
 // ------------------------------------------------------------------ small kernels
@@ -338,17 +421,31 @@ static MlpWork mlp_work(void* ws, int L, int B) {
   return w;
 }
 
-template <int TA, int TB, int EPI>
-static int gemm(const GemmArgs& a, int L, cudaStream_t st) {
-  XT_REQUIRE(a.M % 64 == 0 && a.N % 64 == 0 && a.ksplit >= 1 && a.K % (32 * a.ksplit) == 0,
-             "GEMM shape %d x %d x %d (split %d) not tileable", a.M, a.N, a.K, a.ksplit);
-  dim3 grid(a.M / 64, a.N / 64, L * a.ksplit);
-  k_gemm_bf16<TA, TB, EPI><<<grid, 128, 0, st>>>(a);
-  XT_CHECK_LAUNCH("k_gemm_bf16");
+template <int TA, int TB, int EPI, int BN>
+static int gemm_bn(const GemmArgs& a, int L, cudaStream_t st) {
+  auto kern = k_gemm_tc<TA, TB, EPI, BN>;
+  static bool attr = false;
+  if (!attr) {
+    XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, GtTile<BN>::SMEM));
+    attr = true;
+  }
+  GemmArgs b = a;
+  int rc = tc_error_flag(&b.err);
+  if (rc) return rc;
+  dim3 grid((a.M + GT_M - 1) / GT_M, a.N / BN, L * a.ksplit);
+  kern<<<grid, 128, GtTile<BN>::SMEM, st>>>(b);
+  XT_CHECK_LAUNCH("k_gemm_tc");
   return XT_OK;
 }
 
-// layers 2..4 of the forward pass (H1 computed)
+template <int TA, int TB, int EPI>
+static int gemm(const GemmArgs& a, int L, cudaStream_t st) {
+  XT_REQUIRE(a.M > 0 && a.M % 8 == 0 && (a.N == 64 || a.N == 128) && a.ksplit >= 1 && a.K % (GT_BK * a.ksplit) == 0,
+             "GEMM shape %d x %d x %d (split %d) not tileable", a.M, a.N, a.K, a.ksplit);
+  XT_REQUIRE((a.lda % 8) == 0 && (a.ldb % 8) == 0 && (a.ldc % 4) == 0, "GEMM leading dimensions must allow 16-byte rows");
+  return a.N == 64 ? gemm_bn<TA, TB, EPI, 64>(a, L, st) : gemm_bn<TA, TB, EPI, 128>(a, L, st);
+}
+
 static int mlp_forward_gemms(MlpHandle* h, const MlpWork& w, int B, cudaStream_t st) {
   const int L = h->L, ps = h->psize;
   int rc;

@@ -576,7 +576,7 @@ int xt_learned_status(void) {
   if (v) {
     const int zero = 0;
     XT_CUDA(cudaMemcpy(d, &zero, sizeof(int), cudaMemcpyHostToDevice));
-    set_error("tensor-memory network pass: an MMA completion wait timed out");
+    set_error("learned basis on the tensor cores (network pass or training GEMM): an MMA completion wait timed out");
     return XT_ERR_DEVICE;
   }
   return XT_OK;

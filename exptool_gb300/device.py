@@ -233,7 +233,7 @@ class SphTable:
         return out
 
     def accumulate_batched_tc(self, xyzm, offsets, no_odd=False, chunk=16384, stages=2, ctas_per_sm=0,
-                              workspace=None):
+                              threads_per_particle=1, workspace=None):
         """Coefficients of many snapshots on the tensor cores: particles
         counting-sorted by (snapshot, radial window), then per window a BF16
         tcgen05 product of the interpolation weights and the angular basis
@@ -241,8 +241,9 @@ class SphTable:
         FP64 contraction.  Arguments as for accumulate_batched; ``chunk`` is
         the most particles of one work item, ``stages`` the operand buffers per
         CTA (1 to 3), ``ctas_per_sm`` the CTAs of the persistent launch per SM
-        (0: as many as are resident).  Returns a (nsnap, (lmax+1)^2, nmax)
-        float64 tensor."""
+        (0: as many as are resident), ``threads_per_particle`` 1 or 2 (the
+        angular rows split by the parity of m).  Returns a (nsnap,
+        (lmax+1)^2, nmax) float64 tensor."""
         offs = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
         nsnap = offs.size - 1
         if xyzm.dtype != torch.float32 or xyzm.dim() != 2 or xyzm.shape[1] != 4 or not xyzm.is_contiguous():
@@ -255,16 +256,17 @@ class SphTable:
             torch.empty(need, dtype=torch.uint8, device=xyzm.device)
         _lib.check(self._lib.xt_sph_accumulate_batched_tc(self.handle, dptr(xyzm), offs.ctypes.data, nsnap,
                                                           int(bool(no_odd)), int(chunk), int(stages),
-                                                          int(ctas_per_sm), dptr(out), dptr(ws), ws.numel(),
-                                                          stream_ptr()),
+                                                          int(ctas_per_sm), int(threads_per_particle), dptr(out),
+                                                          dptr(ws), ws.numel(), stream_ptr()),
                    "xt_sph_accumulate_batched_tc")
         return out
 
-    def batched_tc_residency(self, stages):
+    def batched_tc_residency(self, stages, threads_per_particle=1):
         """CTAs of the tensor-core accumulation resident per SM at this
-        pipeline depth (the largest useful ``ctas_per_sm``)."""
+        pipeline depth and split (the largest useful ``ctas_per_sm``)."""
         v = ctypes.c_int(0)
-        _lib.check(self._lib.xt_sph_batched_tc_residency(self.handle, int(stages), ctypes.byref(v)),
+        _lib.check(self._lib.xt_sph_batched_tc_residency(self.handle, int(stages), int(threads_per_particle),
+                                                         ctypes.byref(v)),
                    "xt_sph_batched_tc_residency")
         return int(v.value)
 

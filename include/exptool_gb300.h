@@ -149,16 +149,18 @@ int xt_sph_accumulate_batched(void *handle, const float *xyzm, const long long *
  * chunk = the most particles of one work item (>= 128), stages = operand
  * buffers per CTA (1 to 3; fewer buffers let more CTAs share an SM) and
  * ctas_per_sm = CTAs of the persistent launch per SM (0: as many as are
- * resident; xt_sph_batched_tc_residency gives that number for a depth).
+ * resident; xt_sph_batched_tc_residency gives that number for a depth) and
+ * threads_per_particle = 1 or 2 (2: the angular rows of a particle are split
+ * by the parity of m between two threads, twice the threads per CTA).
  * numr <= 8129, lmax <= 8, at most 2^31 - 1 particles.  The workspace size
  * depends on the snapshot sizes.
  * xt_sph_batched_tc_status synchronises the device and reports (and clears)
  * an error flag a launch set: XT_ERR_DEVICE, else XT_OK. */
 size_t xt_sph_batched_tc_workspace(void *handle, int nsnap, const long long *offsets_host, int chunk);
 int xt_sph_accumulate_batched_tc(void *handle, const float *xyzm, const long long *offsets_host, int nsnap,
-                                 int no_odd, int chunk, int stages, int ctas_per_sm, double *expcoef_out,
-                                 void *workspace, size_t workspace_bytes, void *stream);
-int xt_sph_batched_tc_residency(void *handle, int stages, int *ctas_per_sm);
+                                 int no_odd, int chunk, int stages, int ctas_per_sm, int threads_per_particle,
+                                 double *expcoef_out, void *workspace, size_t workspace_bytes, void *stream);
+int xt_sph_batched_tc_residency(void *handle, int stages, int threads_per_particle, int *ctas_per_sm);
 int xt_sph_batched_tc_status(void);
 
 /* --------------------------------------------------------------- cylindrical (EOF) */

@@ -105,11 +105,14 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
         blk = xd[int(offs[i]):int(offs[i + 1])].double()
         refs.append(dev.to_host(table.accumulate(*(blk[:, k].contiguous() for k in range(4)))) if sizes[i] else None)
     # residency: fewer operand stages never fit fewer CTAs on an SM
-    res = [table.batched_tc_residency(st) for st in (1, 2, 3)]
-    assert res[0] >= res[1] >= res[2] >= 1, res
+    for sp in (1, 2):
+        res = [table.batched_tc_residency(st, sp) for st in (1, 2, 3)]
+        assert res[0] >= res[1] >= res[2] >= 1, (sp, res)
     results = []
-    for chunk, stages, ctas in ((16384, 2, 0), (512, 3, 0), (128, 2, 1), (4096, 1, 0), (4096, 1, 2)):
-        got = dev.to_host(table.accumulate_batched_tc(xd, offs, chunk=chunk, stages=stages, ctas_per_sm=ctas))
+    for chunk, stages, ctas, sp in ((16384, 2, 0, 1), (512, 3, 0, 1), (128, 2, 1, 1), (4096, 1, 0, 1), (4096, 1, 2, 1),
+                                    (4096, 1, 0, 2), (512, 2, 1, 2)):
+        got = dev.to_host(table.accumulate_batched_tc(xd, offs, chunk=chunk, stages=stages, ctas_per_sm=ctas,
+                                                      threads_per_particle=sp))
         dev.batched_tc_status()
         results.append(got)
         for i, n in enumerate(sizes):
@@ -117,9 +120,9 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
                 assert not np.any(got[i]), (chunk, i)
                 continue
             e = norm_err(got[i], refs[i])
-            assert e <= 5e-3, (chunk, stages, ctas, i, e)
+            assert e <= 5e-3, (chunk, stages, ctas, sp, i, e)
             if n >= 10000:
-                assert e <= 5e-4, (chunk, stages, ctas, i, e)
+                assert e <= 5e-4, (chunk, stages, ctas, sp, i, e)
     # the same sums whatever the work-item size or launch width, to FP32 summation
     # order (slots inside a bucket come from shared-memory atomics, so the order of
     # the particles within a work item may differ between calls)
@@ -127,6 +130,8 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
         if n >= 10000:
             assert norm_err(results[1][i], results[0][i]) <= 1e-5
             assert norm_err(results[4][i], results[3][i]) <= 1e-5
+            assert norm_err(results[5][i], results[3][i]) <= 1e-5      # two threads per particle
+            assert norm_err(results[6][i], results[3][i]) <= 1e-5
     # against the oracle on a small snapshot (FP32-rounded inputs)
     t = osl.load_table(cache, model)
     x, y, z, m = (xyzm[offs[1]:offs[2], k].astype(np.float64) for k in range(4))
