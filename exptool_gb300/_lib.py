@@ -85,6 +85,9 @@ _SIGS = {
     "xt_timing_read": (c_int, [c_dp, c_int]),
     "xt_fields_forces": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp,
                                  c_dbl, c_ll, c_dpp, c_vp]),
+    "xt_orbit_sort_workspace": (c_sz, [c_vp, c_ll]),
+    "xt_orbit_sort": (c_int, [c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "xt_orbit_unsort": (c_int, [c_vp, c_vp, c_ll, c_vp, c_vp]),
     "xt_leapfrog": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_dpp, c_ll, c_int, c_int,
                             c_int, c_dbl, c_dbl, c_int, c_int, c_vp, c_vp, c_vp]),
     "xt_mlp_param_size": (c_int, []),

@@ -14,6 +14,79 @@
 
 namespace xt {
 
+// ---------------------------------------------------------------- orbit reordering
+// Ensembles of orbits at unrelated positions make every warp gather its
+// field values from unrelated table cells.  Between chunks of steps the
+// orbits are counting-sorted by the disc table cell of their position
+// (eof.return_bins's cell, eof.py:354-427, from FP32 coordinates), so that the
+// threads of a warp share cells and their gathers hit L1.  The state moves
+// with its orbit (16 rows of n doubles) together with the orbit's original
+// index; each orbit's arithmetic is unchanged, so results are bit-identical
+// to the unsorted run once xt_orbit_unsort restores the order.
+__global__ void __launch_bounds__(256) k_orbit_key(CylTab<float> T, const double* __restrict__ s, long long n,
+                                                   int* __restrict__ hist, int* __restrict__ key,
+                                                   int* __restrict__ slot) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float x = (float)s[S_X * n + q], y = (float)s[S_Y * n + q], z = (float)s[S_Z * n + q];
+    const CylBins<float> B = cyl_bins(T, sqrtf(x * x + y * y), z);
+    const int ix = B.node / (T.numy + 1), iy = B.node - ix * (T.numy + 1);
+    const int cell = ix * T.numy + iy;
+    key[q] = cell;
+    slot[q] = atomicAdd(hist + cell, 1);
+  }
+}
+
+// Exclusive scan of ncell counts in one block of 1024 threads: each thread
+// sums a contiguous run of cells, the runs' totals are scanned across the
+// block, then each thread writes its cells' offsets.
+__global__ void __launch_bounds__(1024) k_orbit_scan(int* __restrict__ hist, int ncell) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x;
+  const int per = (ncell + 1023) / 1024;
+  const int c0 = t * per, c1 = min(c0 + per, ncell);
+  int sum = 0;
+  for (int c = c0; c < c1; ++c) sum += hist[c];
+  part[t] = sum;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {
+    const int v = t >= d ? part[t - d] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = part[t] - sum;                      // exclusive prefix of this thread's run
+  for (int c = c0; c < c1; ++c) {
+    const int h = hist[c];
+    hist[c] = run;
+    run += h;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_orbit_gather(const double* __restrict__ in, double* __restrict__ out,
+                                                      long long n, const int* __restrict__ off,
+                                                      const int* __restrict__ key, const int* __restrict__ slot,
+                                                      const long long* __restrict__ order_in,
+                                                      long long* __restrict__ order_out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long d = (long long)off[key[q]] + slot[q];
+#pragma unroll
+    for (int k = 0; k < S_COUNT; ++k) out[k * n + d] = in[k * n + q];
+    order_out[d] = order_in[q];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_orbit_unsort(const double* __restrict__ in, double* __restrict__ out,
+                                                      long long n, const long long* __restrict__ order) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long d = order[q];
+#pragma unroll
+    for (int k = 0; k < S_COUNT; ++k) out[k * n + d] = in[k * n + q];
+  }
+}
+
 }  // namespace xt
 
 using namespace xt;
@@ -48,6 +121,53 @@ int xt_fields_forces(void* sph, const void* sph_field, void* cyl, const void* cy
   });
   if (rc) return rc;
   XT_CHECK_LAUNCH("k_fields_forces");
+  return XT_OK;
+}
+
+size_t xt_orbit_sort_workspace(void* cyl, long long n) {
+  CylTab<double> cd;
+  CylTab<float> cf;
+  if (!cyl_tabs(cyl, &cd, &cf) || n < 0) return 0;
+  return ((size_t)cf.numx * cf.numy + 2 * (size_t)n) * sizeof(int) + 256;
+}
+
+int xt_orbit_sort(void* cyl, const double* state_in, double* state_out, long long n, const long long* order_in,
+                  long long* order_out, void* workspace, size_t workspace_bytes, void* stream) {
+  CylTab<double> cd;
+  CylTab<float> cf;
+  XT_REQUIRE(cyl_tabs(cyl, &cd, &cf), "NULL table handle");
+  XT_REQUIRE(n >= 0 && n < (1LL << 31), "orbit count must be in [0, 2^31)");
+  if (n == 0) return XT_OK;
+  XT_REQUIRE(state_in && state_out && order_in && order_out && state_in != state_out && order_in != order_out,
+             "need distinct input and output states and orders");
+  const size_t need = xt_orbit_sort_workspace(cyl, n);
+  if (!workspace || workspace_bytes < need) {
+    set_error("workspace of %zu bytes needed, %zu given", need, workspace_bytes);
+    return XT_ERR_WORKSPACE;
+  }
+  const int ncell = cf.numx * cf.numy;
+  XT_REQUIRE(ncell >= 1 && ncell <= (1 << 22), "table of %d cells", ncell);
+  int* hist = static_cast<int*>(workspace);
+  int* key = hist + ncell;
+  int* slot = key + n;
+  cudaStream_t st = as_stream(stream);
+  XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
+  const int grid = grid_for(n, 256, 8);
+  k_orbit_key<<<grid, 256, 0, st>>>(cf, state_in, n, hist, key, slot);
+  XT_CHECK_LAUNCH("k_orbit_key");
+  k_orbit_scan<<<1, 1024, 0, st>>>(hist, ncell);
+  XT_CHECK_LAUNCH("k_orbit_scan");
+  k_orbit_gather<<<grid, 256, 0, st>>>(state_in, state_out, n, hist, key, slot, order_in, order_out);
+  XT_CHECK_LAUNCH("k_orbit_gather");
+  return XT_OK;
+}
+
+int xt_orbit_unsort(const double* state_in, double* state_out, long long n, const long long* order, void* stream) {
+  XT_REQUIRE(n >= 0 && n < (1LL << 31), "orbit count must be in [0, 2^31)");
+  if (n == 0) return XT_OK;
+  XT_REQUIRE(state_in && state_out && order && state_in != state_out, "need distinct states and an order");
+  k_orbit_unsort<<<grid_for(n, 256, 8), 256, 0, as_stream(stream)>>>(state_in, state_out, n, order);
+  XT_CHECK_LAUNCH("k_orbit_unsort");
   return XT_OK;
 }
 

@@ -77,7 +77,7 @@ __device__ __forceinline__ void traj_row(double* traj, long long p, int nint, in
 }
 
 template <typename R, int LCAP>
-__global__ void __launch_bounds__(128) k_leapfrog(SphTab<R> ST, const R* __restrict__ GH, CylTab<R> CT,
+__global__ void __launch_bounds__(128, 4) k_leapfrog(SphTab<R> ST, const R* __restrict__ GH, CylTab<R> CT,
                                                   const R* __restrict__ F, FieldOpts fo, OrbitArgs A) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < A.n;
        p += (long long)gridDim.x * blockDim.x) {

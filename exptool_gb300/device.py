@@ -530,6 +530,26 @@ STATE_SLOTS = ("x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz", "pot", "r2m1",
                "edev")
 
 
+def orbit_sort_workspace(cyl_field, n):
+    return int(_lib.load().xt_orbit_sort_workspace(cyl_field.table.handle, int(n)))
+
+
+def orbit_sort(cyl_field, state_in, state_out, order_in, order_out, workspace):
+    """Counting sort of the orbits of ``state_in`` (16 x n float64) by disc
+    table cell into ``state_out``, carrying the original indices
+    (xt_orbit_sort)."""
+    n = int(state_in.shape[1])
+    _lib.check(_lib.load().xt_orbit_sort(cyl_field.table.handle, dptr(state_in), dptr(state_out), n, dptr(order_in),
+                                         dptr(order_out), dptr(workspace), workspace.numel(), stream_ptr()),
+               "xt_orbit_sort")
+
+
+def orbit_unsort(state_in, state_out, order):
+    """Orbit q of ``state_in`` to column order[q] of ``state_out``."""
+    _lib.check(_lib.load().xt_orbit_unsort(dptr(state_in), dptr(state_out), int(state_in.shape[1]), dptr(order),
+                                           stream_ptr()), "xt_orbit_unsort")
+
+
 def leapfrog(sph_field, cyl_field, state, step0, nsteps, nint, dt, rotc=0.0, apse=False, ap_max=1000, traj=None,
              halo_l=-1, disk_m=-1, no_odd=False, trig_l=True, dts=None):
     """Advance orbit ensemble ``state`` (16 x n float64 tensor) in place;

@@ -103,11 +103,14 @@ class Ensemble:
     State lives on the device as a (16, n) float64 tensor (see
     ``device.STATE_SLOTS``).  ``run`` advances all orbits through steps
     [0, nint) in launches of ``chunk`` steps; with ``graph=True`` the launch
-    sequence is captured once as a CUDA graph and replayed.
+    sequence is captured once as a CUDA graph and replayed.  With ``sort``
+    (default) the orbits are reordered by disc table cell before every chunk,
+    so that neighbouring threads gather from the same cells (xt_orbit_sort),
+    and put back in their order at the end: the same results bit for bit.
     """
 
     def __init__(self, FieldInstance, initpos, initvel, nint, dt, rotfreq=0.0, precision=None, chunk=50,
-                 apse=False, ap_max=1000):
+                 apse=False, ap_max=1000, sort=True):
         self.F = FieldInstance
         self.precision = FieldInstance.precision if precision is None else precision
         self.sf, self.cf = FieldInstance.device_fields(self.precision)
@@ -117,16 +120,35 @@ class Ensemble:
         self.chunk = max(1, int(chunk))
         self.apse, self.ap_max = apse, ap_max
         self.graph = None
+        self.sort = bool(sort)
+        if self.sort:
+            n = int(self.state.shape[1])
+            self._buf = [torch.empty_like(self.state), torch.empty_like(self.state)]
+            self._ord = [torch.empty(n, dtype=torch.int64, device=self.state.device) for _ in range(2)]
+            self._iota = torch.arange(n, dtype=torch.int64, device=self.state.device)
+            self._ws = torch.empty(max(1, dev.orbit_sort_workspace(self.cf, n)), dtype=torch.uint8,
+                                   device=self.state.device)
 
     def _launch_all(self):
         F = self.F
+        cur = self.state
+        if self.sort:
+            k = 0
+            self._buf[0].copy_(self.state)
+            self._ord[0].copy_(self._iota)
         step = 0
         while step < self.nint:
             n = self.chunk if step > 0 else min(self.chunk, self.nint)
-            dev.leapfrog(self.sf, self.cf, self.state, step, n, self.nint, self.dt, rotc=self.rotc, apse=self.apse,
+            if self.sort:
+                dev.orbit_sort(self.cf, self._buf[k], self._buf[1 - k], self._ord[k], self._ord[1 - k], self._ws)
+                k = 1 - k
+                cur = self._buf[k]
+            dev.leapfrog(self.sf, self.cf, cur, step, n, self.nint, self.dt, rotc=self.rotc, apse=self.apse,
                          ap_max=self.ap_max, halo_l=F._halo_l(), disk_m=F._disk_m(), no_odd=F.no_odd,
                          trig_l=not F.halo_correct_m)
             step += n
+        if self.sort:
+            dev.orbit_unsort(cur, self.state, self._ord[k])
 
     def launches_per_run(self):
         return (self.nint + self.chunk - 1) // self.chunk
@@ -162,10 +184,10 @@ class Ensemble:
 
 
 def leapfrog_ensemble(FieldInstance, nint, dt, initpos, initvel, rotfreq=0.0, precision=None, chunk=50, graph=True,
-                      apse=False, ap_max=1000):
+                      apse=False, ap_max=1000, sort=True):
     """Integrate an ensemble of orbits; returns the final state as a dict of
     NumPy arrays (x y z vx vy vz fx fy fz pot ... nstep e0 edev)."""
-    ens = Ensemble(FieldInstance, initpos, initvel, nint, dt, rotfreq, precision, chunk, apse, ap_max)
+    ens = Ensemble(FieldInstance, initpos, initvel, nint, dt, rotfreq, precision, chunk, apse, ap_max, sort)
     st = ens.run(graph=graph).cpu().numpy()
     return {k: st[i] for i, k in enumerate(dev.STATE_SLOTS)}
 

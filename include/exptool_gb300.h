@@ -269,6 +269,20 @@ int xt_leapfrog(void *sph, const void *sph_field, void *cyl, const void *cyl_fie
                 int step0, int nsteps, int nint, double dt, double rotc, int apse, int ap_max, double *traj,
                 const double *dt_per_orbit, void *stream);
 
+/* Reordering of an orbit ensemble between chunks of xt_leapfrog steps (no
+ * reference counterpart; the reference integrates one orbit at a time): the
+ * orbits of state_in (16 x n float64, row k = state array k, contiguous) are
+ * counting-sorted by the disc table cell of their position (the cell of
+ * eof.return_bins, eof.py:354-427) into state_out, so that the threads of a
+ * warp gather from the same table cells; order_out[q] = order_in of the orbit
+ * placed at q.  xt_orbit_unsort writes state_in's orbit q to column order[q]
+ * of state_out.  Each orbit's arithmetic is independent of its position, so a
+ * sorted run unsorted at the end equals the unsorted run bit for bit. */
+size_t xt_orbit_sort_workspace(void *cyl, long long n);
+int xt_orbit_sort(void *cyl, const double *state_in, double *state_out, long long n, const long long *order_in,
+                  long long *order_out, void *workspace, size_t workspace_bytes, void *stream);
+int xt_orbit_unsort(const double *state_in, double *state_out, long long n, const long long *order, void *stream);
+
 /* ------------------------------------------------------------------ learned radial basis
  * No counterpart in the reference: a surrogate for the SL radial tables of
  * spheresl (get_halo_dens_pot_force, spheresl.py:106-160).  One network per

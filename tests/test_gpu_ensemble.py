@@ -115,3 +115,37 @@ def test_fp32_force_within_bound_of_fp64():
     d64 = s64["edev"] / np.abs(s64["e0"])
     d32 = s32["edev"] / np.abs(s32["e0"])
     assert np.max(np.abs(d32 - d64)) <= 1e-5, np.max(np.abs(d32 - d64))
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_cell_sorted_ensemble_is_bit_identical(precision):
+    """Orbits reordered by disc table cell before every chunk (the default,
+    xt_orbit_sort) end in the same states, bit for bit, as the unsorted
+    ensemble, with and without graph replay; one reordering step is a
+    permutation other than the identity that moves whole state columns, and
+    xt_orbit_unsort inverts it."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.utils import integrate
+    F, _ = make_fields()
+    pos, vel = _random_orbits(5000, 7)
+    plain = integrate.Ensemble(F, pos, vel, 150, 0.01, rotfreq=0.05, precision=precision, chunk=40, sort=False)
+    a = plain.run(graph=False).clone()
+    ens = integrate.Ensemble(F, pos, vel, 150, 0.01, rotfreq=0.05, precision=precision, chunk=40, sort=True)
+    b = ens.run(graph=False).clone()
+    c = ens.run(graph=True).clone()
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    assert torch.equal(a, c)
+    # one reordering step on its own
+    n = ens.state.shape[1]
+    out = torch.empty_like(ens.state)
+    order = torch.empty(n, dtype=torch.int64, device="cuda")
+    dev.orbit_sort(ens.cf, ens.state, out, ens._iota, order, ens._ws)
+    back = torch.empty_like(ens.state)
+    dev.orbit_unsort(out, back, order)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.sort(order).values, ens._iota)
+    assert not torch.equal(order, ens._iota)
+    assert torch.equal(back, ens.state)
+    assert torch.equal(out, ens.state[:, order])
