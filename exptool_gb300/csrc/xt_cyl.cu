@@ -1099,6 +1099,19 @@ bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f) {
   return true;
 }
 
+// Exclusive scan of ncell (<= 1024^2) counts into off (may equal hist), with
+// a scratch of 1024 ints: per-tile scans, then the tiles' prefix (also used by
+// the orbit reordering).
+int launch_cell_scan(const int* hist, int* off, int* tile_sum, int ncell, cudaStream_t st) {
+  XT_REQUIRE(ncell >= 1 && ncell <= kScanTile * kScanTile, "scan of %d cells", ncell);
+  const int ntile = (ncell + kScanTile - 1) / kScanTile;
+  k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tile_sum, ncell);
+  XT_CHECK_LAUNCH("k_scan_tiles");
+  k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tile_sum, ncell, ntile);
+  XT_CHECK_LAUNCH("k_scan_add");
+  return XT_OK;
+}
+
 }  // namespace xt
 
 using namespace xt;

@@ -14,6 +14,8 @@ bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f);
 // from the split table efp_df (xt_batch.cu)
 int launch_sph_contract_batched(const float2* efp_df, const double* G, int nsnap, int lmax, int nmax, int numr,
                                 double* out, cudaStream_t st);
+// exclusive scan of ncell <= 2^20 counts (xt_cyl.cu); tile_sum: 1024 ints
+int launch_cell_scan(const int* hist, int* off, int* tile_sum, int ncell, cudaStream_t st);
 int launch_sph_contract_batched(const float2* efp_df, const float2* G, int nsnap, int lmax, int nmax, int numr,
                                 double* out, cudaStream_t st);
 }  // namespace xt

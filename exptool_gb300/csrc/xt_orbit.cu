@@ -37,32 +37,6 @@ __global__ void __launch_bounds__(256) k_orbit_key(CylTab<float> T, const double
   }
 }
 
-// Exclusive scan of ncell counts in one block of 1024 threads: each thread
-// sums a contiguous run of cells, the runs' totals are scanned across the
-// block, then each thread writes its cells' offsets.
-__global__ void __launch_bounds__(1024) k_orbit_scan(int* __restrict__ hist, int ncell) {
-  __shared__ int part[1024];
-  const int t = threadIdx.x;
-  const int per = (ncell + 1023) / 1024;
-  const int c0 = t * per, c1 = min(c0 + per, ncell);
-  int sum = 0;
-  for (int c = c0; c < c1; ++c) sum += hist[c];
-  part[t] = sum;
-  __syncthreads();
-  for (int d = 1; d < 1024; d <<= 1) {
-    const int v = t >= d ? part[t - d] : 0;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  int run = part[t] - sum;                      // exclusive prefix of this thread's run
-  for (int c = c0; c < c1; ++c) {
-    const int h = hist[c];
-    hist[c] = run;
-    run += h;
-  }
-}
-
 __global__ void __launch_bounds__(256) k_orbit_gather(const double* __restrict__ in, double* __restrict__ out,
                                                       long long n, const int* __restrict__ off,
                                                       const int* __restrict__ key, const int* __restrict__ slot,
@@ -128,7 +102,7 @@ size_t xt_orbit_sort_workspace(void* cyl, long long n) {
   CylTab<double> cd;
   CylTab<float> cf;
   if (!cyl_tabs(cyl, &cd, &cf) || n < 0) return 0;
-  return ((size_t)cf.numx * cf.numy + 2 * (size_t)n) * sizeof(int) + 256;
+  return (2 * (size_t)cf.numx * cf.numy + 2 * (size_t)n + 1024) * sizeof(int) + 256;
 }
 
 int xt_orbit_sort(void* cyl, const double* state_in, double* state_out, long long n, const long long* order_in,
@@ -146,18 +120,20 @@ int xt_orbit_sort(void* cyl, const double* state_in, double* state_out, long lon
     return XT_ERR_WORKSPACE;
   }
   const int ncell = cf.numx * cf.numy;
-  XT_REQUIRE(ncell >= 1 && ncell <= (1 << 22), "table of %d cells", ncell);
+  XT_REQUIRE(ncell >= 1 && ncell <= (1 << 20), "table of %d cells", ncell);
   int* hist = static_cast<int*>(workspace);
-  int* key = hist + ncell;
+  int* off = hist + ncell;
+  int* tsum = off + ncell;
+  int* key = tsum + 1024;
   int* slot = key + n;
   cudaStream_t st = as_stream(stream);
   XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
   const int grid = grid_for(n, 256, 8);
   k_orbit_key<<<grid, 256, 0, st>>>(cf, state_in, n, hist, key, slot);
   XT_CHECK_LAUNCH("k_orbit_key");
-  k_orbit_scan<<<1, 1024, 0, st>>>(hist, ncell);
-  XT_CHECK_LAUNCH("k_orbit_scan");
-  k_orbit_gather<<<grid, 256, 0, st>>>(state_in, state_out, n, hist, key, slot, order_in, order_out);
+  int rc = launch_cell_scan(hist, off, tsum, ncell, st);
+  if (rc) return rc;
+  k_orbit_gather<<<grid, 256, 0, st>>>(state_in, state_out, n, off, key, slot, order_in, order_out);
   XT_CHECK_LAUNCH("k_orbit_gather");
   return XT_OK;
 }

@@ -2,9 +2,16 @@
 // per precision in xt_orbit_k64.cu / xt_orbit_k32.cu.
 #pragma once
 
+#include "xt_df.cuh"
 #include "xt_launch.cuh"
 
 namespace xt {
+
+// Exact widening of a force component to FP64: for FP32 forces by integer
+// operations (the same double as the conversion instruction, without the
+// FP64 pipe, which the FP64 kick/drift of the orbit step keeps busy).
+__device__ __forceinline__ double wide(float v) { return f2d_int(v); }
+__device__ __forceinline__ double wide(double v) { return v; }
 
 // One point of Fields.return_forces_cart: out = fxd fxh fyd fyh fzd fzh diskp halop.
 // (cr, sr) = cos/sin of the rotation angle added to phi.
@@ -89,10 +96,10 @@ __global__ void __launch_bounds__(128, 4) k_leapfrog(SphTab<R> ST, const R* __re
     if (A.step0 == 0) {
       // integrate.py:116-122: forces at the initial position, rotation 0
       fields_point<R, LCAP>(ST, GH, CT, F, fo, (R)x, (R)y, (R)z, R(1), R(0), v);
-      fx = (double)v[0] + (double)v[1];
-      fy = (double)v[2] + (double)v[3];
-      fz = (double)v[4] + (double)v[5];
-      pot = (double)v[6] + (double)v[7];
+      fx = wide(v[0]) + wide(v[1]);
+      fy = wide(v[2]) + wide(v[3]);
+      fz = wide(v[4]) + wide(v[5]);
+      pot = wide(v[6]) + wide(v[7]);
       r2m1 = x * x + y * y;
       r2m2 = 0.0;
       aps = 0.0;
@@ -123,10 +130,10 @@ __global__ void __launch_bounds__(128, 4) k_leapfrog(SphTab<R> ST, const R* __re
       double srd = 0.0, crd = 1.0;
       if (A.rotc != 0.0) sincos(A.rotc * ((double)k * dt), &srd, &crd);
       fields_point<R, LCAP>(ST, GH, CT, F, fo, (R)x, (R)y, (R)z, (R)crd, (R)srd, v);
-      const double nfx = (double)v[0] + (double)v[1];
-      const double nfy = (double)v[2] + (double)v[3];
-      const double nfz = (double)v[4] + (double)v[5];
-      pot = (double)v[6] + (double)v[7];
+      const double nfx = wide(v[0]) + wide(v[1]);
+      const double nfy = wide(v[2]) + wide(v[3]);
+      const double nfz = wide(v[4]) + wide(v[5]);
+      pot = wide(v[6]) + wide(v[7]);
       vx = vx + (0.5 * (fx + nfx) * dt);
       vy = vy + (0.5 * (fy + nfy) * dt);
       vz = vz + (0.5 * (fz + nfz) * dt);
