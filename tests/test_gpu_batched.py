@@ -145,3 +145,44 @@ def test_batched_tensor_core_vs_fp64_and_oracle(l6_table, tmp_path, monkeypatch)
     for l in (1, 3, 5):
         assert not np.any(odd[:, l * l:(l + 1) * (l + 1)])
     assert norm_err(odd[2][0:1], refs[2][0:1]) <= 5e-4
+
+
+@pytest.mark.parametrize("lmax,nmax,cmap", [(4, 10, 1), (8, 12, 2)])
+def test_batched_tensor_core_other_tables(tmp_path_factory, lmax, nmax, cmap):
+    """The tensor-core engine on the other instantiations of its tile (lmax 4:
+    N = 32; lmax 8: N = 96) and on the rational radial map (cmap 1), with one
+    and two threads per particle and one or two stages, against the FP64
+    single-snapshot path on the same FP32-rounded particles (the BF16 bounds of
+    the lmax 6 test).  Two threads per particle order the rows by the parity
+    of m; the rows come back to their places through the permutation table."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import spheresl
+    from exptool_gb300.tables.samplers import hernquist_sample
+    from exptool_gb300.tables.sl_solver import make_hernquist_sl
+    d = str(tmp_path_factory.mktemp(f"sl{lmax}c{cmap}"))
+    cache, model = make_hernquist_sl(d, lmax=lmax, nmax=nmax, numr=1200, rmin=1e-3, rmax=100.0, cmap=cmap,
+                                     tag=f"l{lmax}c{cmap}")
+    sizes = [30000, 700, 52000]
+    snaps = [hernquist_sample(n, 900 + i) for i, n in enumerate(sizes)]
+    xyzm = np.concatenate([np.stack(s, axis=1) for s in snaps], axis=0).astype(np.float32)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    table = spheresl.table_from_files(cache, model)
+    xd = torch.from_numpy(xyzm).cuda().contiguous()
+    refs = []
+    for i in range(len(sizes)):
+        blk = xd[int(offs[i]):int(offs[i + 1])].double()
+        refs.append(dev.to_host(table.accumulate(*(blk[:, k].contiguous() for k in range(4)))))
+    got = {}
+    for sp in (1, 2):
+        for stages in (1, 2):
+            out = dev.to_host(table.accumulate_batched_tc(xd, offs, chunk=8192, stages=stages,
+                                                          threads_per_particle=sp))
+            dev.batched_tc_status()
+            got[sp, stages] = out
+            for i, n in enumerate(sizes):
+                e = norm_err(out[i], refs[i])
+                assert e <= (5e-4 if n >= 10000 else 5e-3), (lmax, cmap, sp, stages, i, e)
+    for i, n in enumerate(sizes):
+        if n >= 10000:
+            assert norm_err(got[2, 1][i], got[1, 1][i]) <= 1e-5, (lmax, i)
