@@ -20,6 +20,7 @@
 
 #include "xt_df.cuh"
 #include "xt_internal.cuh"
+#include "xt_tc.cuh"
 
 namespace xt {
 
@@ -33,9 +34,10 @@ struct FusedGraph {
     const void* ws;
     const double *cos_out, *sin_out;
     double* outs[5];
+    int field_engine;
     bool same(const Key& o) const {
       if (n != o.n || precision != o.precision || m1 != o.m1 || m2 != o.m2 || nan_to_origin != o.nan_to_origin ||
-          ws != o.ws || cos_out != o.cos_out || sin_out != o.sin_out)
+          ws != o.ws || cos_out != o.cos_out || sin_out != o.sin_out || field_engine != o.field_engine)
         return false;
       for (int i = 0; i < 5; ++i)
         if (outs[i] != o.outs[i]) return false;
@@ -556,8 +558,18 @@ __device__ __forceinline__ int block_exclusive_scan_1024(int v, int* warp_tot, i
   return x - v + warp_tot[wid];
 }
 
+// Node blocks of the tiled tables whose field the evaluation reads: those
+// holding a corner node of a cell with particles (cell = ix * numy + iy,
+// corners (ix + {0,1}) * (numy + 1) + iy + {0,1}).  The deposit grid is zero
+// outside them, so the contraction may skip the others as well.
+struct ActiveBlocks {
+  int* flag = nullptr;    // [nblk], cleared before the scan; nullptr: not wanted
+  int* list = nullptr;    // [1 + nblk]: count, then the marked blocks in increasing order
+  int numy = 0, nblk = 0;
+};
+
 __global__ void __launch_bounds__(kScanTile) k_scan_tiles(const int* __restrict__ hist, int* __restrict__ off,
-                                                          int* __restrict__ tile_sum, int ncell) {
+                                                          int* __restrict__ tile_sum, int ncell, ActiveBlocks ab) {
   __shared__ int wt[33];
   const int i = blockIdx.x * kScanTile + threadIdx.x;
   const int v = i < ncell ? hist[i] : 0;
@@ -565,12 +577,21 @@ __global__ void __launch_bounds__(kScanTile) k_scan_tiles(const int* __restrict_
   const int ex = block_exclusive_scan_1024(v, wt, total);
   if (i < ncell) off[i] = ex;
   if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+  if (ab.flag && v > 0) {
+    const int ix = i / ab.numy, iy = i - ix * ab.numy;
+    const int n00 = ix * (ab.numy + 1) + iy, n10 = n00 + ab.numy + 1;
+    ab.flag[n00 / kTileNodes] = 1;   // same-value stores: their order does not matter
+    ab.flag[(n00 + 1) / kTileNodes] = 1;
+    ab.flag[n10 / kTileNodes] = 1;
+    ab.flag[(n10 + 1) / kTileNodes] = 1;
+  }
 }
 
 // Adds the exclusive prefix of the tile totals (scanned by every block from
-// the tile_sum array; ntile <= 1024) to each cell offset.
+// the tile_sum array; ntile <= 1024) to each cell offset.  With ab.list, block
+// 0 also lists the flagged node blocks in increasing order.
 __global__ void __launch_bounds__(kScanTile) k_scan_add(int* __restrict__ off, const int* __restrict__ tile_sum,
-                                                        int ncell, int ntile) {
+                                                        int ncell, int ntile, ActiveBlocks ab) {
   __shared__ int wt[33];
   __shared__ int pref;
   const int t = threadIdx.x;
@@ -580,6 +601,18 @@ __global__ void __launch_bounds__(kScanTile) k_scan_add(int* __restrict__ off, c
   __syncthreads();
   const int i = blockIdx.x * kScanTile + t;
   if (i < ncell) off[i] += pref;
+  if (ab.list && blockIdx.x == 0) {
+    int base = 0;
+    for (int b0 = 0; b0 < ab.nblk; b0 += kScanTile) {
+      const int b = b0 + t;
+      const int f = (b < ab.nblk && ab.flag[b]) ? 1 : 0;
+      __syncthreads();   // wt is reused by consecutive scans
+      const int at = block_exclusive_scan_1024(f, wt, total);
+      if (f) ab.list[1 + base + at] = b;
+      base += total;
+    }
+    if (t == 0) ab.list[0] = base;
+  }
 }
 
 // Counting-sort scatter: record p moves to off[cell] + its slot, carrying p.
@@ -859,12 +892,17 @@ __device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
 // one (m, field) entry for a quad of consecutive nodes from 16-byte loads of
 // hi and 8-byte loads of the remainders, RB table rows in flight and four
 // independent sums.  The block's nodes are written back contiguously through
-// shared memory in the layout of k_cyl_field with nf = 6.
+// shared memory in the layout of k_cyl_field with nf = 6.  Block i takes the
+// node block blist[1 + i] of the blist[0] listed; the field of the others is
+// not written.
 template <typename OT, bool SPLIT, int RB, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict__ hi, const short* __restrict__ lo,
                                                     const double* __restrict__ cosc, const double* __restrict__ sinc,
-                                                    int mmax, int norder, size_t nnode, OT* __restrict__ F) {
+                                                    int mmax, int norder, size_t nnode, const int* __restrict__ blist,
+                                                    OT* __restrict__ F) {
   constexpr int QN = kTileNodes, TQ = QN / 4;
+  if ((int)blockIdx.x >= blist[0]) return;   // blocks past the listed node blocks
+  const size_t bid = (size_t)blist[1 + blockIdx.x];
   extern __shared__ unsigned char smem_raw[];
   df* cf = reinterpret_cast<df*>(smem_raw);                       // [2][(mmax+1)*norder]
   OT* tile = reinterpret_cast<OT*>(cf + 2 * (mmax + 1) * norder);
@@ -873,8 +911,8 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
   __syncthreads();
   const int nf = 6;
   const int mf_total = (mmax + 1) * nf;
-  const size_t node0 = (size_t)blockIdx.x * QN;
-  const size_t tbase = (size_t)blockIdx.x * 6 * ncoef * QN;
+  const size_t node0 = bid * QN;
+  const size_t tbase = bid * 6 * ncoef * QN;
   for (int task = threadIdx.x; task < TQ * mf_total; task += blockDim.x) {
     const int ql = task % TQ;
     const int mf = task / TQ;
@@ -913,6 +951,197 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
   const size_t nvalid = (node0 + QN <= nnode) ? QN : (nnode - node0);
   OT* dst = F + node0 * mf_total;
   for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) dst[idx] = tile[idx];
+}
+
+// Field of the fused paths through a bulk-copy (TMA) pipeline.  The work is
+// cut into units of (listed node block, field f, m-range of mg values of m);
+// persistent CTA c takes the units [c U / G, (c + 1) U / G) of the U in
+// order (G CTAs).  The table rows of a unit are one contiguous run of the
+// tiled tables (rows (f, m, k) for m in the range, every k; for the sine
+// fields the m = 0 rows are skipped), which the copy warp moves into a ring of
+// nstage shared-memory stages with cp.async.bulk, counted on the stage's
+// `full` mbarrier.  Two groups of fourteen compute warps take alternate
+// units, so that two units are summed while the next are in flight.  In a
+// group, warp-task (m, half) covers 16 node pairs; lane (k half, pair) sums
+// its half of the orders for both nodes of its pair in lazily renormalised
+// double-float, one shuffle joins the halves (the lane of the first half
+// keeps the even node, the other the odd), and the lane stores its node's
+// entry of F (layout of k_cyl_field with nf = 6; the m = 0 sine entries are
+// written as zero).  A group's warps release the stage on its `empty`
+// mbarrier; the copy warp refills it.  Waits are bounded: a timeout sets
+// *err = 1 and an abort flag that ends every later wait at once; the copy
+// warp stops issuing, and waits (bounded) for its copies in flight before it
+// exits.
+constexpr int kFieldGroupWarps = 14;
+constexpr int kFieldComputeWarps = 2 * kFieldGroupWarps;
+constexpr int kFieldThreads = 32 * (kFieldComputeWarps + 1);
+constexpr int kFieldMaxStages = 8;
+
+__device__ __forceinline__ bool field_wait(uint32_t addr, uint32_t parity, volatile int* abort, int* err) {
+  for (long long it = 0; it < TC_SPIN_LIMIT; ++it) {
+    if (mbar_test(addr, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  atomicExch(err, 1);
+  return false;
+}
+
+template <typename OT, bool SPLIT>
+__global__ void __launch_bounds__(kFieldThreads, 1)
+    k_cyl_field_bulk(const float* __restrict__ hi, const short* __restrict__ lo, const double* __restrict__ cosc,
+                     const double* __restrict__ sinc, int mmax, int norder, size_t nnode,
+                     const int* __restrict__ blist, int mg, int nstage, unsigned stage_hi_bytes,
+                     unsigned stage_bytes, unsigned cf_bytes, OT* __restrict__ F, int* __restrict__ err) {
+  constexpr int QN = kTileNodes;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  const int ncoef = (mmax + 1) * norder;
+  const int mf_total = (mmax + 1) * 6;
+  const int nmc = (mmax + mg) / mg;
+  const int per_block = 6 * nmc;
+  const long long ntot = (long long)blist[0] * per_block;
+  const int u0 = (int)(ntot * blockIdx.x / gridDim.x);
+  const int nunit = (int)(ntot * (blockIdx.x + 1) / gridDim.x) - u0;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* empty = full + kFieldMaxStages;
+  df* cf = reinterpret_cast<df*>(smem_raw + 128);
+  unsigned char* stages = smem_raw + 128 + cf_bytes;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int i = 0; i < nstage; ++i) {
+      mbar_init_count(smem_u32(full + i), 1);
+      mbar_init_count(smem_u32(empty + i), kFieldGroupWarps);
+    }
+    mbar_init_fence();
+  }
+  for (int i = threadIdx.x; i < 2 * ncoef; i += blockDim.x) cf[i] = df_from(i < ncoef ? cosc[i] : sinc[i - ncoef]);
+  __syncthreads();
+  volatile int* abort = &s_abort;
+  // unit u: node block b, field f, m in [ma, mb); rows copied from m = mc0
+  // (ma, or 1 for the sine fields when ma = 0)
+  auto unit = [&](int u, int& b, int& f, int& ma, int& mc0, int& mb) {
+    const int j = u / per_block, r = u - j * per_block;
+    f = r / nmc;
+    ma = (r - f * nmc) * mg;
+    mb = min(mmax + 1, ma + mg);
+    mc0 = (f >= 3 && ma == 0) ? 1 : ma;
+    b = blist[1 + j];
+  };
+
+  if (warp == kFieldComputeWarps) {
+    // copy warp: one lane issues every unit's copies
+    if (lane != 0) return;
+    int issued = 0;
+    for (int v = 0; v < nunit; ++v) {
+      const int st = v % nstage, use = v / nstage;
+      if (use > 0 && !field_wait(smem_u32(empty + st), (use - 1) & 1, abort, err)) break;
+      int b, f, ma, mc0, mb;
+      unit(u0 + v, b, f, ma, mc0, mb);
+      const uint32_t fa = smem_u32(full + st);
+      const unsigned rows = mb > mc0 ? (unsigned)((mb - mc0) * norder) : 0u;
+      if (rows == 0) {
+        mbar_arrive(fa);
+      } else {
+        const unsigned bh = rows * QN * 4u, bl = SPLIT ? rows * QN * 2u : 0u;
+        const size_t src = (size_t)b * 6 * ncoef * QN + ((size_t)f * ncoef + (size_t)mc0 * norder) * QN;
+        mbar_arrive_expect_tx(fa, bh + bl);
+        bulk_load(smem_u32(stages + (size_t)st * stage_bytes), hi + src, bh, fa);
+        if (SPLIT) bulk_load(smem_u32(stages + (size_t)st * stage_bytes + stage_hi_bytes), lo + src, bl, fa);
+      }
+      issued = v + 1;
+    }
+    // the copies still in flight land before the CTA may end
+    for (int v = max(0, issued - nstage); v < issued; ++v) mbar_wait(smem_u32(full + v % nstage), (v / nstage) & 1);
+    return;
+  }
+
+  const int group = warp / kFieldGroupWarps, gw = warp - group * kFieldGroupWarps;
+  const int kh = lane >> 4, p16 = lane & 15;
+  const int khalf = (norder + 1) >> 1;
+  const int kb = kh ? khalf : 0, ke = kh ? norder : khalf;
+  for (int v = group; v < nunit; v += 2) {
+    const int st = v % nstage;
+    field_wait(smem_u32(full + st), (v / nstage) & 1, abort, err);
+    int b, f, ma, mc0, mb;
+    unit(u0 + v, b, f, ma, mc0, mb);
+    const float* sh = reinterpret_cast<const float*>(stages + (size_t)st * stage_bytes);
+    const short* sl = reinterpret_cast<const short*>(stages + (size_t)st * stage_bytes + stage_hi_bytes);
+    const df* c0 = cf + (f >= 3 ? ncoef : 0);
+    for (int wt = gw; wt < 2 * (mb - ma); wt += kFieldGroupWarps) {
+      const int m = ma + (wt >> 1);
+      const int p = ((wt & 1) << 4) | p16;
+      dacc a0, a1;
+      if (m >= mc0) {
+        const size_t row0 = (size_t)(m - mc0) * norder * QN + 2 * p;
+        const df* c = c0 + m * norder;
+#pragma unroll 3
+        for (int k = kb; k < ke; ++k) {
+          const float2 h = *reinterpret_cast<const float2*>(sh + row0 + (size_t)k * QN);
+          const df ck = c[k];
+          if constexpr (SPLIT) {
+            const short2 l = *reinterpret_cast<const short2*>(sl + row0 + (size_t)k * QN);
+            a0.fma(ck, df{h.x, lo16_decode(h.x, l.x)});
+            a1.fma(ck, df{h.y, lo16_decode(h.y, l.y)});
+          } else {
+            a0.fma(ck, df{h.x, 0.f});
+            a1.fma(ck, df{h.y, 0.f});
+          }
+        }
+      }
+      // the first k half keeps node 2p, the second node 2p + 1
+      const df send = kh ? a0.raw() : a1.raw();
+      const df own = kh ? a1.raw() : a0.raw();
+      const df recv = {__shfl_xor_sync(0xffffffffu, send.h, 16), __shfl_xor_sync(0xffffffffu, send.l, 16)};
+      const size_t node = (size_t)b * QN + 2 * p + kh;
+      if (node < nnode) F[node * mf_total + m * 6 + f] = from_df<OT>(df_add(own, recv));
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_u32(empty + st));
+  }
+}
+
+// Field engine of the fused paths: 0 chooses the bulk-copy pipeline where its
+// stages fit in shared memory, 1 requires it, 2 uses the row-load kernel.
+static int g_field_engine = 0;
+static __device__ int g_cyl_err;
+
+// Shared-memory plan of k_cyl_field_bulk: the widest m-range (mg) whose
+// stages fit four deep (one summed by each compute group, two in flight)
+// beside the coefficients, and as many stages (up to kFieldMaxStages) as then
+// fit.
+struct FieldBulkPlan {
+  int mg = 0, nstage = 0;
+  unsigned stage_hi = 0, stage = 0, cf = 0;
+  size_t smem = 0;
+};
+
+static bool field_bulk_plan(const CylHandle* h, bool f64, FieldBulkPlan& P) {
+  static int optin = -1;
+  if (optin < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+      optin = 0;
+  }
+  const size_t cap = optin > 1024 ? (size_t)optin - 1024 : 0;   // 1 KB for the static shared variables
+  const size_t ncoef = (size_t)(h->mmax + 1) * h->norder;
+  P.cf = (unsigned)((2 * ncoef * sizeof(df) + 127) & ~(size_t)127);
+  const size_t fixed = 128 + P.cf;
+  for (int mg = h->mmax + 1; mg >= 1; --mg) {
+    const size_t shi = (size_t)mg * h->norder * kTileNodes * sizeof(float);
+    const size_t st = shi + (f64 ? (size_t)mg * h->norder * kTileNodes * sizeof(short) : 0);
+    if (fixed + 4 * st <= cap) {
+      P.mg = mg;
+      P.nstage = (int)std::min<size_t>(kFieldMaxStages, (cap - fixed) / st);
+      P.stage_hi = (unsigned)shi;
+      P.stage = (unsigned)st;
+      P.smem = fixed + (size_t)P.nstage * st;
+      return true;
+    }
+  }
+  return false;
 }
 
 // Double-float evaluation of the binned records (FP64 path,
@@ -1022,19 +1251,21 @@ static const int kContractRows = 6;        // orders k per k_cyl_contract_df blo
 // D and E are read once from DRAM.  The block's sums are reduced in df (warp
 // shuffles, then shared memory) and stored per chunk as FP64 for
 // k_cyl_contract_final.  D planes have a pitch of `pitch` nodes; padding
-// entries are zero in D and in the tiled tables.
+// entries are zero in D and in the tiled tables.  Only the node blocks of
+// blist (count, then block indices) are read: D is zero in the others.
 template <int KB>
 __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict__ hi, const short* __restrict__ lo,
                                                          size_t pitch, const double* __restrict__ D,
                                                          const float* __restrict__ E, int mmax, int norder,
                                                          size_t nnode, int nchunk, int ngroup,
-                                                         double* __restrict__ part) {
+                                                         const int* __restrict__ blist, double* __restrict__ part) {
   const int chunk = blockIdx.x / ngroup, g = blockIdx.x - chunk * ngroup, p = blockIdx.y;
   const int m = (p + 1) >> 1, cs = p ? ((p + 1) & 1) : 0;
   const int kbase = g * KB;
   dacc acc[KB];
   {
-    const int nq = (int)((nnode + 3) / 4);
+    constexpr int QB = kTileNodes / 4;   // quads per node block
+    const int nq = blist[0] * QB;
     const int per = (nq + nchunk - 1) / nchunk;
     const int q0 = chunk * per, q1 = min(q0 + per, nq);
     const size_t nrow = 6 * (size_t)(mmax + 1) * norder;
@@ -1042,8 +1273,10 @@ __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict
     const double* d = D + (size_t)(2 * m + cs) * pitch;
     const float* ep = E + (size_t)(2 * m + cs) * pitch;
     for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-      const size_t node = 4 * (size_t)q;
-      const size_t tb = ((node / kTileNodes) * nrow + row0) * kTileNodes + node % kTileNodes;
+      const size_t blk = (size_t)blist[1 + q / QB];
+      const size_t node = blk * kTileNodes + 4 * (q % QB);
+      if (node >= nnode) continue;   // past the last node (pitch: nnode rounded up to 4)
+      const size_t tb = (blk * nrow + row0) * kTileNodes + node % kTileNodes;
       float4 vh[KB];
       short4 vl[KB];
 #pragma unroll
@@ -1105,9 +1338,9 @@ bool cyl_tabs(void* handle, CylTab<double>* d, CylTab<float>* f) {
 int launch_cell_scan(const int* hist, int* off, int* tile_sum, int ncell, cudaStream_t st) {
   XT_REQUIRE(ncell >= 1 && ncell <= kScanTile * kScanTile, "scan of %d cells", ncell);
   const int ntile = (ncell + kScanTile - 1) / kScanTile;
-  k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tile_sum, ncell);
+  k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tile_sum, ncell, ActiveBlocks{});
   XT_CHECK_LAUNCH("k_scan_tiles");
-  k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tile_sum, ncell, ntile);
+  k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tile_sum, ncell, ntile, ActiveBlocks{});
   XT_CHECK_LAUNCH("k_scan_add");
   return XT_OK;
 }
@@ -1346,7 +1579,8 @@ static int timing_mark(int k, cudaStream_t st) {
 }
 
 struct FusedLayout {
-  size_t grid, egrid, part, hist, off, tsum, rec, srec, field, total;
+  size_t grid, egrid, part, hist, flag, blist, off, tsum, rec, srec, field, total;
+  size_t hist_bytes;   // the cell counts and the node-block flags after them, cleared together
 };
 
 static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) {
@@ -1358,7 +1592,11 @@ static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) 
   L.grid = take((size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(double));   // planes of pitch_f nodes
   L.egrid = take((size_t)(h->mmax + 1) * 2 * h->pitch_f * sizeof(float));   // FP32 companion (error parts)
   L.part = take((size_t)(h->mmax + 1) * h->norder * 2 * kContractChunksDf * sizeof(double));
-  L.hist = take(ncell * sizeof(int));
+  const size_t nblk = (h->nnode + kTileNodes - 1) / kTileNodes;
+  L.hist_bytes = align256(ncell * sizeof(int)) + nblk * sizeof(int);
+  L.hist = take(L.hist_bytes);
+  L.flag = L.hist + align256(ncell * sizeof(int));
+  L.blist = take((1 + nblk) * sizeof(int));
   L.off = take(ncell * sizeof(int));
   L.tsum = take(kScanTile * sizeof(int));
   const size_t recb = precision == XT_F32 ? sizeof(BinRec<float>) : sizeof(BinRec<df>);
@@ -1367,6 +1605,27 @@ static FusedLayout fused_layout(const CylHandle* h, long long n, int precision) 
   L.field = take(h->nnode * (h->mmax + 1) * 6 * rs);
   L.total = o;
   return L;
+}
+
+int xt_cyl_field_engine(int engine) {
+  XT_REQUIRE(engine >= 0 && engine <= 2, "field engine must be 0, 1 or 2, got %d", engine);
+  g_field_engine = engine;
+  return XT_OK;
+}
+
+int xt_cyl_status(void) {
+  int* err = nullptr;
+  XT_CUDA(cudaDeviceSynchronize());
+  XT_CUDA(cudaGetSymbolAddress((void**)&err, g_cyl_err));
+  int v = 0;
+  XT_CUDA(cudaMemcpy(&v, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) {
+    const int zero = 0;
+    XT_CUDA(cudaMemcpy(err, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    set_error("cylindrical field: a bulk-copy wait timed out");
+    return XT_ERR_DEVICE;
+  }
+  return XT_OK;
 }
 
 int xt_timing_enable(int on) {
@@ -1440,7 +1699,7 @@ static int fused_graph_launch(CylHandle* h, int precision, const double* x, cons
   std::lock_guard<std::mutex> lock(h->graph_mu);
   FusedGraph& G = h->fused;
   FusedGraph::Key key{n, precision, m1, m2, nan_to_origin, workspace, cos_out, sin_out,
-                      {outs[0], outs[1], outs[2], outs[3], outs[4]}};
+                      {outs[0], outs[1], outs[2], outs[3], outs[4]}, g_field_engine};
   const bool f64 = precision == XT_F64;
   if (!G.valid || !G.key.same(key)) {
     if (!(G.seen && G.last.same(key))) {     // first sighting of this shape: run it directly
@@ -1546,6 +1805,12 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
   int* off = reinterpret_cast<int*>(ws + L.off);
   int* tsum = reinterpret_cast<int*>(ws + L.tsum);
   const int ncell = h->numx * h->numy;
+  const int nblk = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
+  ActiveBlocks ab;
+  ab.flag = reinterpret_cast<int*>(ws + L.flag);
+  ab.list = reinterpret_cast<int*>(ws + L.blist);
+  ab.numy = h->numy;
+  ab.nblk = nblk;
   const long long ngrid = (long long)(h->mmax + 1) * 2 * (long long)h->pitch_f;   // entries of D and of E
   auto run = [&](auto tag) -> int {
     // the binning kernel zeroes D and E; without particles they are cleared here
@@ -1553,7 +1818,9 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
       XT_CUDA(cudaMemsetAsync(D, 0, (size_t)ngrid * sizeof(double), st));
       XT_CUDA(cudaMemsetAsync(E, 0, (size_t)ngrid * sizeof(float), st));
     }
-    XT_CUDA(cudaMemsetAsync(hist, 0, (size_t)ncell * sizeof(int), st));
+    XT_CUDA(cudaMemsetAsync(hist, 0, L.hist_bytes, st));   // cell counts and node-block flags
+    // without particles no node block is read (the scans that list them do not run)
+    if (n == 0) XT_CUDA(cudaMemsetAsync(ab.list, 0, sizeof(int), st));
     using R = decltype(tag);
     constexpr bool F64 = std::is_same<R, double>::value;
     using RT = typename std::conditional<F64, df, float>::type;   // record arithmetic
@@ -1576,9 +1843,9 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
       if ((rc = timing_mark(1, st))) return rc;
       {
         const int ntile = (ncell + kScanTile - 1) / kScanTile;
-        k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tsum, ncell);
+        k_scan_tiles<<<ntile, kScanTile, 0, st>>>(hist, off, tsum, ncell, ab);
         XT_CHECK_LAUNCH("k_scan_tiles");
-        k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tsum, ncell, ntile);
+        k_scan_add<<<ntile, kScanTile, 0, st>>>(off, tsum, ncell, ntile, ab);
         XT_CHECK_LAUNCH("k_scan_add");
       }
       if ((rc = timing_mark(2, st))) return rc;
@@ -1623,7 +1890,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
     const int cap = resident_blocks_per_sm((const void*)k_cyl_contract_df<kContractRows>, 128, 0) * sm_count();
     const int nch = std::max(1, std::min(kContractChunksDf, cap / (ngroup * npair)));
     k_cyl_contract_df<kContractRows><<<dim3(nch * ngroup, npair), 128, 0, st>>>(
-        h->tile_hi, h->tile_lo, h->pitch_f, D, E, h->mmax, h->norder, h->nnode, nch, ngroup, part);
+        h->tile_hi, h->tile_lo, h->pitch_f, D, E, h->mmax, h->norder, h->nnode, nch, ngroup, ab.list, part);
     XT_CHECK_LAUNCH("k_cyl_contract_df");
     // (the sum of the partials folded into the contraction's last block was
     // measured no faster)
@@ -1636,22 +1903,37 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
     // FP64 path: double-float field from the double-float tables; mixed path:
     // FP32 field from the FP32 tables (coefficients staged as df in both)
     using FT = std::conditional_t<F64, df, float>;
-    // One block per node block of the tiled tables: 224 threads (the 672
-    // (m, field, quad) tasks of a 64-node block in three rounds, four blocks
-    // per SM), six rows in flight.  Measured on the 257^2-node, M = 6, Q = 18
-    // table: 0.059 ms against 0.067 (256 threads), 0.066 (672) and 0.072 (96).
-    {
+    FieldBulkPlan P;
+    const bool bulk = g_field_engine != 2 && field_bulk_plan(h, F64, P);
+    XT_REQUIRE(bulk || g_field_engine != 1, "the bulk-copy field pipeline does not fit M = %d, Q = %d", h->mmax,
+               h->norder);
+    if (bulk) {
+      // bulk-copy pipeline: one persistent CTA per SM over the node blocks
+      auto kern = k_cyl_field_bulk<FT, F64>;
+      XT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+      static int* err = nullptr;
+      if (!err) XT_CUDA(cudaGetSymbolAddress((void**)&err, g_cyl_err));
+      const int grid = std::min(nblk, sm_count());
+      kern<<<grid, kFieldThreads, P.smem, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax, h->norder,
+                                                h->nnode, ab.list, P.mg, P.nstage, P.stage_hi, P.stage, P.cf,
+                                                reinterpret_cast<FT*>(field), err);
+    } else {
+      // row loads: one block per node block of the tiled tables, 224 threads
+      // (the 672 (m, field, quad) tasks of a 64-node block in three rounds,
+      // four blocks per SM), six rows in flight.  Measured on the 257^2-node,
+      // M = 6, Q = 18 table: 0.059 ms against 0.067 (256 threads), 0.066 (672)
+      // and 0.072 (96).
       constexpr int RB = 6, NT = 224, MINB = 4;
-      const int fblocks = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
       const size_t sm = 2 * (size_t)(h->mmax + 1) * h->norder * sizeof(df) +
                         kTileNodes * (size_t)(h->mmax + 1) * 6 * sizeof(FT);
       if (sm > 48 * 1024)
         XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, F64, RB, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm));
-      k_cyl_field2<FT, F64, RB, NT, MINB><<<fblocks, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax,
-                                                                   h->norder, h->nnode, reinterpret_cast<FT*>(field));
+      k_cyl_field2<FT, F64, RB, NT, MINB><<<nblk, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax,
+                                                                h->norder, h->nnode, ab.list,
+                                                                reinterpret_cast<FT*>(field));
     }
-    XT_CHECK_LAUNCH("k_cyl_field2");
+    XT_CHECK_LAUNCH(bulk ? "k_cyl_field_bulk" : "k_cyl_field2");
     if ((rc = timing_mark(6, st))) return rc;
     if (n > 0) {
       // Device results are evaluated from the cell-sorted records (neighbouring

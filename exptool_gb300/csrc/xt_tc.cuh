@@ -1,7 +1,9 @@
 // tcgen05 (5th-generation tensor core) building blocks shared by the
 // kernels that use it: shared-memory matrix and instruction descriptors,
 // MMA issue and commit, the fences around thread synchronisation, mbarrier
-// set-up and a bounded wait, and tensor-memory loads.
+// set-up and a bounded wait, and tensor-memory loads; and the bulk copies
+// (cp.async.bulk, the non-tensor TMA path) between global and shared memory
+// with their mbarrier transaction counts.
 //
 // Operand tiles use the canonical K-major, no-swizzle layout: 8-row x 16-byte
 // core matrices, LBO bytes between core matrices along K, SBO bytes between
@@ -92,6 +94,57 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
     if (done) return true;
   }
   return false;
+}
+
+// mbarrier with an arrival count, and its arrivals: a plain one, and one that
+// also expects `bytes` of bulk-copy transactions in the current phase.
+__device__ __forceinline__ void mbar_init_count(uint32_t addr, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t addr, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+// from global to this CTA's shared memory; completion is counted on mbar.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+// Bulk copy from shared to global memory in the issuing thread's bulk group;
+// the shared source must be made visible to the async proxy first
+// (fence_async_smem by every thread that wrote it, then a barrier).
+__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the issuing thread's bulk stores have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and have completed their writes
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Barrier over the first `count` threads of the CTA (a multiple of 32) on
+// named barrier `id`.
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {

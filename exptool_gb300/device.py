@@ -502,6 +502,18 @@ class CylField:
         self.table, self.buf, self.precision, self.density = table, buf, precision, density
 
 
+def cyl_field_engine(engine):
+    """Kernel of the cylindrical field stage for later calls: 0 automatic
+    (the bulk-copy pipeline where it fits), 1 the pipeline, 2 row loads."""
+    _lib.check(_lib.load().xt_cyl_field_engine(int(engine)), "xt_cyl_field_engine")
+
+
+def cyl_status():
+    """Raise XTError if a cylindrical field launch reported a bulk-copy wait
+    that timed out; synchronises the device."""
+    _lib.check(_lib.load().xt_cyl_status(), "xt_cyl_status")
+
+
 def batched_tc_status():
     """Raise XTError if a batched tensor-core launch reported an error (an
     MMA wait that timed out, or a particle outside its sorted window);

@@ -1,8 +1,8 @@
 """Orbit frequencies with the interface of ``exptool/orbits/frequencies.py``,
 computed for whole orbit maps at once on the GPU by one kernel of this library
 (``xt_orbit_spectra``): one CTA per orbit takes the N-point DFT of its signal
-in double-float arithmetic in shared memory (radix-2 FFT for N a power of two,
-Bluestein's transform otherwise) and searches the spectrum for its peaks in
+in double-float arithmetic in shared memory (radix-4 Stockham FFT for N a
+power of two, Bluestein's transform otherwise) and searches the spectrum for its peaks in
 place, so only indices and powers leave the device.  The reference loops over
 orbits with numpy.fft.
 

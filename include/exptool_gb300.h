@@ -235,6 +235,20 @@ int xt_cyl_eval_sorted(void *handle, const double *x, const double *y, const dou
                        int m1, int m2, const double *cos_c, const double *sin_c, double *const *outs,
                        void *workspace, size_t workspace_bytes, void *stream);
 
+/* Field stage of xt_cyl_accumulate_eval and xt_cyl_eval_sorted (the
+ * potential and force tables contracted with the coefficients at every node,
+ * eof.py:1100-1125 summed once per node instead of per particle).
+ * xt_cyl_field_engine selects its kernel for later calls: 0 (default) the
+ * bulk-copy pipeline (cp.async.bulk staging of each node block's table rows in
+ * shared memory, one persistent CTA per SM) where its stages fit, else row
+ * loads; 1 the pipeline (XT_ERR_ARG from the calls where it does not fit);
+ * 2 row loads.  Both give the field to double-float rounding (not bit-equal:
+ * the pipeline sums two halves of the orders separately).
+ * xt_cyl_status synchronises the device and reports (and clears) the error
+ * flag of the pipeline's bounded waits: XT_ERR_DEVICE, else XT_OK. */
+int xt_cyl_field_engine(int engine);
+int xt_cyl_status(void);
+
 /* Stage timing (diagnostics, no counterpart in the reference): with
  * xt_timing_enable(1), xt_cyl_accumulate_eval records CUDA events on its
  * stream between its stages; xt_timing_read waits for the last one and writes

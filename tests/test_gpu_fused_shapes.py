@@ -62,3 +62,45 @@ def test_fused_shapes_against_oracle(shape, precision):
     # the coefficient difference is inside the tolerance above
     for k in range(6):
         assert _rel(outs[k], ref[k]) <= tol, (k, _rel(outs[k], ref[k]))
+
+
+ENGINE_SHAPES = [(8, 24, 40, 30), (0, 4, 20, 12), (6, 18, 48, 24), (5, 7, 33, 21)]
+
+
+@pytest.mark.parametrize("shape", ENGINE_SHAPES, ids=lambda s: "m%d_n%d_%dx%d" % s)
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_field_engines_agree(shape, precision):
+    """The field stage's bulk-copy pipeline (engine 1) and row-load kernel
+    (engine 2) on the same particles: forces agree to double-float rounding
+    of the field (FP64 path) or to FP32 rounding of it (mixed path), and the
+    pipeline's against the oracle at the bar of the test above.  The shapes
+    take the pipeline through two m-ranges per field (M = 8, Q = 24), sine
+    units with no rows (M = 0), and last node blocks of 55, 17 and 9 nodes
+    whose FP32 tile is written by plain stores; its wait flag stays clear."""
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import eof
+    from oracle import eof as oeof
+    mmax, norder, numx, numy = shape
+    (potC, rforceC, zforceC, potS, rforceS, zforceS), (x, y, z, m), p = _case(*shape, seed=23, n=30000)
+    table = eof.table_from_arrays(mmax, norder, numx, numy, p["cmap"], p["XMIN"], p["dX"], p["YMIN"], p["dY"],
+                                  p["ascale"], p["hscale"], potC, rforceC, zforceC, potS, rforceS, zforceS)
+    got = {}
+    try:
+        for engine in (1, 2):
+            dev.cyl_field_engine(engine)
+            cos, sin, outs = table.accumulate_eval(*(dev.to_dev(a) for a in (x, y, z, m)), precision=precision)
+            got[engine] = [dev.to_host(o) for o in outs]
+            dev.cyl_status()
+    finally:
+        dev.cyl_field_engine(0)
+    agree = 1e-12 if precision == "f64" else 1e-6
+    for k in range(6):
+        assert _rel(got[1][k], got[2][k]) <= agree, (k, _rel(got[1][k], got[2][k]))
+    c, s = oeof.accumulate(x, y, z, m, potC, potS, mmax, norder, p["XMIN"], p["dX"], p["YMIN"], p["dY"], numx, numy,
+                           p["ascale"], p["hscale"], p["cmap"])
+    ref = oeof.accumulated_eval_particles(x, y, z, c, s, potC, rforceC, zforceC, potS, rforceS, zforceS, p["XMIN"],
+                                          p["dX"], p["YMIN"], p["dY"], numx, numy, mmax, norder, p["ascale"],
+                                          p["hscale"], p["cmap"])
+    tol = 1e-10 if precision == "f64" else 2e-5
+    for k in range(6):
+        assert _rel(got[1][k], ref[k]) <= tol, (k, _rel(got[1][k], ref[k]))
