@@ -45,13 +45,15 @@ L2_BYTES = 129 * 1024 * 1024
 # workload, from an ncu --set full capture of `bench.py --profile`, and what
 # bounds the stage there
 STAGE_TRAFFIC_F64 = {
-    "k_cyl_binrec": (32_190_976 + 9_330_944, "FP32-pipe bound (double-float set-up): FMA pipe 52 %, IPC 2.9 / SM"),
-    "k_cyl_scatter": (57_617_152 + 11_612_672, "scattered 16-byte record stores: LSU throttle"),
-    "k_cyl_deposit_sorted": (52_226_304 + 15_616, "issue bound: 128 registers, IPC 2.4 / SM, FMA pipe 39 %"),
-    "k_cyl_contract_partial+final": (103_575_040 + 2_585_600, "HBM latency: 53 % of peak DRAM throughput"),
-    "k_cyl_field": (278_408_960 + 15_237_120, "HBM: 67 % of peak DRAM throughput, IPC 2.5 / SM"),
-    "k_cyl_eval_sorted": (89_757_440 + 36_104_448,
-                          "FP32-pipe bound (double-float arithmetic): FMA pipe 53 %, IPC 2.5 / SM"),
+    "k_cyl_binrec": (32_196_608 + 9_432_576, "FP32-pipe bound (double-float set-up): FMA pipe 52 %, IPC 2.9 / SM"),
+    "k_cyl_scatter": (57_392_384 + 11_328_768, "scattered 16-byte record stores: LSU throttle"),
+    "k_cyl_deposit_sorted": (52_241_920 + 10_752, "issue bound: 128 registers, IPC 2.4 / SM, FMA pipe 37 %"),
+    "k_cyl_contract_partial+final": (63_789_056 + 539_648,
+                                     "HBM latency: 41 % of peak DRAM throughput (listed node blocks only)"),
+    "k_cyl_field": (172_532_224 + 8_532_736,
+                    "bulk-copy pipeline, HBM and issue: 59 % of peak DRAM throughput, IPC 2.9 / SM"),
+    "k_cyl_eval_sorted": (89_821_696 + 36_030_464,
+                          "FP32-pipe bound (double-float arithmetic): FMA pipe 57 %, IPC 2.6 / SM"),
 }
 
 
@@ -59,8 +61,8 @@ STAGE_TRAFFIC_F64 = {
 # fused stage, from the same ncu capture: the double-float stages are bound by
 # FP32 issue, so the HBM fraction alone understates how busy they are
 STAGE_PIPE_F64 = {
-    "k_cyl_binrec": (51.9, 2.9), "k_cyl_scatter": (1.3, 0.16), "k_cyl_deposit_sorted": (38.5, 2.4),
-    "k_cyl_contract_partial+final": (37.0, 2.6), "k_cyl_field": (36.6, 2.5), "k_cyl_eval_sorted": (53.4, 2.5),
+    "k_cyl_binrec": (52.4, 2.9), "k_cyl_scatter": (1.6, 0.15), "k_cyl_deposit_sorted": (37.1, 2.4),
+    "k_cyl_contract_partial+final": (33.4, 2.4), "k_cyl_field": (43.0, 2.9), "k_cyl_eval_sorted": (56.5, 2.6),
 }
 
 
@@ -630,9 +632,14 @@ def gpu_arm(args, rank, world):
     phases = {n: {"ms": round(float(ph64[i]), 4), "alg_bytes": sep_alg[n],
                   "gbs": round(sep_alg[n] / (ph64[i] * 1e-3) / 1e9, 1)} for i, n in enumerate(names)}
     stages64 = stage_times(fused, "f64", K)
+    nact, nblk = table.active_blocks(fws, N1, "f64")
     stages32 = stage_times(fused, "f32", K)
     st_names = ["k_cyl_binrec", "k_scan_cells", "k_cyl_scatter", "k_cyl_deposit_sorted",
                 "k_cyl_contract_partial+final", "k_cyl_field", "k_cyl_eval_sorted"]
+
+    # the contraction and the field read only the listed node blocks (64 nodes
+    # each, those touching a cell with particles)
+    anode = nact * 64
 
     def stage_alg(rs):
         # algorithmic bytes per launch of each stage (rs = bytes of the compute
@@ -644,15 +651,18 @@ def gpu_arm(args, rank, world):
         grid = 14 * nnode * 8
         tab = 6 if rs == 8 else 4
         return [N1 * (32 + rec + 8 + 4), 2 * 4 * 65536, N1 * (2 * rec + 4), N1 * rec + grid,
-                13 * 18 * nnode * 6 + grid + 14 * nnode * 4,
-                (7 + 7 + 7 + 6 + 6 + 6) * 18 * nnode * tab + nnode * 7 * 6 * rs,
+                13 * 18 * anode * 6 + 14 * anode * (8 + 4),
+                (7 + 7 + 7 + 6 + 6 + 6) * 18 * anode * tab + anode * 7 * 6 * rs,
                 N1 * (rec + 40) + nnode * 7 * 6 * rs]
 
     alg64 = stage_alg(8)
     alg32 = stage_alg(4)
     dom = int(np.argmax(stages64))
     ach = alg64[dom] / (stages64[dom] * 1e-3) / 1e9
-    fused_stages = {"f64": {n: {"ms": round(float(stages64[i]), 4),
+    fused_stages = {"node_blocks": {"listed": nact, "total": nblk,
+                                    "what": "contraction and field read only node blocks touching a cell with "
+                                            "particles"},
+                    "f64": {n: {"ms": round(float(stages64[i]), 4),
                                 "gbs": round(alg64[i] / (stages64[i] * 1e-3) / 1e9, 1)}
                             for i, n in enumerate(st_names)},
                     "f32": {n: {"ms": round(float(stages32[i]), 4),
@@ -679,8 +689,9 @@ def gpu_arm(args, rank, world):
                 "d2h_bytes_per_step": d2h, "api": "eof.compute_coefficients_and_forces, pinned numpy inputs",
                 "separate_calls_value": world * N1 / sep_s},
         "pipeline": "fused: double-float per-particle set-up once, counting sort of 48-byte records by table "
-                    "cell, run-accumulated cooperative deposit, double-float contraction, field and sorted "
-                    "evaluation (9 kernels)",
+                    "cell (the scans also list the node blocks touching occupied cells), run-accumulated "
+                    "cooperative deposit, double-float contraction and field over the listed node blocks (the "
+                    "field through a cp.async.bulk shared-memory pipeline) and sorted evaluation (9 kernels)",
         "gpu_launches": 9 * K,
         "roofline": {"bound": "hbm", "kernel": st_names[dom], "achieved": round(ach, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(ach / peak, 4), "traffic": STAGE_TRAFFIC_F64[st_names[dom]][0],

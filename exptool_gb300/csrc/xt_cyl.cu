@@ -1613,6 +1613,18 @@ int xt_cyl_field_engine(int engine) {
   return XT_OK;
 }
 
+int xt_cyl_active_blocks(void* handle, const void* workspace, long long n, int precision, int* active,
+                         int* total) {
+  CylHandle* h = static_cast<CylHandle*>(handle);
+  XT_REQUIRE(h && workspace && active && total, "NULL argument");
+  XT_REQUIRE(n >= 0, "particle count must be >= 0");
+  const FusedLayout L = fused_layout(h, n, precision);
+  XT_CUDA(cudaDeviceSynchronize());
+  XT_CUDA(cudaMemcpy(active, static_cast<const char*>(workspace) + L.blist, sizeof(int), cudaMemcpyDeviceToHost));
+  *total = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
+  return XT_OK;
+}
+
 int xt_cyl_status(void) {
   int* err = nullptr;
   XT_CUDA(cudaDeviceSynchronize());

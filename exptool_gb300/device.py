@@ -384,6 +384,16 @@ class CylTable:
                                                     dptr(ws), ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
         return cos, sin, outs
 
+    def active_blocks(self, workspace, n, precision="f64"):
+        """(listed, total) node blocks of the last fused call made on
+        ``workspace`` for n particles: the blocks the contraction and the
+        field stage read (those touching a cell with particles).  Synchronises
+        the device."""
+        a, t = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(self._lib.xt_cyl_active_blocks(self.handle, dptr(workspace), int(n), precision_code(precision),
+                                                  ctypes.byref(a), ctypes.byref(t)), "xt_cyl_active_blocks")
+        return a.value, t.value
+
     def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True, r_out=None):
         """accumulate_eval into per-thread buffers kept for the last particle
         count and precision: returns the (2, mmax+1, norder) coefficient block

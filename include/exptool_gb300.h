@@ -249,6 +249,15 @@ int xt_cyl_eval_sorted(void *handle, const double *x, const double *y, const dou
 int xt_cyl_field_engine(int engine);
 int xt_cyl_status(void);
 
+/* Node blocks (64 consecutive nodes of the tables) that the last
+ * xt_cyl_accumulate_eval / xt_cyl_accumulate_sorted / xt_cyl_eval_sorted call
+ * on `workspace` (made for n particles at `precision`) contracted and
+ * evaluated: those holding a corner node of a table cell with particles;
+ * the deposit grid is zero elsewhere and the evaluation reads no other node.
+ * Synchronises the device; *total = all node blocks of the table.
+ * Diagnostics, no counterpart in the reference. */
+int xt_cyl_active_blocks(void *handle, const void *workspace, long long n, int precision, int *active, int *total);
+
 /* Stage timing (diagnostics, no counterpart in the reference): with
  * xt_timing_enable(1), xt_cyl_accumulate_eval records CUDA events on its
  * stream between its stages; xt_timing_read waits for the last one and writes
