@@ -106,21 +106,35 @@ __global__ void k_split_tab(const double* __restrict__ a, float* __restrict__ hi
 
 constexpr int kTileNodes = 64;   // nodes per block of the tiled fused tables
 
+// The tiled tables take the nodes in rows of constant z: tile position
+// t = iy * (numx + 1) + ix holds node ix * (numy + 1) + iy, and a block is 64
+// consecutive positions.  A disc fills a band of z rows, so fewer blocks
+// touch its cells than with runs along z (429 against 632 of 1033 blocks for
+// the 1e6-particle exponential disc on the 257^2 table).
+struct TileOrder {
+  int nx1, ny1;   // numx + 1, numy + 1
+  __host__ __device__ size_t node(size_t t) const {
+    const size_t iy = t / nx1;
+    return (t - iy * nx1) * ny1 + iy;
+  }
+  __host__ __device__ size_t pos(int ix, int iy) const { return (size_t)iy * nx1 + ix; }
+};
+
 // Tiled fused tables (CylHandle::tile_hi/tile_lo) from the FP64 tables a
 // ([8][mmax+1][norder][nnode]); entries past nnode are zero.  Set-up, once.
 __global__ void k_tile_tab(const double* __restrict__ a, float* __restrict__ hi, short* __restrict__ lo,
-                           int nmk, size_t nnode, size_t nblk) {
+                           int nmk, size_t nnode, size_t nblk, TileOrder to) {
   const size_t rows = 6 * (size_t)nmk;
   const size_t n = nblk * rows * kTileNodes;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const size_t b = i / (rows * kTileNodes), rem = i - b * rows * kTileNodes;
-    const size_t row = rem / kTileNodes, node = b * kTileNodes + (rem - row * kTileNodes);
+    const size_t row = rem / kTileNodes, tp = b * kTileNodes + (rem - row * kTileNodes);
     const int f = (int)(row / nmk), mk = (int)(row - (size_t)f * nmk);
     const int t = f < 3 ? f : f + 1;                       // skip densC
     float h = 0.f;
     short l = 0;
-    if (node < nnode) {
-      const double v = a[((size_t)t * nmk + mk) * nnode + node];
+    if (tp < nnode) {
+      const double v = a[((size_t)t * nmk + mk) * nnode + to.node(tp)];
       h = (float)v;
       l = lo16_encode(v, h);
     }
@@ -559,13 +573,14 @@ __device__ __forceinline__ int block_exclusive_scan_1024(int v, int* warp_tot, i
 }
 
 // Node blocks of the tiled tables whose field the evaluation reads: those
-// holding a corner node of a cell with particles (cell = ix * numy + iy,
-// corners (ix + {0,1}) * (numy + 1) + iy + {0,1}).  The deposit grid is zero
-// outside them, so the contraction may skip the others as well.
+// holding a corner node (ix + {0,1}, iy + {0,1}) of a cell with particles
+// (cell = ix * numy + iy).  The deposit grid is zero outside them, so the
+// contraction may skip the others as well.
 struct ActiveBlocks {
   int* flag = nullptr;    // [nblk], cleared before the scan; nullptr: not wanted
   int* list = nullptr;    // [1 + nblk]: count, then the marked blocks in increasing order
   int numy = 0, nblk = 0;
+  TileOrder to{1, 1};
 };
 
 __global__ void __launch_bounds__(kScanTile) k_scan_tiles(const int* __restrict__ hist, int* __restrict__ off,
@@ -579,11 +594,11 @@ __global__ void __launch_bounds__(kScanTile) k_scan_tiles(const int* __restrict_
   if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
   if (ab.flag && v > 0) {
     const int ix = i / ab.numy, iy = i - ix * ab.numy;
-    const int n00 = ix * (ab.numy + 1) + iy, n10 = n00 + ab.numy + 1;
-    ab.flag[n00 / kTileNodes] = 1;   // same-value stores: their order does not matter
-    ab.flag[(n00 + 1) / kTileNodes] = 1;
-    ab.flag[n10 / kTileNodes] = 1;
-    ab.flag[(n10 + 1) / kTileNodes] = 1;
+    const size_t t00 = ab.to.pos(ix, iy), t01 = t00 + ab.to.nx1;   // (ix, iy + 1)
+    ab.flag[t00 / kTileNodes] = 1;   // same-value stores: their order does not matter
+    ab.flag[(t00 + 1) / kTileNodes] = 1;
+    ab.flag[t01 / kTileNodes] = 1;
+    ab.flag[(t01 + 1) / kTileNodes] = 1;
   }
 }
 
@@ -739,11 +754,14 @@ constexpr int kDepSlots = 32;
 // and then the sine sums (m = 1..MCAP), so that half the sums are live at a
 // time (double-float sums: 104 -> 56 registers of accumulators, for more
 // resident warps) and each pass runs only its own Chebyshev recurrence; the
-// second pass re-reads the run's records from L1.
+// second pass re-reads the run's records from L1.  The grids D and E are
+// indexed by the tile position of the node (TileOrder: rows of constant z),
+// the order in which the contraction reads them.
 template <typename M, int MCAP, int NPASS>
 __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
-    k_cyl_deposit_sorted(int numy, int mmax, long long n, int run, const BinRec<typename M::T>* __restrict__ srec,
-                         double* __restrict__ D, float* __restrict__ E, size_t plane) {
+    k_cyl_deposit_sorted(int numy, int nx1, int mmax, long long n, int run,
+                         const BinRec<typename M::T>* __restrict__ srec, double* __restrict__ D,
+                         float* __restrict__ E, size_t plane) {
   using T = typename M::T;
   using A = typename M::A;
   // sums per pass: all 2 MCAP + 1 in one pass, else the cosines then the sines
@@ -751,9 +769,8 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
   constexpr int NEMAX = 4 * (NJ0 > NJ1 ? NJ0 : NJ1);
   constexpr int PITCH = NEMAX + 1;              // conflict-free parking of up to 8 lanes
   __shared__ A park[4][kDepSlots][PITCH];
-  __shared__ int park_node[4][kDepSlots];     // lower-left node of the parked lane's cell
+  __shared__ int park_node[4][kDepSlots];     // tile position of the parked lane's lower-left node
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int ny1 = numy + 1;
   const int nju = 2 * mmax + 1;                 // sums in use (global index j)
   const long long nrun = (n + run - 1) / run;
 
@@ -783,7 +800,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
         if (batch & (1u << lane)) {
           const int sidx = __popc(batch & ((1u << lane) - 1));
           const int ix = cell / numy, iy = cell - ix * numy;
-          park_node[wib][sidx] = ix * ny1 + iy;
+          park_node[wib][sidx] = iy * nx1 + ix;
 #pragma unroll
           for (int j = 0; j < NJP; ++j)
 #pragma unroll
@@ -801,7 +818,7 @@ __global__ void __launch_bounds__(128, NPASS == 2 ? 4 : (MCAP <= 6 ? 3 : 2))
           if (j < nju) {
             const int m = (j + 1) >> 1;        // j = 0: m=0 cos; j = 2m-1: cos m; j = 2m: sin m
             const int cs = (j != 0 && !(j & 1)) ? 1 : 0;
-            const size_t off = (size_t)(2 * m + cs) * plane + ((k & 1) ? ny1 : 0) + ((k & 2) ? 1 : 0);
+            const size_t off = (size_t)(2 * m + cs) * plane + ((k & 1) ? 1 : 0) + ((k & 2) ? nx1 : 0);
             int nd = park_node[wib][0];
             A a = park[wib][0][e];
             for (int sidx = 1; sidx < nb; ++sidx) {
@@ -891,15 +908,15 @@ __device__ __forceinline__ float from_df<float>(df v) { return v.h + v.l; }
 // (kTileNodes nodes, one contiguous region of them).  Each thread computes
 // one (m, field) entry for a quad of consecutive nodes from 16-byte loads of
 // hi and 8-byte loads of the remainders, RB table rows in flight and four
-// independent sums.  The block's nodes are written back contiguously through
-// shared memory in the layout of k_cyl_field with nf = 6.  Block i takes the
-// node block blist[1 + i] of the blist[0] listed; the field of the others is
-// not written.
+// independent sums.  The block's nodes are written back through shared
+// memory, each node's entries contiguous, in the layout of k_cyl_field with
+// nf = 6.  Block i takes the node block blist[1 + i] of the blist[0] listed;
+// the field of the others is not written.
 template <typename OT, bool SPLIT, int RB, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict__ hi, const short* __restrict__ lo,
                                                     const double* __restrict__ cosc, const double* __restrict__ sinc,
-                                                    int mmax, int norder, size_t nnode, const int* __restrict__ blist,
-                                                    OT* __restrict__ F) {
+                                                    int mmax, int norder, size_t nnode, TileOrder to,
+                                                    const int* __restrict__ blist, OT* __restrict__ F) {
   constexpr int QN = kTileNodes, TQ = QN / 4;
   if ((int)blockIdx.x >= blist[0]) return;   // blocks past the listed node blocks
   const size_t bid = (size_t)blist[1 + blockIdx.x];
@@ -949,8 +966,10 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
   }
   __syncthreads();
   const size_t nvalid = (node0 + QN <= nnode) ? QN : (nnode - node0);
-  OT* dst = F + node0 * mf_total;
-  for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) dst[idx] = tile[idx];
+  for (int idx = threadIdx.x; idx < (int)(nvalid * mf_total); idx += blockDim.x) {
+    const int j = idx / mf_total;
+    F[to.node(node0 + j) * mf_total + (idx - j * mf_total)] = tile[idx];
+  }
 }
 
 // Field of the fused paths through a bulk-copy (TMA) pipeline.  The work is
@@ -965,7 +984,7 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
 // group, warp-task (m, half) covers 16 node pairs; lane (k half, pair) sums
 // its half of the orders for both nodes of its pair in lazily renormalised
 // double-float, one shuffle joins the halves (the lane of the first half
-// keeps the even node, the other the odd), and the lane stores its node's
+// keeps the even position, the other the odd), and the lane stores its node's
 // entry of F (layout of k_cyl_field with nf = 6; the m = 0 sine entries are
 // written as zero).  A group's warps release the stage on its `empty`
 // mbarrier; the copy warp refills it.  Waits are bounded: a timeout sets
@@ -990,7 +1009,7 @@ __device__ __forceinline__ bool field_wait(uint32_t addr, uint32_t parity, volat
 template <typename OT, bool SPLIT>
 __global__ void __launch_bounds__(kFieldThreads, 1)
     k_cyl_field_bulk(const float* __restrict__ hi, const short* __restrict__ lo, const double* __restrict__ cosc,
-                     const double* __restrict__ sinc, int mmax, int norder, size_t nnode,
+                     const double* __restrict__ sinc, int mmax, int norder, size_t nnode, TileOrder to,
                      const int* __restrict__ blist, int mg, int nstage, unsigned stage_hi_bytes,
                      unsigned stage_bytes, unsigned cf_bytes, OT* __restrict__ F, int* __restrict__ err) {
   constexpr int QN = kTileNodes;
@@ -1069,6 +1088,8 @@ __global__ void __launch_bounds__(kFieldThreads, 1)
     const float* sh = reinterpret_cast<const float*>(stages + (size_t)st * stage_bytes);
     const short* sl = reinterpret_cast<const short*>(stages + (size_t)st * stage_bytes + stage_hi_bytes);
     const df* c0 = cf + (f >= 3 ? ncoef : 0);
+    const size_t t0 = (size_t)b * QN;   // the block's first tile position
+    const int iy0 = (int)(t0 / to.nx1), ix0 = (int)(t0 - (size_t)iy0 * to.nx1);
     for (int wt = gw; wt < 2 * (mb - ma); wt += kFieldGroupWarps) {
       const int m = ma + (wt >> 1);
       const int p = ((wt & 1) << 4) | p16;
@@ -1094,8 +1115,15 @@ __global__ void __launch_bounds__(kFieldThreads, 1)
       const df send = kh ? a0.raw() : a1.raw();
       const df own = kh ? a1.raw() : a0.raw();
       const df recv = {__shfl_xor_sync(0xffffffffu, send.h, 16), __shfl_xor_sync(0xffffffffu, send.l, 16)};
-      const size_t node = (size_t)b * QN + 2 * p + kh;
-      if (node < nnode) F[node * mf_total + m * 6 + f] = from_df<OT>(df_add(own, recv));
+      const int o = 2 * p + kh;   // offset in the block: position t0 + o, node (ix, iy)
+      if (t0 + o < nnode) {
+        int ix = ix0 + o, iy = iy0;
+        while (ix >= to.nx1) {   // at most 64 / nx1 + 1 rows
+          ix -= to.nx1;
+          ++iy;
+        }
+        F[((size_t)ix * to.ny1 + iy) * mf_total + m * 6 + f] = from_df<OT>(df_add(own, recv));
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(smem_u32(empty + st));
@@ -1247,7 +1275,8 @@ static const int kContractRows = 6;        // orders k per k_cyl_contract_df blo
 // Each thread multiplies the quads' FP64 sums (split into float pairs by
 // integer operations) by the tiled double-float tables (16-byte loads of hi,
 // 8-byte loads of the 16-bit remainders, all KB rows in flight) in lazily
-// renormalised df sums.  The groups of one chunk are neighbouring blocks, so
+// renormalised df sums; a quad is four consecutive tile positions, and D and
+// E are indexed by tile position as well.  The groups of one chunk are neighbouring blocks, so
 // D and E are read once from DRAM.  The block's sums are reduced in df (warp
 // shuffles, then shared memory) and stored per chunk as FP64 for
 // k_cyl_contract_final.  D planes have a pitch of `pitch` nodes; padding
@@ -1274,9 +1303,9 @@ __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict
     const float* ep = E + (size_t)(2 * m + cs) * pitch;
     for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       const size_t blk = (size_t)blist[1 + q / QB];
-      const size_t node = blk * kTileNodes + 4 * (q % QB);
-      if (node >= nnode) continue;   // past the last node (pitch: nnode rounded up to 4)
-      const size_t tb = (blk * nrow + row0) * kTileNodes + node % kTileNodes;
+      const size_t t = blk * kTileNodes + 4 * (q % QB);   // tile position of the quad's first node
+      if (t >= nnode) continue;   // past the last node (pitch: nnode rounded up to 4; D, E zero there)
+      const size_t tb = (blk * nrow + row0) * kTileNodes + t % kTileNodes;
       float4 vh[KB];
       short4 vl[KB];
 #pragma unroll
@@ -1287,9 +1316,9 @@ __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict
           vl[u] = *reinterpret_cast<const short4*>(lo + o);
         }
       }
-      const double2 da = *reinterpret_cast<const double2*>(d + node);
-      const double2 db = *reinterpret_cast<const double2*>(d + node + 2);
-      const float4 ev = *reinterpret_cast<const float4*>(ep + node);
+      const double2 da = *reinterpret_cast<const double2*>(d + t);
+      const double2 db = *reinterpret_cast<const double2*>(d + t + 2);
+      const float4 ev = *reinterpret_cast<const float4*>(ep + t);
       const df dv[4] = {df_add(df_split_or_from(da.x), {ev.x, 0.f}), df_add(df_split_or_from(da.y), {ev.y, 0.f}),
                         df_add(df_split_or_from(db.x), {ev.z, 0.f}), df_add(df_split_or_from(db.y), {ev.w, 0.f})};
 #pragma unroll
@@ -1408,7 +1437,7 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
     k_split_tab<<<grid_for((long long)(rows * h->pitch_f), 256, 8), 256>>>(h->tab, h->tab_f32, rows, h->nnode,
                                                                            h->pitch_f);
     k_tile_tab<<<grid_for((long long)ntile, 256, 8), 256>>>(h->tab, h->tile_hi, h->tile_lo, (mmax + 1) * norder,
-                                                            h->nnode, nblk);
+                                                            h->nnode, nblk, TileOrder{numx + 1, numy + 1});
     e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaGetLastError();
   }
@@ -1823,6 +1852,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
   ab.list = reinterpret_cast<int*>(ws + L.blist);
   ab.numy = h->numy;
   ab.nblk = nblk;
+  ab.to = TileOrder{h->numx + 1, h->numy + 1};
   const long long ngrid = (long long)(h->mmax + 1) * 2 * (long long)h->pitch_f;   // entries of D and of E
   auto run = [&](auto tag) -> int {
     // the binning kernel zeroes D and E; without particles they are cleared here
@@ -1880,7 +1910,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
         const int run = 4;
         const long long nrun = (n + run - 1) / run;
         const int grid = (int)std::min<long long>((nrun + 127) / 128, 8LL * resident_grid(kern, 128, 0, nrun));
-        kern<<<grid, 128, 0, st>>>(h->numy, h->mmax, n, run, srec, D, E, h->pitch_f);
+        kern<<<grid, 128, 0, st>>>(h->numy, h->numx + 1, h->mmax, n, run, srec, D, E, h->pitch_f);
       };
       if (h->mmax <= 2) dep(std::integral_constant<int, 2>{});
       else if (h->mmax <= 4) dep(std::integral_constant<int, 4>{});
@@ -1927,7 +1957,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
       if (!err) XT_CUDA(cudaGetSymbolAddress((void**)&err, g_cyl_err));
       const int grid = std::min(nblk, sm_count());
       kern<<<grid, kFieldThreads, P.smem, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax, h->norder,
-                                                h->nnode, ab.list, P.mg, P.nstage, P.stage_hi, P.stage, P.cf,
+                                                h->nnode, ab.to, ab.list, P.mg, P.nstage, P.stage_hi, P.stage, P.cf,
                                                 reinterpret_cast<FT*>(field), err);
     } else {
       // row loads: one block per node block of the tiled tables, 224 threads
@@ -1942,7 +1972,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
         XT_CUDA(cudaFuncSetAttribute(k_cyl_field2<FT, F64, RB, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm));
       k_cyl_field2<FT, F64, RB, NT, MINB><<<nblk, NT, sm, st>>>(h->tile_hi, h->tile_lo, cos_src, sin_src, h->mmax,
-                                                                h->norder, h->nnode, ab.list,
+                                                                h->norder, h->nnode, ab.to, ab.list,
                                                                 reinterpret_cast<FT*>(field));
     }
     XT_CHECK_LAUNCH(bulk ? "k_cyl_field_bulk" : "k_cyl_field2");
