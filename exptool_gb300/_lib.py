@@ -84,6 +84,7 @@ _SIGS = {
     "xt_timing_enable": (c_int, [c_int]),
     "xt_cyl_field_engine": (c_int, [c_int]),
     "xt_cyl_status": (c_int, []),
+    "xt_df_eval": (c_int, [c_int, c_vp, c_vp, c_ll, c_vp]),
     "xt_cyl_active_blocks": (c_int, [c_vp, c_vp, c_ll, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     "xt_timing_read": (c_int, [c_dp, c_int]),
     "xt_fields_forces": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp,

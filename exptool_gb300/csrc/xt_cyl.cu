@@ -13,6 +13,7 @@
 // reads 4 corners x (mmax+1) x 6 values instead of 4 x 6 x (mmax+1) x norder.
 #include <algorithm>
 #include <cstdlib>
+#include <cmath>
 #include <mutex>
 #include <cstring>
 #include <type_traits>
@@ -455,6 +456,131 @@ __device__ __forceinline__ void df_cell(df X, int nmax_cells, float& f, df& off)
   off = df_sub(X, {t, 0.f});
 }
 
+// Table-driven double-float log (Tang, "Table-driven implementation of the
+// logarithm function in IEEE floating-point arithmetic", ACM TOMS 1990):
+// entry j + 32 (j = -32..64) holds log c_j and 1 / c_j as float pairs for
+// c_j = 1 + j / 128, filled on the host from FP64 values (upload_log_table).
+constexpr int kLogTabLo = -32, kLogTabN = 97;
+static __device__ float4 g_logtab[kLogTabN];
+
+// log c_j + log1p(d / c_j) for |d / c_j| <= 2^-8 (d exact as a pair):
+// log1p(u) = u - u^2/2 + u^3/3 in double-float and - u^4/4 + u^5/5 - u^6/6 +
+// u^7/7 in FP32 (below 2^-34, the first omitted term below 2^-66).
+__device__ __forceinline__ df df_log_core(int j, df d) {
+  const float4 tb = __ldg(&g_logtab[j - kLogTabLo]);
+  const df u = df_mul(d, df{tb.z, tb.w});
+  const df u2 = df_mul(u, u);
+  const df u3 = df_mul(u2, u);
+  const float uh = u.h;
+  const float tail = u2.h * u2.h * (-0.25f + uh * (0.2f - uh * (0.16666667f - uh * 0.14285715f)));
+  const df third = {0x1.555556p-2f, -0x1.555556p-27f};
+  df s = df_add(u, df{-0.5f * u2.h, -0.5f * u2.l});
+  s = df_add(s, df_mul(u3, third));
+  s.l += tail;
+  return df_add(df{tb.x, tb.y}, s);
+}
+
+// log t for 2^-125 < t < 2^126: t = 2^k f with f in [0.75, 1.5) (so that t
+// near 1 keeps k = 0: no cancellation of k ln 2 against log c), c = c_j the
+// nearest table point, f - c exact (Sterbenz), log t = k ln 2 + log c +
+// log1p((f - c) / c).  About 2^-47 relative.
+__device__ __forceinline__ df df_log_tab(df t) {
+  const int eb = (__float_as_int(t.h) >> 23) & 0xff;   // t.h = 1.m 2^(eb - 127), normal
+  int k = eb - 127;
+  const float sc = __int_as_float((254 - eb) << 23);   // 2^-k, exact
+  df f = {t.h * sc, t.l * sc};                         // [1, 2)
+  if (f.h >= 1.5f) {
+    f = {0.5f * f.h, 0.5f * f.l};
+    ++k;
+  }
+  int j = __float2int_rn((f.h - 1.f) * 128.f);
+  j = min(max(j, kLogTabLo), kLogTabLo + kLogTabN - 1);
+  const float c = __fmaf_rn((float)j, 0.0078125f, 1.f);   // 1 + j/128, exact
+  df r = df_log_core(j, fast_two_sum(f.h - c, f.l));
+  if (k != 0) r = df_add(df_scale(kDfLn2, (float)k), r);
+  return r;
+}
+
+// log(1 + w) for -0.25 <= w < 0.5 without forming 1 + w: j = round(128 w),
+// w - j/128 exact (Sterbenz for j != 0), log1p(w) = log c_j +
+// log1p((w - j/128) / c_j).  About 2^-47 relative.
+__device__ __forceinline__ df df_log1p_tab(df w) {
+  int j = __float2int_rn(w.h * 128.f);
+  j = min(max(j, kLogTabLo), kLogTabLo + kLogTabN - 1);
+  return df_log_core(j, fast_two_sum(w.h - (float)j * 0.0078125f, w.l));
+}
+
+// asinh a for 0 <= a < 2^100: the series a (1 - a^2/6 + 3a^4/40 - 5a^6/112 +
+// 35a^8/1152 - 63a^10/2816) below 1/16 (terms from a^6 in FP32, the first
+// omitted below 2^-53); log1p(a + a^2 / (1 + sqrt(1 + a^2))) below 0.4 (w <
+// 0.48: no rounding of 1 + w, which would cost up to 2^-44 relative near
+// 1/16); log(a + sqrt(1 + a^2)) up to 2^24 (the result is above 0.39); log 2a
+// above (the omitted 1/(4a^2) below 2^-50).
+__device__ __forceinline__ df df_asinh_tab(df a) {
+  const df one = {1.f, 0.f};
+  if (a.h < 0.0625f) {
+    const df a2 = df_mul(a, a);
+    const float x = a2.h;
+    const float tail = x * x * x * (-0.044642857f + x * (0.030381944f - x * 0.022372159f));
+    const df sixth = {0x1.555556p-3f, -0x1.555556p-28f};
+    const df c340 = {0x1.333334p-4f, -0x1.99999ap-29f};   // 3/40
+    df p = df_add(one, df_neg(df_mul(a2, sixth)));
+    p = df_add(p, df_mul(df_mul(a2, a2), c340));
+    p.l += tail;
+    return df_mul(a, p);
+  }
+  if (a.h < 0.4f) {
+    const df a2 = df_mul(a, a);
+    return df_log1p_tab(df_add(a, df_div(a2, df_add(one, df_sqrt(df_add(one, a2))))));
+  }
+  if (a.h < 16777216.f) return df_log_tab(df_add(a, df_sqrt(df_add(one, df_mul(a, a)))));
+  return df_log_tab(df{2.f * a.h, 2.f * a.l});
+}
+
+// z / (|z| + eps) for the z map: +-(1 - delta) with delta = eps / (|z| + eps)
+// in FP32 where delta < 2^-25 (then the pair is normalised and delta's FP32
+// rounding is below 2^-49), the double-float quotient otherwise.
+__device__ __forceinline__ df df_zsign(df z, df eps) {
+  const float az = fabsf(z.h);
+  if (az > eps.h * 33554432.f) {
+    const float delta = __fdiv_rn(eps.h, az + eps.h);
+    return z.h > 0.f ? df{1.f, -delta} : df{-1.f, delta};
+  }
+  return df_div(z, df_add(df_abs(z), eps));
+}
+
+static int upload_log_table() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  XT_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && done[dev]) return XT_OK;
+  float4 tab[kLogTabN];
+  for (int i = 0; i < kLogTabN; ++i) {
+    const double c = 1.0 + (i + kLogTabLo) / 128.0, L = std::log(c), inv = 1.0 / c;
+    const float lh = (float)L, ih = (float)inv;
+    tab[i] = make_float4(lh, (float)(L - (double)lh), ih, (float)(inv - (double)ih));
+  }
+  XT_CUDA(cudaMemcpyToSymbol(g_logtab, tab, sizeof(tab)));
+  if (dev >= 0 && dev < 64) done[dev] = true;
+  return XT_OK;
+}
+
+// The double-float functions of the FP64 binning on n values (diagnostics):
+// fn 0 log x, 1 asinh x (x >= 0), 2 the z map z / (|z| + 1e-8) asinh |z|.
+__global__ void k_df_eval(int fn, const double* __restrict__ in, double* __restrict__ out, long long n) {
+  const df eps = df_from(1.0e-8);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const df x = df_from(in[i]);
+    df r;
+    if (fn == 0) r = df_log_tab(x);
+    else if (fn == 1) r = df_asinh_tab(x);
+    else r = df_mul(df_zsign(x, eps), df_asinh_tab(df_abs(x)));
+    out[i] = df_to(r);
+  }
+}
+
 // Table constants as float pairs, split on the host.
 struct BinrecDf {
   df xmin, idx, ymin, idy, ias, ih, soft, zeps, m4pi;
@@ -499,13 +625,13 @@ __global__ void __launch_bounds__(256) k_cyl_binrec_df(CylTab<double> T, BinrecD
         const df u = df_mul(Rc, ias);
         xi = df_div(df_sub(u, one), df_add(u, one));
       } else if (T.cmap == 2) {
-        xi = df_log(Rc);
+        xi = df_log_tab(Rc);
       } else {
         xi = Rc;
       }
       df_cell(df_mul(df_sub(xi, xmin), idx), T.numx, fx, dx);
-      const df sg = df_div(zd, df_add(df_abs(zd), zeps));
-      const df yv = df_mul(sg, df_asinh(df_mul(df_abs(zd), K.ih)));
+      const df sg = df_zsign(zd, zeps);
+      const df yv = df_mul(sg, df_asinh_tab(df_mul(df_abs(zd), K.ih)));
       df_cell(df_mul(df_sub(yv, ymin), idy), T.numy, fy, dy);
       if (Rout) Rout[p] = df_to_int(Rc);
     } else {
@@ -1392,6 +1518,7 @@ int xt_cyl_table_create(int mmax, int norder, int numx, int numy, int cmap, int 
   XT_REQUIRE(dX != 0.0 && dY != 0.0, "degenerate table spacing");
   XT_REQUIRE(potC && potS, "NULL potential table");
   XT_REQUIRE(!dens || (densC && densS), "density tables required when dens != 0");
+  if (int rc = upload_log_table()) return rc;   // the binning's log table
   CylHandle* h = new CylHandle();
   h->mmax = mmax; h->norder = norder; h->numx = numx; h->numy = numy; h->cmap = cmap; h->dens = dens ? 1 : 0;
   h->XMIN = XMIN; h->dX = dX; h->YMIN = YMIN; h->dY = dY; h->ascale = ascale; h->hscale = hscale;
@@ -1651,6 +1778,17 @@ int xt_cyl_active_blocks(void* handle, const void* workspace, long long n, int p
   XT_CUDA(cudaDeviceSynchronize());
   XT_CUDA(cudaMemcpy(active, static_cast<const char*>(workspace) + L.blist, sizeof(int), cudaMemcpyDeviceToHost));
   *total = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
+  return XT_OK;
+}
+
+int xt_df_eval(int fn, const double* in, double* out, long long n, void* stream) {
+  XT_REQUIRE(fn >= 0 && fn <= 2, "function must be 0, 1 or 2, got %d", fn);
+  XT_REQUIRE(n >= 0 && (n == 0 || (in && out)), "bad arrays");
+  if (int rc = upload_log_table()) return rc;
+  if (n == 0) return XT_OK;
+  cudaStream_t st = as_stream(stream);
+  k_df_eval<<<resident_grid(k_df_eval, 256, 0, n), 256, 0, st>>>(fn, in, out, n);
+  XT_CHECK_LAUNCH("k_df_eval");
   return XT_OK;
 }
 

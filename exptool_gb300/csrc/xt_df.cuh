@@ -165,58 +165,9 @@ __device__ __forceinline__ df df_split(double v, bool& ok) {
   return {hi, lo};
 }
 
-// 1/(2j+1) for j = 0..11 and ln 2 as float pairs (hi = float rounding of the
-// value, lo = float rounding of the remainder).
-static __constant__ df kDfInvOdd[12] = {
-    {0x1.0p+0f, 0x0.0p+0f},
-    {0x1.555556p-2f, -0x1.555556p-27f},
-    {0x1.99999ap-3f, -0x1.99999ap-29f},
-    {0x1.24924ap-3f, -0x1.b6db6ep-28f},
-    {0x1.c71c72p-4f, -0x1.c71c72p-31f},
-    {0x1.745d18p-4f, -0x1.745d18p-29f},
-    {0x1.3b13b2p-4f, -0x1.89d89ep-29f},
-    {0x1.111112p-4f, -0x1.dddddep-29f},
-    {0x1.e1e1e2p-5f, -0x1.e1e1e2p-33f},
-    {0x1.af286cp-5f, -0x1.af286cp-32f},
-    {0x1.861862p-5f, -0x1.e79e7ap-31f},
-    {0x1.642c86p-5f, -0x1.bd37a8p-31f},
-};
+// ln 2 as a float pair (hi = float rounding of the value, lo = float rounding
+// of the remainder).
 static __constant__ df kDfLn2 = {0x1.62e430p-1f, -0x1.05c610p-29f};
-
-// log from the series log f = 2 atanh(s), s = (f - 1)/(f + 1) = 2 (s + s^3/3 + ...),
-// 12 terms (|s| <= 0.2 after range reduction: s^24/25 < 1e-18).
-__device__ __forceinline__ df df_log_series(df s, int k) {
-  const df s2 = df_mul(s, s);
-  df p = kDfInvOdd[11];
-#pragma unroll
-  for (int j = 10; j >= 0; --j) p = df_add(df_mul(p, s2), kDfInvOdd[j]);
-  const df lf = df_scale(df_mul(s, p), 2.f);
-  return df_add(df_scale(kDfLn2, (float)k), lf);
-}
-
-// Natural log of t > 0 (normal float range): t = 2^k f with f in [0.75, 1.5).
-__device__ __forceinline__ df df_log(df t) {
-  int e;
-  const float m = frexpf(t.h, &e);                  // t.h = m 2^e, m in [0.5, 1)
-  const int k = (m < 0.75f) ? e - 1 : e;
-  const float sc = __int_as_float((127 - k) << 23);  // 2^-k, exact scaling
-  const df f = {t.h * sc, t.l * sc};
-  const df one = {1.f, 0.f};
-  return df_log_series(df_div(df_sub(f, one), df_add(f, one)), k);
-}
-
-// log(1 + w) for w >= 0 keeping the relative accuracy of small w.
-__device__ __forceinline__ df df_log1p(df w) {
-  if (w.h < 0.5f) return df_log_series(df_div(w, df_add(w, {2.f, 0.f})), 0);
-  return df_log(df_add(w, {1.f, 0.f}));
-}
-
-// asinh(a) = log1p(a + a^2 / (1 + sqrt(1 + a^2))) for a >= 0.
-__device__ __forceinline__ df df_asinh(df a) {
-  const df a2 = df_mul(a, a);
-  const df one = {1.f, 0.f};
-  return df_log1p(df_add(a, df_div(a2, df_add(one, df_sqrt(df_add(one, a2))))));
-}
 
 // Exact float -> double conversion with integer operations, keeping the FP64
 // pipe free (every float: zero, normal, infinity and NaN by bit manipulation,

@@ -258,6 +258,14 @@ int xt_cyl_status(void);
  * Diagnostics, no counterpart in the reference. */
 int xt_cyl_active_blocks(void *handle, const void *workspace, long long n, int precision, int *active, int *total);
 
+/* The double-float functions of the FP64 binning on n device values, each
+ * input rounded to a float pair and each result widened to FP64 (diagnostics,
+ * for accuracy tests; no counterpart in the reference): fn 0 log x
+ * (2^-125 < x < 2^126), 1 asinh x (0 <= x < 2^100), 2 the z map of
+ * compatibility.z_to_y at hscale = 1, z / (|z| + 1e-8) asinh |z|
+ * (compatibility.py:83-91). */
+int xt_df_eval(int fn, const double *in, double *out, long long n, void *stream);
+
 /* Stage timing (diagnostics, no counterpart in the reference): with
  * xt_timing_enable(1), xt_cyl_accumulate_eval records CUDA events on its
  * stream between its stages; xt_timing_read waits for the last one and writes
