@@ -1327,18 +1327,37 @@ __global__ void __launch_bounds__(128, 5) k_cyl_eval_sorted_df(CylTab<double> T,
     const df w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
     const df c1 = r.c1, s1 = r.s1, c2 = df_scale(c1, 2.f);   // c2: exact
     // bilinear interpolation of the six fields of order m (lazy df sums, read
-    // unnormalised by the products that follow)
+    // unnormalised by the products that follow).  A corner's six fields of
+    // one m are 48 contiguous bytes at a 16-byte boundary (nodes 336 bytes
+    // apart): three 16-byte loads, taken corner by corner.
+    auto ld6 = [](const df* p, df f[6]) {
+      const float4* q = reinterpret_cast<const float4*>(p);
+      const float4 a = q[0], b = q[1], c = q[2];
+      f[0] = {a.x, a.y};
+      f[1] = {a.z, a.w};
+      f[2] = {b.x, b.y};
+      f[3] = {b.z, b.w};
+      f[4] = {c.x, c.y};
+      f[5] = {c.z, c.w};
+    };
     auto interp = [&](int m, df v[6]) {
       const int b = m * 6;
+      dacc a[6];
+      df f[6];
+      ld6(f00 + b, f);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        dacc a;
-        a.set(f00[b + k], w0);
-        a.fma(f10[b + k], w1);
-        a.fma(f01[b + k], w2);
-        a.fma(f11[b + k], w3);
-        v[k] = a.raw();
-      }
+      for (int k = 0; k < 6; ++k) a[k].set(f[k], w0);
+      ld6(f10 + b, f);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a[k].fma(f[k], w1);
+      ld6(f01 + b, f);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a[k].fma(f[k], w2);
+      ld6(f11 + b, f);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a[k].fma(f[k], w3);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) v[k] = a[k].raw();
     };
     df p0{0.f, 0.f};
     dacc p, fr, fp, fz;
