@@ -757,16 +757,37 @@ __global__ void __launch_bounds__(kScanTile) k_scan_add(int* __restrict__ off, c
 }
 
 // Counting-sort scatter: record p moves to off[cell] + its slot, carrying p.
+// A thread takes kScatterUnroll records a grid stride apart at a time, so
+// that their loads, the dependent offset loads and the scattered stores of
+// several records are in flight together.
+constexpr int kScatterUnroll = 4;
+
 template <typename RT>
 __global__ void __launch_bounds__(256) k_cyl_scatter(long long n, const int* __restrict__ off,
                                                      const BinRec<RT>* __restrict__ rec,
                                                      BinRec<RT>* __restrict__ srec) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-       p += (long long)gridDim.x * blockDim.x) {
-    BinRec<RT> r = rec[p];
-    const long long q = (long long)off[r.cell] + r.idx;
-    r.idx = (int)p;
-    srec[q] = r;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; p0 < n; p0 += kScatterUnroll * stride) {
+    BinRec<RT> r[kScatterUnroll];
+    long long q[kScatterUnroll];
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u) {
+      const long long p = p0 + u * stride;
+      if (p < n) r[u] = rec[p];
+    }
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u) {
+      const long long p = p0 + u * stride;
+      if (p < n) q[u] = (long long)off[r[u].cell] + r[u].idx;
+    }
+#pragma unroll
+    for (int u = 0; u < kScatterUnroll; ++u) {
+      const long long p = p0 + u * stride;
+      if (p < n) {
+        r[u].idx = (int)p;
+        srec[q[u]] = r[u];
+      }
+    }
   }
 }
 
