@@ -45,14 +45,14 @@ L2_BYTES = 129 * 1024 * 1024
 # workload, from an ncu --set full capture of `bench.py --profile`, and what
 # bounds the stage there
 STAGE_TRAFFIC_F64 = {
-    "k_cyl_binrec": (32_234_240 + 9_280_256, "FP32-pipe bound (double-float set-up): FMA pipe 45 %, IPC 2.8 / SM"),
-    "k_cyl_scatter": (55_212_544 + 9_271_296, "scattered 16-byte record stores: LSU throttle"),
-    "k_cyl_deposit_sorted": (52_031_232 + 12_800, "issue bound: 128 registers, IPC 2.4 / SM, FMA pipe 37 %"),
-    "k_cyl_contract_partial+final": (42_887_680 + 11_008,
-                                     "HBM latency: 34 % of peak DRAM throughput (listed node blocks only)"),
-    "k_cyl_field": (116_457_728 + 4_438_528,
-                    "bulk-copy pipeline, HBM and issue: 50 % of peak DRAM throughput, IPC 2.8 / SM"),
-    "k_cyl_eval_sorted": (89_828_352 + 36_101_376,
+    "k_cyl_binrec": (32_230_656 + 9_383_424, "FP32-pipe bound (double-float set-up): FMA pipe 45 %, IPC 2.8 / SM"),
+    "k_cyl_scatter": (55_190_528 + 9_678_848, "scattered 16-byte record stores: LSU throttle"),
+    "k_cyl_deposit_sorted": (52_030_720 + 7_936, "issue bound: 128 registers, IPC 2.4 / SM, FMA pipe 37 %"),
+    "k_cyl_contract_partial+final": (42_886_656 + 13_568,
+                                     "HBM latency: 33 % of peak DRAM throughput (listed node blocks only)"),
+    "k_cyl_field": (116_463_360 + 4_372_736,
+                    "bulk-copy pipeline, HBM and issue: 50 % of peak DRAM throughput, IPC 2.9 / SM"),
+    "k_cyl_eval_sorted": (89_737_728 + 36_027_392,
                           "FP32-pipe bound (double-float arithmetic): FMA pipe 57 %, IPC 2.6 / SM"),
 }
 
@@ -61,8 +61,8 @@ STAGE_TRAFFIC_F64 = {
 # fused stage, from the same ncu capture: the double-float stages are bound by
 # FP32 issue, so the HBM fraction alone understates how busy they are
 STAGE_PIPE_F64 = {
-    "k_cyl_binrec": (45.2, 2.8), "k_cyl_scatter": (1.4, 0.13), "k_cyl_deposit_sorted": (36.8, 2.4),
-    "k_cyl_contract_partial+final": (32.8, 2.3), "k_cyl_field": (39.7, 2.8), "k_cyl_eval_sorted": (57.1, 2.6),
+    "k_cyl_binrec": (44.9, 2.8), "k_cyl_scatter": (1.5, 0.14), "k_cyl_deposit_sorted": (36.9, 2.4),
+    "k_cyl_contract_partial+final": (32.5, 2.2), "k_cyl_field": (40.2, 2.9), "k_cyl_eval_sorted": (57.1, 2.6),
 }
 
 
