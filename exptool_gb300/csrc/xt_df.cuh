@@ -35,6 +35,16 @@ __device__ __forceinline__ df fast_two_sum(float a, float b) {
   return {s, e};
 }
 
+// a + b exactly as a pair (Knuth's TwoSum).
+__device__ __forceinline__ df df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
+}
+
+// a > b for normalised pairs
+__device__ __forceinline__ bool df_gt(df a, df b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+
 __device__ __forceinline__ df df_add(df a, df b) {
   const float s = __fadd_rn(a.h, b.h);
   const float v = __fsub_rn(s, a.h);

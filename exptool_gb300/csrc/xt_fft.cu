@@ -43,8 +43,6 @@ __device__ __forceinline__ cdf c_ld(const float4* p) {
 }
 __device__ __forceinline__ void c_st(float4* p, cdf a) { *p = make_float4(a.re.h, a.re.l, a.im.h, a.im.l); }
 
-// df comparison a > b (both normalised)
-__device__ __forceinline__ bool df_gt(df a, df b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
 __device__ __forceinline__ df df_absv(df a) { return a.h < 0.f ? df_neg(a) : a; }
 
 // exp(-2 pi i t / m) for 0 <= t < m from the half table tw[t] (t < m / 2):

@@ -2,6 +2,8 @@
 // per precision in xt_orbit_k64.cu / xt_orbit_k32.cu.
 #pragma once
 
+#include <type_traits>
+
 #include "xt_df.cuh"
 #include "xt_launch.cuh"
 
@@ -83,11 +85,118 @@ __device__ __forceinline__ void traj_row(double* traj, long long p, int nint, in
   for (int i = 0; i < 10; ++i) t[i] = q[i];
 }
 
+// One orbit of the FP32-force leapfrog with its state (position, velocity,
+// forces, potential, squared radii, energies) in double-float on the FP32
+// pipe: GB300 issues two FP64 FMAs per clock per SM against 128 FP32, and the
+// FP64 kick/drift of about 50 FP64 operations per step bound the FP32-force
+// step.  The same steps as the FP64 state below (integrate.py:116-160), with
+// sums of the two FP32 force parts exact (TwoSum) and positions rounded to
+// FP32 for the force evaluation.  The state is read and written as FP64
+// (split and widened by integer operations).
+template <int LCAP>
+__device__ __forceinline__ void leapfrog_orbit_df(const SphTab<float>& ST, const float* __restrict__ GH,
+                                                  const CylTab<float>& CT, const float* __restrict__ F,
+                                                  const FieldOpts& fo, const OrbitArgs& A, long long p) {
+  df x = df_split_or_from(A.s[S_X][p]), y = df_split_or_from(A.s[S_Y][p]), z = df_split_or_from(A.s[S_Z][p]);
+  df vx = df_split_or_from(A.s[S_VX][p]), vy = df_split_or_from(A.s[S_VY][p]),
+     vz = df_split_or_from(A.s[S_VZ][p]);
+  df fx, fy, fz, pot, r2m1, r2m2, e0, edev;
+  float aps;
+  int nstep;
+  float v[8];
+  auto posf = [](df a) { return __fadd_rn(a.h, a.l); };
+  auto energy = [&]() {
+    const df k2 = df_add(df_add(df_mul(vx, vx), df_mul(vy, vy)), df_mul(vz, vz));
+    return df_add(df{0.5f * k2.h, 0.5f * k2.l}, pot);
+  };
+  auto row = [&](int k) {
+    const double q[10] = {df_to_int(x),  df_to_int(y),   df_to_int(z),  df_to_int(vx), df_to_int(vy),
+                          df_to_int(vz), df_to_int(pot), df_to_int(fx), df_to_int(fy), df_to_int(fz)};
+    traj_row(A.traj, p, A.nint, k, q);
+  };
+  if (A.step0 == 0) {
+    fields_point<float, LCAP>(ST, GH, CT, F, fo, posf(x), posf(y), posf(z), 1.f, 0.f, v);
+    fx = df_two_sum(v[0], v[1]);
+    fy = df_two_sum(v[2], v[3]);
+    fz = df_two_sum(v[4], v[5]);
+    pot = df_two_sum(v[6], v[7]);
+    r2m1 = df_add(df_mul(x, x), df_mul(y, y));
+    r2m2 = {0.f, 0.f};
+    aps = 0.f;
+    nstep = 1;
+    e0 = energy();
+    edev = {0.f, 0.f};
+    if (A.traj) row(0);
+  } else {
+    fx = df_split_or_from(A.s[S_FX][p]);
+    fy = df_split_or_from(A.s[S_FY][p]);
+    fz = df_split_or_from(A.s[S_FZ][p]);
+    pot = df_split_or_from(A.s[S_POT][p]);
+    r2m1 = df_split_or_from(A.s[S_R2M1][p]);
+    r2m2 = df_split_or_from(A.s[S_R2M2][p]);
+    aps = (float)A.s[S_APS][p];
+    nstep = (int)A.s[S_NSTEP][p];
+    e0 = df_split_or_from(A.s[S_E0][p]);
+    edev = df_split_or_from(A.s[S_EDEV][p]);
+  }
+  const double dtv = A.dts ? A.dts[p] : A.dt;
+  const df dt = df_split_or_from(dtv), hdt = {0.5f * dt.h, 0.5f * dt.l};
+  const df hdt2 = df_mul(hdt, dt);   // dt^2 / 2
+  const float apmax = (float)A.ap_max;
+  const int kbeg = A.step0 < 1 ? 1 : A.step0;
+  int kend = A.step0 + A.nsteps;
+  if (kend > A.nint) kend = A.nint;
+  for (int k = kbeg; k < kend; ++k) {
+    if (!(aps < apmax)) break;   // integrate.py:126 loop condition
+    if (nstep != k) break;       // orbit already stopped
+    x = df_add(df_add(x, df_mul(vx, dt)), df_mul(fx, hdt2));
+    y = df_add(df_add(y, df_mul(vy, dt)), df_mul(fy, hdt2));
+    z = df_add(df_add(z, df_mul(vz, dt)), df_mul(fz, hdt2));
+    float srd = 0.f, crd = 1.f;
+    if (A.rotc != 0.0) {
+      double sd, cd;
+      sincos(A.rotc * ((double)k * dtv), &sd, &cd);
+      srd = (float)sd;
+      crd = (float)cd;
+    }
+    fields_point<float, LCAP>(ST, GH, CT, F, fo, posf(x), posf(y), posf(z), crd, srd, v);
+    const df nfx = df_two_sum(v[0], v[1]), nfy = df_two_sum(v[2], v[3]), nfz = df_two_sum(v[4], v[5]);
+    pot = df_two_sum(v[6], v[7]);
+    vx = df_add(vx, df_mul(df_add(fx, nfx), hdt));
+    vy = df_add(vy, df_mul(df_add(fy, nfy), hdt));
+    vz = df_add(vz, df_mul(df_add(fz, nfz), hdt));
+    fx = nfx;
+    fy = nfy;
+    fz = nfz;
+    const df r2now = df_add(df_mul(x, x), df_mul(y, y));
+    if (A.apse && k > 1 && df_gt(r2m1, r2m2) && df_gt(r2m1, r2now)) aps += 1.f;
+    r2m2 = r2m1;
+    r2m1 = r2now;
+    nstep = k + 1;
+    df de = df_sub(energy(), e0);
+    if (de.h < 0.f) de = df_neg(de);
+    if (df_gt(de, edev)) edev = de;
+    if (A.traj) row(k);
+  }
+  A.s[S_X][p] = df_to_int(x); A.s[S_Y][p] = df_to_int(y); A.s[S_Z][p] = df_to_int(z);
+  A.s[S_VX][p] = df_to_int(vx); A.s[S_VY][p] = df_to_int(vy); A.s[S_VZ][p] = df_to_int(vz);
+  A.s[S_FX][p] = df_to_int(fx); A.s[S_FY][p] = df_to_int(fy); A.s[S_FZ][p] = df_to_int(fz);
+  A.s[S_POT][p] = df_to_int(pot);
+  A.s[S_R2M1][p] = df_to_int(r2m1); A.s[S_R2M2][p] = df_to_int(r2m2);
+  A.s[S_APS][p] = (double)aps;
+  A.s[S_NSTEP][p] = (double)nstep;
+  A.s[S_E0][p] = df_to_int(e0); A.s[S_EDEV][p] = df_to_int(edev);
+}
+
 template <typename R, int LCAP>
 __global__ void __launch_bounds__(128, 4) k_leapfrog(SphTab<R> ST, const R* __restrict__ GH, CylTab<R> CT,
                                                   const R* __restrict__ F, FieldOpts fo, OrbitArgs A) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < A.n;
        p += (long long)gridDim.x * blockDim.x) {
+    if constexpr (std::is_same<R, float>::value) {
+      leapfrog_orbit_df<LCAP>(ST, GH, CT, F, fo, A, p);
+      continue;
+    }
     double x = A.s[S_X][p], y = A.s[S_Y][p], z = A.s[S_Z][p];
     double vx = A.s[S_VX][p], vy = A.s[S_VY][p], vz = A.s[S_VZ][p];
     double fx, fy, fz, pot, r2m1, r2m2, aps, e0, edev;
