@@ -906,7 +906,8 @@ def orbit_extra(eof_path, cos_d, sin_d, sph_cache, sph_model, sph_table, hx, hy,
                 dt=0.002):
     """Orbit ensemble in the frozen halo + disc field: n disc orbits (seed 2),
     v_phi = v_c(R) from the field, 10 % Gaussian dispersion, velocity Verlet
-    dt = 0.002 for nint steps, FP32 forces / FP64 kick-drift, CUDA-graph replay."""
+    dt = 0.002 for nint steps, FP32 forces with the orbit state in double-float,
+    CUDA-graph replay."""
     import torch
     from exptool_gb300.basis import eof, potential, spheresl
     from exptool_gb300.tables.samplers import disc_cylindrical
@@ -950,7 +951,7 @@ def orbit_extra(eof_path, cos_d, sin_d, sph_cache, sph_model, sph_table, hx, hy,
     dphi = st[15] / np.abs(pot0)
     q = lambda a, f: float(np.quantile(a, f))
     return {"workload": "1e6 disc orbits in frozen halo(SL lmax4)+disc(EOF m6 n18) field, dt=0.002, 2000 steps, "
-                        "FP32 force / FP64 kick-drift, CUDA graph",
+                        "FP32 force / double-float kick-drift, CUDA graph",
             "ms_per_run": ms, "orbit_steps_per_s": n * (nint - 1) / (ms * 1e-3),
             "launches_per_run": ens.launches_per_run(),
             "energy_drift": "per orbit max over the 2000 steps of |E(t) - E0|; target 1e-4 judged on the median "

@@ -234,19 +234,20 @@ def compute_coefficients_and_forces(PSPInput, eof_file, verbose=1, m1=0, m2=1000
     # are used in place.  Particle arrays in page-locked host memory are read by the binning
     # kernel in place (the host -> device traffic overlaps its work); other
     # inputs are copied to the device first.  R is written by the binning
-    # kernel straight into page-locked host memory; the coefficients and the
-    # other five results are computed into reused device blocks and leave in
-    # two copies issued by one library call, with one synchronisation.  Particles with a NaN
-    # coordinate are placed at the origin on the device.
+    # kernel straight into page-locked host memory; the other five results
+    # are evaluated one part of the particles at a time and each part is
+    # copied into page-locked host memory while the next is evaluated; the
+    # coefficients follow in one copy, with one synchronisation.  Particles
+    # with a NaN coordinate are placed at the origin on the device.
     # one page-locked block holds the coefficients, p0 p fr fp fz and R; the
     # returned arrays are views of it
     nc = (table.mmax + 1) * table.norder
     blk = torch.empty(2 * nc + 6 * n, dtype=torch.float64, pin_memory=True)
     base = blk.data_ptr()
-    coef, res = table.accumulate_eval_blocks(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision,
-                                             m1=m1, m2=m2, nan_to_origin=not nanblock,
-                                             r_out=base + 8 * (2 * nc + 5 * n))
-    dev.copy_and_sync([(base, coef.data_ptr(), 16 * nc), (base + 16 * nc, res.data_ptr(), 40 * n)])
+    coef, _ = table.accumulate_eval_blocks(*(dev.kernel_input(a) for a in (x, y, z, m)), precision=precision,
+                                           m1=m1, m2=m2, nan_to_origin=not nanblock,
+                                           r_out=base + 8 * (2 * nc + 5 * n), res_out=base + 16 * nc)
+    dev.copy_and_sync([(base, coef.data_ptr(), 16 * nc)])
     h = blk.numpy()
     host = [h[:nc].reshape(table.mmax + 1, table.norder), h[nc:2 * nc].reshape(table.mmax + 1, table.norder)]
     host += [h[2 * nc + k * n:2 * nc + (k + 1) * n] for k in range(6)]

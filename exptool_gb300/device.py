@@ -394,15 +394,20 @@ class CylTable:
                                                   ctypes.byref(a), ctypes.byref(t)), "xt_cyl_active_blocks")
         return a.value, t.value
 
-    def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True, r_out=None):
+    def accumulate_eval_blocks(self, x, y, z, m, precision="f64", m1=0, m2=1000, nan_to_origin=True, r_out=None,
+                               res_out=None):
         """accumulate_eval into per-thread buffers kept for the last particle
         count and precision: returns the (2, mmax+1, norder) coefficient block
         (cos, sin) and the (5, n) block of p0, p, fr, fp, fz.  The next call on
         this thread with the same size overwrites both, so callers copy them
         out first.  R goes to ``r_out`` (a length-n float64 tensor or a raw
         address, device or page-locked host memory; the binning kernel writes
-        it directly).  The call's C arguments are kept with the buffers, so a
-        repeated call only sets the particle and R addresses."""
+        it directly).  With ``res_out`` (the address of 5 n page-locked
+        float64) p0 p fr fp fz go there instead, each part of the particles
+        copied out while the next is evaluated, and the second value returned
+        is None; the copies are complete when the stream's work is.  The call's
+        C arguments are kept with the buffers, so a repeated call only sets the
+        particle and result addresses."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
         key = (n, pc)
@@ -416,13 +421,15 @@ class CylTable:
             b = (key, ws, coef, res, outs)
             self._fused_bufs.v = b
         _, ws, coef, res, outs = b
+        for k in range(5):
+            outs[k] = (res_out + 8 * n * k) if res_out is not None else res.data_ptr() + 8 * n * k
         outs[5] = _addr(r_out) if r_out is not None else res.data_ptr() + 40 * n
         cos_p = coef.data_ptr()
         _lib.check(self._lib.xt_cyl_accumulate_eval(self.handle, _addr(x), _addr(y), _addr(z), _addr(m), n, pc,
                                                     int(m1), int(m2), int(bool(nan_to_origin)), cos_p,
                                                     cos_p + 8 * (self.mmax + 1) * self.norder, outs, ws.data_ptr(),
                                                     ws.numel(), stream_ptr()), "xt_cyl_accumulate_eval")
-        return coef, res[:5]
+        return coef, (None if res_out is not None else res[:5])
 
     def sorted_ok(self):
         """Whether the table fits the sorted pipeline (mmax <= 8, norder <= 24,
