@@ -459,18 +459,25 @@ class CylTable:
                    "xt_cyl_accumulate_sorted")
         return coef
 
-    def eval_sorted(self, x, y, z, cos, sin, precision="f64", m1=0, m2=1000, r_out=None):
+    def eval_sorted(self, x, y, z, cos, sin, precision="f64", m1=0, m2=1000, r_out=None, res_out=None):
         """accumulated_eval_particles (no density) through the sorted pipeline
         from device coefficients cos, sin ((mmax+1, norder) float64): a (6, n)
         device tensor of p0, p, fr, fp, fz, R in particle order.  With
         ``r_out`` (a length-n float64 tensor or a raw address, device or
         page-locked host memory) R is written there by the binning kernel
-        instead of into row 5."""
+        instead of into row 5.  With ``res_out`` (the address of 5 n
+        page-locked float64) p0 p fr fp fz go there, half of the particles at a
+        time behind the evaluation, and None is returned; they are complete
+        when the stream's work is."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
         ws = self._sorted_workspace(n, pc)
-        res = torch.empty((6, n), dtype=torch.float64, device=device())
-        outs = (ctypes.c_void_p * 6)(*[res.data_ptr() + 8 * n * k for k in range(6)])
+        res = None
+        if res_out is None:
+            res = torch.empty((6, n), dtype=torch.float64, device=device())
+            outs = (ctypes.c_void_p * 6)(*[res.data_ptr() + 8 * n * k for k in range(6)])
+        else:
+            outs = (ctypes.c_void_p * 6)(*[res_out + 8 * n * k for k in range(5)], None)
         if r_out is not None:
             outs[5] = _addr(r_out)
         _lib.check(self._lib.xt_cyl_eval_sorted(self.handle, _addr(x), _addr(y), _addr(z), n, pc, int(m1), int(m2),
