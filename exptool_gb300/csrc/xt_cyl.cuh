@@ -5,6 +5,8 @@
 // accumulated_eval_particles :989-1144).
 #pragma once
 
+#include <type_traits>
+
 #include "xt_common.cuh"
 
 namespace xt {
@@ -90,10 +92,16 @@ __device__ __forceinline__ void cyl_eval_bins(const CylTab<R>& T, const R* __res
     if (!use) continue;
     const int b = m * o.nf;
     R v[8];
+    // fields in pairs: nf is 6 or 8 and nodes are (mmax+1) nf values apart, so
+    // every pair starts at a multiple of two values (one 8- or 16-byte load)
+    using R2 = typename std::conditional<std::is_same<R, float>::value, float2, double2>::type;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 8; k += 2) {
       if (k >= o.nf) break;
-      v[k] = f00[b + k] * B.c00 + f10[b + k] * B.c10 + f01[b + k] * B.c01 + f11[b + k] * B.c11;
+      const R2 g00 = *reinterpret_cast<const R2*>(f00 + b + k), g10 = *reinterpret_cast<const R2*>(f10 + b + k);
+      const R2 g01 = *reinterpret_cast<const R2*>(f01 + b + k), g11 = *reinterpret_cast<const R2*>(f11 + b + k);
+      v[k] = g00.x * B.c00 + g10.x * B.c10 + g01.x * B.c01 + g11.x * B.c11;
+      v[k + 1] = g00.y * B.c00 + g10.y * B.c10 + g01.y * B.c01 + g11.y * B.c11;
     }
     const R pm = c * v[0] + s * v[3];
     const R frm = c * v[1] + s * v[4];
