@@ -76,7 +76,7 @@ __device__ __forceinline__ void cyl_eval_bins(const CylTab<R>& T, const R* __res
   R p0 = 0, p = 0, fr = 0, fp = 0, fz = 0, d0 = 0, d = 0, fr0 = 0, fz0 = 0;
   R cprev = R(1), sprev = R(0), ccur = c1, scur = s1;   // cos/sin of m phi by recurrence
   const int mtop = o.mmax_use;
-#pragma unroll 1
+#pragma unroll 2
   for (int m = 0; m <= mtop; ++m) {
     R c, s;
     if (m == 0) { c = R(1); s = R(0); }
