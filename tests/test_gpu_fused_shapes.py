@@ -104,3 +104,41 @@ def test_field_engines_agree(shape, precision):
     tol = 1e-10 if precision == "f64" else 2e-5
     for k in range(6):
         assert _rel(got[1][k], ref[k]) <= tol, (k, _rel(got[1][k], ref[k]))
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_empty_snapshot_between_full_ones(precision):
+    """The fused call on no particles returns zero coefficients (the deposit
+    grids are cleared and no node block is listed), and the workspace it
+    leaves does not leak into a full call or back: empty, full, empty on one
+    workspace, the full call against the oracle."""
+    import torch
+    from exptool_gb300 import _lib
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import eof
+    from oracle import eof as oeof
+    shape = (5, 7, 33, 21)
+    mmax, norder, numx, numy = shape
+    (potC, rforceC, zforceC, potS, rforceS, zforceS), (x, y, z, m), p = _case(*shape, seed=31, n=5000)
+    table = eof.table_from_arrays(mmax, norder, numx, numy, p["cmap"], p["XMIN"], p["dX"], p["YMIN"], p["dY"],
+                                  p["ascale"], p["hscale"], potC, rforceC, zforceC, potS, rforceS, zforceS)
+    pc = _lib.XT_F64 if precision == "f64" else _lib.XT_F32
+    ws = torch.empty(_lib.load().xt_cyl_accumulate_eval_workspace(table.handle, x.size, pc), dtype=torch.uint8,
+                     device="cuda")
+    none = [torch.empty(0, dtype=torch.float64, device="cuda") for _ in range(4)]
+    full = [dev.to_dev(a) for a in (x, y, z, m)]
+    c, s = oeof.accumulate(x, y, z, m, potC, potS, mmax, norder, p["XMIN"], p["dX"], p["YMIN"], p["dY"], numx, numy,
+                           p["ascale"], p["hscale"], p["cmap"])
+    tol = 1e-10 if precision == "f64" else 2e-5
+    for run in ("empty", "full", "empty"):
+        args = none if run == "empty" else full
+        cos, sin, outs = table.accumulate_eval(*args, precision=precision, workspace=ws)
+        cos, sin = dev.to_host(cos), dev.to_host(sin)
+        if run == "empty":
+            assert not np.any(cos) and not np.any(sin)
+            assert all(o.numel() == 0 for o in outs)
+        else:
+            for mm in range(mmax + 1):
+                assert _rel(cos[mm], c[mm]) <= tol, ("cos", mm)
+                if mm:
+                    assert _rel(sin[mm], s[mm]) <= tol, ("sin", mm)
