@@ -84,7 +84,7 @@ struct CylHandle {
   // Tables of the fused paths, tiled by blocks of kTileNodes nodes: block b
   // holds, for rows r = (f * (mmax+1) + m) * norder + k with f = potC rforceC
   // zforceC potS rforceS zforceS, the entries of nodes b*kTileNodes ... as
-  // FP32 roundings (tile_hi) and 16-bit remainders (tile_lo, lo16_decode).
+  // FP32 roundings (tile_hi) and 16-bit remainders (tile_lo, lo16_unscaled).
   float* tile_hi = nullptr;
   short* tile_lo = nullptr;
   size_t tile_rows = 0;      // 6 (mmax+1) norder
@@ -1132,10 +1132,18 @@ __global__ void __launch_bounds__(NT, MINB) k_cyl_field2(const float* __restrict
         for (int u = 0; u < RB; ++u) {
           if (k0 + u < norder) {
             const df c = coef[k0 + u];
-            acc[0].fma(c, df{vh[u].x, SPLIT ? lo16_decode(vh[u].x, vl[u].x) : 0.f});
-            acc[1].fma(c, df{vh[u].y, SPLIT ? lo16_decode(vh[u].y, vl[u].y) : 0.f});
-            acc[2].fma(c, df{vh[u].z, SPLIT ? lo16_decode(vh[u].z, vl[u].z) : 0.f});
-            acc[3].fma(c, df{vh[u].w, SPLIT ? lo16_decode(vh[u].w, vl[u].w) : 0.f});
+            if constexpr (SPLIT) {
+              const float cs = c.h * kLo16Scale;
+              acc[0].fma_lo16(c, cs, vh[u].x, lo16_unscaled(vh[u].x, vl[u].x));
+              acc[1].fma_lo16(c, cs, vh[u].y, lo16_unscaled(vh[u].y, vl[u].y));
+              acc[2].fma_lo16(c, cs, vh[u].z, lo16_unscaled(vh[u].z, vl[u].z));
+              acc[3].fma_lo16(c, cs, vh[u].w, lo16_unscaled(vh[u].w, vl[u].w));
+            } else {
+              acc[0].fma(c, df{vh[u].x, 0.f});
+              acc[1].fma(c, df{vh[u].y, 0.f});
+              acc[2].fma(c, df{vh[u].z, 0.f});
+              acc[3].fma(c, df{vh[u].w, 0.f});
+            }
           }
         }
       }
@@ -1282,8 +1290,9 @@ __global__ void __launch_bounds__(kFieldThreads, 1)
           const df ck = c[k];
           if constexpr (SPLIT) {
             const short2 l = *reinterpret_cast<const short2*>(sl + row0 + (size_t)k * QN);
-            a0.fma(ck, df{h.x, lo16_decode(h.x, l.x)});
-            a1.fma(ck, df{h.y, lo16_decode(h.y, l.y)});
+            const float cks = ck.h * kLo16Scale;
+            a0.fma_lo16(ck, cks, h.x, lo16_unscaled(h.x, l.x));
+            a1.fma_lo16(ck, cks, h.y, lo16_unscaled(h.y, l.y));
           } else {
             a0.fma(ck, df{h.x, 0.f});
             a1.fma(ck, df{h.y, 0.f});
@@ -1522,13 +1531,14 @@ __global__ void __launch_bounds__(128) k_cyl_contract_df(const float* __restrict
       const float4 ev = *reinterpret_cast<const float4*>(ep + t);
       const df dv[4] = {df_add(df_split_or_from(da.x), {ev.x, 0.f}), df_add(df_split_or_from(da.y), {ev.y, 0.f}),
                         df_add(df_split_or_from(db.x), {ev.z, 0.f}), df_add(df_split_or_from(db.y), {ev.w, 0.f})};
+      const float dvs[4] = {dv[0].h * kLo16Scale, dv[1].h * kLo16Scale, dv[2].h * kLo16Scale, dv[3].h * kLo16Scale};
 #pragma unroll
       for (int u = 0; u < KB; ++u) {
         if (kbase + u < norder) {
-          acc[u].fma(dv[0], df{vh[u].x, lo16_decode(vh[u].x, vl[u].x)});
-          acc[u].fma(dv[1], df{vh[u].y, lo16_decode(vh[u].y, vl[u].y)});
-          acc[u].fma(dv[2], df{vh[u].z, lo16_decode(vh[u].z, vl[u].z)});
-          acc[u].fma(dv[3], df{vh[u].w, lo16_decode(vh[u].w, vl[u].w)});
+          acc[u].fma_lo16(dv[0], dvs[0], vh[u].x, lo16_unscaled(vh[u].x, vl[u].x));
+          acc[u].fma_lo16(dv[1], dvs[1], vh[u].y, lo16_unscaled(vh[u].y, vl[u].y));
+          acc[u].fma_lo16(dv[2], dvs[2], vh[u].z, lo16_unscaled(vh[u].z, vl[u].z));
+          acc[u].fma_lo16(dv[3], dvs[3], vh[u].w, lo16_unscaled(vh[u].w, vl[u].w));
         }
       }
     }

@@ -87,6 +87,19 @@ struct dacc {
     s = t;
     e = __fadd_rn(e, __fadd_rn(err, pe));
   }
+  // fma(x, {yh, yl}) for a table entry whose remainder yl is given unscaled:
+  // kl = lo16_unscaled(yh, k), xs = x.h * kLo16Scale (so xs kl = x.h yl)
+  __device__ __forceinline__ void fma_lo16(df x, float xs, float yh, float kl) {
+    const float p = __fmul_rn(x.h, yh);
+    float pe = __fmaf_rn(x.h, yh, -p);
+    pe = __fmaf_rn(xs, kl, pe);
+    pe = __fmaf_rn(x.l, yh, pe);
+    const float t = __fadd_rn(s, p);
+    const float v = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, v)), __fsub_rn(p, v));
+    s = t;
+    e = __fadd_rn(e, __fadd_rn(err, pe));
+  }
   // the same state as fma(x, y) from zero (the TwoSum with s = 0 is exact),
   // without the TwoSum
   __device__ __forceinline__ void set(df x, df y) {
@@ -200,7 +213,7 @@ __device__ __forceinline__ double df_to_int(df a) { return f2d_int(a.h) + f2d_in
 // rounding of t and k = round((t - hi) / 2^(e-38)), e the exponent of hi:
 // |t - hi| <= 2^(e-24), so |k| <= 2^14, and hi + k 2^(e-38) equals t to
 // 2^-39 relative.  hi with a biased exponent below 39 (|hi| < 2^-88) keeps
-// k = 0, as do infinities and NaN.  The scale is built from hi's exponent
+// k = 0, as do |hi| >= 2^113, infinities and NaN.  The scale is built from hi's exponent
 // bits and k is converted by the 1.5 * 2^23 magic-number sum (exact for
 // |k| < 2^22), so decoding is four integer/FP32 instructions.
 constexpr int kLo16Shift = 38;
@@ -211,9 +224,20 @@ __device__ __forceinline__ float lo16_decode(float hi, int k) {
   return __fmul_rn(kf, __int_as_float(max(b, 0)));
 }
 
+// The remainder without its constant scale, k 2^e (e the exponent of hi):
+// lo16_decode(hi, k) = lo16_unscaled(hi, k) 2^-38 exactly.  Exact for
+// |hi| < 2^113 (lo16_encode stores no remainder above), 0 for a zero or
+// subnormal hi.  A product c lo is then (c 2^-38) (k 2^e), with the 2^-38
+// applied to c once per coefficient.
+__device__ __forceinline__ float lo16_unscaled(float hi, int k) {
+  const float kf = __fsub_rn(__int_as_float(0x4B400000 + k), 12582912.f);
+  return __fmul_rn(kf, __int_as_float(__float_as_int(hi) & 0x7f800000));
+}
+constexpr float kLo16Scale = 0x1.0p-38f;   // 2^-kLo16Shift
+
 __device__ __forceinline__ short lo16_encode(double t, float hi) {
   const int hb = (__float_as_int(hi) >> 23) & 0xff;
-  if (hb < kLo16Shift + 1 || hb == 0xff) return 0;
+  if (hb < kLo16Shift + 1 || hb >= 127 + 113) return 0;   // (also infinities and NaN)
   const double r = t - (double)hi;                       // exact
   return (short)llrint(ldexp(r, 127 + kLo16Shift - hb));  // r / 2^(e-38), exact scaling
 }
