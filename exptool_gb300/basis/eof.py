@@ -298,8 +298,8 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
         c, s = dev.pad2(c, table.mmax + 1, table.norder), dev.pad2(s, table.mmax + 1, table.norder)
         n = int(np.asarray(d["x"]).size) if not isinstance(d["x"], torch.Tensor) else int(d["x"].numel())
         # one page-locked block for the results: R written into it by the
-        # binning kernel, p0 p fr fp fz copied in half by half behind the
-        # evaluation; one wait
+        # binning kernel, p0 p fr fp fz copied in part by part (3/8, 5/8 of
+        # the particles) behind the evaluation; one wait
         blk = torch.empty(6 * n, dtype=torch.float64, pin_memory=True)
         table.eval_sorted(*(dev.kernel_input(a) for a in (d["x"], d["y"], zsrc)), c, s, precision=precision,
                           m1=m1, m2=m2, r_out=blk.data_ptr() + 40 * n, res_out=blk.data_ptr())

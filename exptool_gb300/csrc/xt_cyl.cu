@@ -69,9 +69,12 @@ struct FusedGraph {
 };
 
 // Parts of the particle range whose results, bound for host memory, are
-// evaluated and copied out in turn (measured on 1e6 disc particles: two parts
-// save 0.046 ms per call against evaluating then copying, four 0.032 ms: each
-// part adds deposit segments, scan buckets and an evaluation launch).
+// evaluated and copied out in turn (measured on 1e6 disc particles: two halves
+// save 0.046 ms per call against evaluating then copying, four quarters 0.032
+// ms: each part adds deposit segments, scan buckets and an evaluation launch).
+// The first part holds 3/8 of the particles: the copy out runs at about half
+// the evaluation's rate, so a smaller first part starts it sooner, and the
+// second part's evaluation (5/8) still ends before the first part's copy.
 constexpr int kHostParts = 2;
 
 struct CylHandle {
@@ -402,8 +405,9 @@ static_assert(sizeof(BinRec<df>) == 48 && sizeof(BinRec<float>) == 32, "record s
 
 // Counting-sort bucket of particle p in table cell `cell`: the cell alone, or
 // with qchunk > 0 (results bound for host memory) the cell within the
-// particle's part p / qchunk of the particle range, so that the records of
-// each part are contiguous and its results complete as a block.
+// particle's part min(p / qchunk, kHostParts - 1) of the particle range, so
+// that the records of each part are contiguous and its results complete as a
+// block.
 __device__ __forceinline__ int sort_bucket(long long p, int qchunk, int ncell, int cell) {
   if (qchunk <= 0) return cell;
   int q = 0;   // p / qchunk by comparisons (below kHostParts)
@@ -1838,13 +1842,19 @@ struct FusedLayout {
   size_t hist_bytes;   // the bucket counts and the node-block flags after them, cleared together
 };
 
-// Particles per part of the sort when the results go to page-locked host
-// memory (the parts are evaluated and copied out in turn); 0 for device
+// Particles in the first part of the sort when the results go to page-locked
+// host memory (the parts are evaluated and copied out in turn); 0 for device
 // results, which are sorted by cell alone, and for other host memory.
 static int fused_qchunk(const CylHandle* h, long long n, bool staged) {
   const long long ncell = (long long)h->numx * h->numy;
   if (!staged || n <= 0 || kHostParts * ncell > (long long)kScanTile * kScanTile) return 0;
-  return (int)((n + kHostParts - 1) / kHostParts);
+  return (int)std::max<long long>(32, ((3 * n + 7) / 8 + 31) & ~31LL);
+}
+
+// Parts of the host-result sort for part size qchunk (0: one part); the last
+// part takes the rest of the particles.
+static int host_parts(long long n, int qchunk) {
+  return qchunk ? (int)std::min<long long>((n + qchunk - 1) / qchunk, kHostParts) : 1;
 }
 
 // host_out: some of p0 p fr fp fz is host memory; staged: all of those that
@@ -1996,10 +2006,10 @@ static BinrecDf binrec_constants(const CylTab<double>& T) {
 static int stage_copies(CylHandle* h, const FusedLayout& L, void* workspace, long long n, int qchunk,
                         double* const* outs, cudaStream_t st) {
   const double* stage = reinterpret_cast<const double*>(static_cast<char*>(workspace) + L.stage);
-  const int npart = (int)((n + qchunk - 1) / qchunk);
+  const int npart = host_parts(n, qchunk);
   for (int q = 0; q < npart; ++q) {
     XT_CUDA(cudaStreamWaitEvent(h->copy, h->qev[q], 0));
-    const long long p0 = (long long)q * qchunk, np = std::min<long long>(qchunk, n - p0);
+    const long long p0 = (long long)q * qchunk, np = q + 1 < npart ? qchunk : n - p0;
     for (int k = 0; k < 5; ++k)
       if (outs[k])
         XT_CUDA(cudaMemcpyAsync(outs[k] + p0, stage + (size_t)k * n + p0, (size_t)np * sizeof(double),
@@ -2134,7 +2144,7 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
   const int nblk = (int)((h->nnode + kTileNodes - 1) / kTileNodes);
   // results bound for host memory: records sorted by (part, cell), the parts
   // evaluated in turn and copied out behind the evaluation
-  const int npart = qchunk ? (int)((n + qchunk - 1) / qchunk) : 1;
+  const int npart = host_parts(n, qchunk);
   const int nbucket = qchunk ? npart * ncell : ncell;
   ActiveBlocks ab;
   ab.flag = reinterpret_cast<int*>(ws + L.flag);
@@ -2314,7 +2324,8 @@ static int sorted_enqueue(CylHandle* h, const FusedLayout& L, void* workspace, c
         for (int q = 0; q < npart; ++q) {
           const int* rb = off + (size_t)q * ncell;
           const int* re = q + 1 < npart ? off + (size_t)(q + 1) * ncell : nullptr;
-          if ((rc = eval(so, rb, re, qchunk, std::true_type{}))) return rc;
+          const long long np = q + 1 < npart ? qchunk : n - (long long)q * qchunk;
+          if ((rc = eval(so, rb, re, np, std::true_type{}))) return rc;
           XT_CUDA(cudaEventRecordWithFlags(h->qev[q], st, evf));
         }
       }

@@ -466,9 +466,9 @@ class CylTable:
         ``r_out`` (a length-n float64 tensor or a raw address, device or
         page-locked host memory) R is written there by the binning kernel
         instead of into row 5.  With ``res_out`` (the address of 5 n
-        page-locked float64) p0 p fr fp fz go there, half of the particles at a
-        time behind the evaluation, and None is returned; they are complete
-        when the stream's work is."""
+        page-locked float64) p0 p fr fp fz go there, one part of the particles
+        (3/8, then 5/8) at a time behind the evaluation, and None is returned;
+        they are complete when the stream's work is."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
         ws = self._sorted_workspace(n, pc)

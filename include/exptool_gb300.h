@@ -208,9 +208,10 @@ int xt_cyl_eval_points(void *handle, const void *field, int precision, int densi
  * norder <= 24.  Unlike the other entry points, x, y, z, m and outs may also
  * be host memory the device addresses (xt_pointer_access XT_PTR_PINNED or
  * XT_PTR_PAGEABLE): the kernels then read the particles in place over the
- * host link.  Page-locked results are evaluated half of the particles at a
- * time into the workspace and each half is copied out on a second stream while
- * the other is evaluated (the call's stream waits for the copies); pageable
+ * host link.  Page-locked results are evaluated in two parts of the particle
+ * range (the first 3/8, then the rest) into the workspace, the first part
+ * copied out on a second stream while the second is evaluated (the call's
+ * stream waits for the copies); pageable
  * results are evaluated in particle order so that their writes over the link
  * are coalesced.  XT_PTR_INACCESSIBLE pointers return XT_ERR_ARG. */
 size_t xt_cyl_accumulate_eval_workspace(void *handle, long long n, int precision);
