@@ -1857,16 +1857,16 @@ static int host_parts(long long n, int qchunk) {
   return qchunk ? (int)std::min<long long>((n + qchunk - 1) / qchunk, kHostParts) : 1;
 }
 
-// host_out: some of p0 p fr fp fz is host memory; staged: all of those that
-// are host memory are page-locked (their copies can run on a stream).
-static void host_result_kinds(double* const* outs, bool& host_out, bool& staged) {
+// From the pointer kinds of p0 p fr fp fz (kind[i] < 0: NULL): host_out,
+// some of them are host memory; staged, all of those that are host memory are
+// page-locked (their copies can run on a stream).
+static void host_result_kinds(const int* kind, bool& host_out, bool& staged) {
   host_out = false;
   staged = true;
   for (int i = 0; i < 5; ++i) {
-    if (!outs[i]) continue;
-    const int k = pointer_access(outs[i]);
-    host_out |= k != XT_PTR_DEVICE;
-    staged &= k == XT_PTR_DEVICE || k == XT_PTR_PINNED;
+    if (kind[i] < 0) continue;
+    host_out |= kind[i] != XT_PTR_DEVICE;
+    staged &= kind[i] == XT_PTR_DEVICE || kind[i] == XT_PTR_PINNED;
   }
   staged &= host_out;
 }
@@ -2353,20 +2353,19 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
              "the fused path supports numx*numy <= %d cells", kScanTile * kScanTile);
   // particle arrays and results may live in host memory the device can
   // address (pinned, or any host memory where the device has pageable access)
-  bool host_out = false;
+  bool host_out = false, staged = false;
   if (n > 0) {
     for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
       XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
                  p);
+    int kind[6];
     for (int i = 0; i < 6; ++i) {
-      if (!outs[i]) continue;
-      const int k = pointer_access(outs[i]);
-      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
-      if (i < 5) host_out |= k != XT_PTR_DEVICE;   // R (outs[5]) is written coalesced by the binning kernel
+      kind[i] = outs[i] ? pointer_access(outs[i]) : -1;
+      XT_REQUIRE(kind[i] != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
     }
+    // R (outs[5]) is written coalesced by the binning kernel
+    host_result_kinds(kind, host_out, staged);
   }
-  bool staged = false;
-  if (n > 0) host_result_kinds(outs, host_out, staged);
   const int qchunk = fused_qchunk(h, n, staged);
   const FusedLayout L = fused_layout(h, n, precision);
   if (!workspace || workspace_bytes < L.total) {
@@ -2391,10 +2390,10 @@ int xt_cyl_accumulate_eval(void* handle, const double* x, const double* y, const
 }
 
 
-// Shared argument checks of the sorted entry points; sets host_out when a
-// result array is host memory.
+// Shared argument checks of the sorted entry points; sets host_out and staged
+// as host_result_kinds does.
 static int sorted_checks(const CylHandle* h, const double* x, const double* y, const double* z, const double* m,
-                         long long n, int precision, double* const* outs, int nouts, bool& host_out) {
+                         long long n, int precision, double* const* outs, int nouts, bool& host_out, bool& staged) {
   XT_REQUIRE(h, "NULL table handle");
   XT_REQUIRE(n >= 0 && n < (1LL << 31), "particle count must be in [0, 2^31)");
   XT_REQUIRE(n == 0 || (x && y && z && m), "NULL particle array");
@@ -2403,17 +2402,17 @@ static int sorted_checks(const CylHandle* h, const double* x, const double* y, c
              h->mmax, h->norder);
   XT_REQUIRE((long long)h->numx * h->numy <= (long long)kScanTile * kScanTile,
              "the sorted path supports numx*numy <= %d cells", kScanTile * kScanTile);
-  host_out = false;
+  host_out = staged = false;
   if (n > 0) {
     for (const void* p : {(const void*)x, (const void*)y, (const void*)z, (const void*)m})
       XT_REQUIRE(pointer_access(p) != XT_PTR_INACCESSIBLE, "particle array %p is host memory the device cannot address",
                  p);
-    for (int i = 0; i < nouts; ++i) {
-      if (!outs[i]) continue;
-      const int k = pointer_access(outs[i]);
-      XT_REQUIRE(k != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
-      if (i < 5) host_out |= k != XT_PTR_DEVICE;
+    int kind[6] = {-1, -1, -1, -1, -1, -1};
+    for (int i = 0; i < nouts && i < 6; ++i) {
+      kind[i] = outs[i] ? pointer_access(outs[i]) : -1;
+      XT_REQUIRE(kind[i] != XT_PTR_INACCESSIBLE, "result array %d is host memory the device cannot address", i);
     }
+    host_result_kinds(kind, host_out, staged);
   }
   return XT_OK;
 }
@@ -2422,9 +2421,9 @@ int xt_cyl_accumulate_sorted(void* handle, const double* x, const double* y, con
                              long long n, int precision, int nan_to_origin, double* cos_out, double* sin_out,
                              void* workspace, size_t workspace_bytes, void* stream) {
   CylHandle* h = static_cast<CylHandle*>(handle);
-  bool host_out = false;
+  bool host_out = false, staged = false;
   double* const none[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  int rc = sorted_checks(h, x, y, z, m, n, precision, none, 6, host_out);
+  int rc = sorted_checks(h, x, y, z, m, n, precision, none, 6, host_out, staged);
   if (rc) return rc;
   XT_REQUIRE(cos_out && sin_out, "NULL output");
   const FusedLayout L = fused_layout(h, n, precision);
@@ -2441,14 +2440,12 @@ int xt_cyl_eval_sorted(void* handle, const double* x, const double* y, const dou
                        void* workspace, size_t workspace_bytes, void* stream) {
   CylHandle* h = static_cast<CylHandle*>(handle);
   XT_REQUIRE(outs, "NULL output list");
-  bool host_out = false;
+  bool host_out = false, staged = false;
   // the binning kernel reads a mass per particle for the deposit weight, which
   // evaluation does not use: it is given the x array
-  int rc = sorted_checks(h, x, y, z, x, n, precision, outs, 6, host_out);
+  int rc = sorted_checks(h, x, y, z, x, n, precision, outs, 6, host_out, staged);
   if (rc) return rc;
   XT_REQUIRE(cos_c && sin_c, "NULL coefficients");
-  bool staged = false;
-  if (n > 0) host_result_kinds(outs, host_out, staged);
   const FusedLayout L = fused_layout(h, n, precision);
   if (!workspace || workspace_bytes < L.total) {
     set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);
