@@ -1373,7 +1373,11 @@ static bool field_bulk_plan(const CylHandle* h, bool f64, FieldBulkPlan& P) {
 // blocks or a rolled m loop 0.127 ms.  Two threads per record (orders split
 // between the lanes of a pair, sums exchanged by shuffles; 64 registers, twice
 // the warps) took 0.152 ms: the kernel is bound by its double-float
-// instruction count, not by latency.
+// instruction count, not by latency.  Interpolation sums split against a
+// power of two above the cell's partial sums (ExtractScalar: 7 FP32
+// operations a product instead of 12) took 0.1136 ms against 0.1165, with
+// spills at 96 registers and about 3x the interpolation's rounding error: not
+// taken.
 template <bool SORTED>
 __global__ void __launch_bounds__(128, 5) k_cyl_eval_sorted_df(CylTab<double> T, const df* __restrict__ F, long long n,
                                                             const BinRec<df>* __restrict__ recs, int m1, int m2,
