@@ -169,7 +169,7 @@ def accumulate(ParticleInstance, potC, potS, MMAX, NMAX, XMIN, dX, YMIN, dY, NUM
     pS = np.asarray(potS)[:MMAX + 1, :NMAX]
     table = table_from_arrays(MMAX, NMAX, NUMX, NUMY, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, pC, potS=pS)
     c, s = _accumulate_dev(table, positions(ParticleInstance, allow_device=True), precision, nan_to_origin=False)
-    return dev.to_host(c), dev.to_host(s)
+    return tuple(dev.to_host_many([c, s]))
 
 
 def _accumulate_dev(table, xyzm, precision, nan_to_origin):
@@ -216,8 +216,7 @@ def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max
     # particles with a NaN coordinate are placed at the origin on the device
     # (eof.py:1189-1204) unless nanblock
     c, s = _accumulate_dev(table, (x, y, z, m), precision, nan_to_origin=not nanblock)
-    out.cos = dev.to_host(c)
-    out.sin = dev.to_host(s)
+    out.cos, out.sin = dev.to_host_many([c, s])
     return out
 
 
@@ -291,11 +290,7 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
     if not density and table.sorted_ok():
         # binning, counting sort by table cell, field and evaluation in cell
         # order; particle arrays in page-locked host memory are read in place
-        c = dev.to_dev(np.asarray(accum_cos, dtype=np.float64) if not isinstance(accum_cos, torch.Tensor)
-                       else accum_cos)
-        s = dev.to_dev(np.asarray(accum_sin, dtype=np.float64) if not isinstance(accum_sin, torch.Tensor)
-                       else accum_sin)
-        c, s = dev.pad2(c, table.mmax + 1, table.norder), dev.pad2(s, table.mmax + 1, table.norder)
+        c, s = dev.coef_pair_to_dev(accum_cos, accum_sin, table.mmax + 1, table.norder)
         n = int(np.asarray(d["x"]).size) if not isinstance(d["x"], torch.Tensor) else int(d["x"].numel())
         # one page-locked block for the results: R written into it by the
         # binning kernel, p0 p fr fp fz copied in part by part (3/8, 5/8 of
@@ -312,7 +307,7 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
     z = dev.to_dev(zsrc)
     outs = table.eval_points(field, x, y, z, _lib.XT_CYL_ACCUMULATED_EVAL_PARTICLES, _lib.XT_COORD_CART, m1=m1, m2=m2,
                              want=[1, 1, 1, 1, 1, 1, int(density), int(density)])
-    p0, p, fr, fp, fz, R, d0, dd = (dev.to_host(t) if t is not None else None for t in outs)
+    p0, p, fr, fp, fz, R, d0, dd = dev.to_host_many(list(outs))
     if density:
         return p0, p, d0, dd, fr, fp, fz, R
     return p0, p, fr, fp, fz, R

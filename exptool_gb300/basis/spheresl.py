@@ -193,7 +193,7 @@ def all_eval_particles(Particles, expcoef, sph_file, mod_file, verbose=0, L1=-10
     a, b, c = (dev.to_dev(d[k]) for k in ("x", "y", "z"))
     outs = table.eval_points(field, a, b, c, _lib.XT_SPH_ALL_EVAL_PARTICLES, _lib.XT_COORD_CART, L1=L1, L2=L2,
                              no_odd=NO_ODD)
-    return tuple(dev.to_host(t) for t in outs)
+    return tuple(dev.to_host_many(list(outs)))
 
 
 def eval_particles(ParticleInstance, expcoef, sph_file, mod_file, nprocs=-1, verbose=1, l1=0, l2=1000,
@@ -232,7 +232,7 @@ def all_eval(r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax, evtabl
     Returns den0, den1, pot0, pot1, potr, pott, potp."""
     outs, scalar = _point_eval(_lib.XT_SPH_ALL_EVAL, r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax,
                                evtable, eftable, no_odd, False, precision)
-    res = [dev.to_host(t) for t in outs[:7]]
+    res = dev.to_host_many(list(outs[:7]))
     return tuple(float(v[0]) for v in res) if scalar else tuple(res)
 
 
@@ -244,7 +244,7 @@ def force_eval(r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax, evta
     ``correct_m=True`` uses cos(m phi) / sin(m phi) as ``all_eval`` does."""
     outs, scalar = _point_eval(_lib.XT_SPH_FORCE_EVAL, r, costh, phi, expcoef, xi, p0, d0, cmap, scale, lmax, nmax,
                                evtable, eftable, no_odd, not correct_m, precision)
-    res = [dev.to_host(t) for t in outs[:5]]
+    res = dev.to_host_many(list(outs[:5]))
     return tuple(float(v[0]) for v in res) if scalar else tuple(res)
 
 

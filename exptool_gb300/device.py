@@ -104,12 +104,14 @@ def copy_and_sync(pairs):
 
 def to_host_many(ts) -> list:
     """Several device tensors -> NumPy arrays in pinned host memory: all
-    copies enqueued on the current stream, one synchronisation."""
-    hs = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in ts]
+    copies enqueued on the current stream, one synchronisation (None entries
+    stay None)."""
+    hs = [None if t is None else torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in ts]
     for h, t in zip(hs, ts):
-        h.copy_(t, non_blocking=True)
+        if t is not None:
+            h.copy_(t, non_blocking=True)
     torch.cuda.current_stream().synchronize()
-    return [h.numpy() for h in hs]
+    return [None if h is None else h.numpy() for h in hs]
 
 
 def to_host(t: torch.Tensor) -> np.ndarray:
@@ -509,6 +511,23 @@ class CylTable:
                                                 int(mmax_use), int(bool(no_odd)), int(bool(perturb)), pp,
                                                 stream_ptr()), "xt_cyl_eval_points")
         return outs
+
+
+def coef_pair_to_dev(cos, sin, rows, cols):
+    """Coefficients (cos, sin) -> two (rows, cols) float64 CUDA tensors,
+    zero-padded or cropped.  Host arrays go through one page-locked block and
+    one copy enqueued on the current stream without waiting (torch holds the
+    block until the copy has run); CUDA tensors are padded on the device."""
+    if isinstance(cos, torch.Tensor) or isinstance(sin, torch.Tensor):
+        return pad2(to_dev(cos), rows, cols), pad2(to_dev(sin), rows, cols)
+    h = torch.zeros((2, rows, cols), dtype=torch.float64, pin_memory=True)
+    hn = h.numpy()
+    for k, a in enumerate((cos, sin)):
+        a = np.asarray(a, dtype=np.float64)
+        r, c = min(rows, a.shape[0]), min(cols, a.shape[1])
+        hn[k, :r, :c] = a[:r, :c]
+    d = h.to(device(), non_blocking=True)
+    return d[0], d[1]
 
 
 def pad2(t, rows, cols):
