@@ -168,23 +168,24 @@ def accumulate(ParticleInstance, potC, potS, MMAX, NMAX, XMIN, dX, YMIN, dY, NUM
     pC = np.asarray(potC)[:MMAX + 1, :NMAX]
     pS = np.asarray(potS)[:MMAX + 1, :NMAX]
     table = table_from_arrays(MMAX, NMAX, NUMX, NUMY, CMAP, XMIN, dX, YMIN, dY, ASCALE, HSCALE, pC, potS=pS)
-    c, s = _accumulate_dev(table, positions(ParticleInstance, allow_device=True), precision, nan_to_origin=False)
-    return tuple(dev.to_host_many([c, s]))
+    return _accumulate_host(table, positions(ParticleInstance, allow_device=True), precision, nan_to_origin=False)
 
 
-def _accumulate_dev(table, xyzm, precision, nan_to_origin):
-    """(cos, sin) device tensors: the sorted pipeline where the table fits it
-    (particle arrays in page-locked host memory are read in place), else the
-    particle-order deposit."""
+def _accumulate_host(table, xyzm, precision, nan_to_origin):
+    """(cos, sin) NumPy arrays: the sorted pipeline where the table fits it
+    (particle arrays in page-locked host memory are read in place, and the
+    last kernel writes the coefficients into page-locked memory), else the
+    particle-order deposit and one copy out."""
     if table.sorted_ok():
         coef = table.accumulate_sorted(*(dev.kernel_input(a) for a in xyzm), precision=precision,
-                                       nan_to_origin=nan_to_origin)
+                                       nan_to_origin=nan_to_origin, host=True)
         return coef[0], coef[1]
     x, y, z, m = (dev.to_dev(a) for a in xyzm)
     if nan_to_origin:
         bad = torch.isnan(x) | torch.isnan(y) | torch.isnan(z)
         x, y, z = (torch.where(bad, torch.zeros_like(a), a) for a in (x, y, z))
-    return table.accumulate(x, y, z, m, precision=precision)
+    c, s = table.accumulate(x, y, z, m, precision=precision)
+    return tuple(dev.fetch_many([c, s]))
 
 
 def make_coefficients_multi(ParticleInstance, nprocs, potC, potS, mmax, norder, XMIN, dX, YMIN, dY, numx, numy,
@@ -215,8 +216,7 @@ def compute_coefficients(PSPInput, eof_file, verbose=1, no_odd=False, nprocs_max
     out.nmax = table.norder
     # particles with a NaN coordinate are placed at the origin on the device
     # (eof.py:1189-1204) unless nanblock
-    c, s = _accumulate_dev(table, (x, y, z, m), precision, nan_to_origin=not nanblock)
-    out.cos, out.sin = dev.to_host_many([c, s])
+    out.cos, out.sin = _accumulate_host(table, (x, y, z, m), precision, nan_to_origin=not nanblock)
     return out
 
 

@@ -95,7 +95,7 @@ def compute_coefficients_solitary(ParticleInstance, sph_file, model_file, verbos
     table = table_from_files(sph_file, model_file)
     x, y, z, m = (dev.to_dev(a) for a in positions(ParticleInstance))
     ec = table.accumulate(x, y, z, m, no_odd=no_odd, precision=precision)
-    return dev.to_host(ec)
+    return dev.fetch_many([ec])[0]
 
 
 def compute_coefficients(PSPInput, sph_file, mod_file, verbose=1, no_odd=False, precision="f64"):
@@ -114,7 +114,7 @@ def compute_coefficients(PSPInput, sph_file, mod_file, verbose=1, no_odd=False, 
     out.lmax = table.lmax
     out.nmax = table.nmax
     xd, yd, zd, md = (dev.to_dev(a) for a in (x, y, z, m))
-    out.expcoef = dev.to_host(table.accumulate(xd, yd, zd, md, no_odd=no_odd, precision=precision))
+    out.expcoef = dev.fetch_many([table.accumulate(xd, yd, zd, md, no_odd=no_odd, precision=precision)])[0]
     return out
 
 

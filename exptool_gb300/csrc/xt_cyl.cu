@@ -2430,6 +2430,8 @@ int xt_cyl_accumulate_sorted(void* handle, const double* x, const double* y, con
   int rc = sorted_checks(h, x, y, z, m, n, precision, none, 6, host_out, staged);
   if (rc) return rc;
   XT_REQUIRE(cos_out && sin_out, "NULL output");
+  XT_REQUIRE(pointer_access(cos_out) != XT_PTR_INACCESSIBLE && pointer_access(sin_out) != XT_PTR_INACCESSIBLE,
+             "coefficient output is host memory the device cannot address");
   const FusedLayout L = fused_layout(h, n, precision);
   if (!workspace || workspace_bytes < L.total) {
     set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);

@@ -114,6 +114,38 @@ def to_host_many(ts) -> list:
     return [None if h is None else h.numpy() for h in hs]
 
 
+_fetch_scratch = threading.local()
+_upload_scratch = threading.local()
+
+
+def fetch_many(ts) -> list:
+    """Small device tensors (coefficients) -> NumPy arrays of their own: one
+    library copy each into a per-thread page-locked scratch block, one wait,
+    then a host copy out of the block.  Cheaper per call than fresh
+    page-locked tensors from torch for a few kilobytes."""
+    ts = [t.contiguous() for t in ts]
+    nbs = [t.numel() * t.element_size() for t in ts]
+    offs = np.cumsum([0] + [(nb + 255) & ~255 for nb in nbs]).tolist()
+    buf = pinned_scratch(offs[-1])
+    base = buf.data_ptr()
+    copy_and_sync([(base + o, t.data_ptr(), nb) for o, t, nb in zip(offs, ts, nbs) if nb])
+    hb = buf.numpy()
+    return [hb[o:o + nb].view(_NP_DTYPE[t.dtype]).reshape(tuple(t.shape)).copy() for o, t, nb in zip(offs, ts, nbs)]
+
+
+def pinned_scratch(nbytes: int) -> torch.Tensor:
+    """This thread's page-locked scratch block (uint8, at least nbytes), kept
+    between calls; its contents are valid until the thread's next use."""
+    buf = getattr(_fetch_scratch, "v", None)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 1 << 16), dtype=torch.uint8, pin_memory=True)
+        _fetch_scratch.v = buf
+    return buf
+
+
+_NP_DTYPE = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32, torch.int64: np.int64}
+
+
 def to_host(t: torch.Tensor) -> np.ndarray:
     """Device tensor -> NumPy array in pinned host memory (torch's caching
     host allocator), so the device-to-host copy is a direct DMA; the array
@@ -447,19 +479,31 @@ class CylTable:
             self._sorted_ws.v = ws
         return ws
 
-    def accumulate_sorted(self, x, y, z, m, precision="f64", nan_to_origin=True):
+    def accumulate_sorted(self, x, y, z, m, precision="f64", nan_to_origin=True, host=False):
         """Coefficients through the sorted pipeline (binning, counting sort by
         cell, run-accumulated deposit, contraction): a (2, mmax+1, norder)
-        device tensor of cos and sin.  x, y, z, m as for accumulate_eval."""
+        device tensor of cos and sin, or with ``host`` a NumPy array of its
+        own (the last kernel writes the coefficients into a per-thread
+        page-locked block, then one wait).  x, y, z, m as for accumulate_eval."""
         n = int(x.numel()) if isinstance(x, torch.Tensor) else int(np.asarray(x).size)
         pc = precision_code(precision)
         ws = self._sorted_workspace(n, pc)
-        coef = torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device())
+        nc = (self.mmax + 1) * self.norder
+        if host:
+            coef = None
+            base = pinned_scratch(16 * nc).data_ptr()
+        else:
+            coef = torch.empty((2, self.mmax + 1, self.norder), dtype=torch.float64, device=device())
+            base = coef.data_ptr()
         _lib.check(self._lib.xt_cyl_accumulate_sorted(self.handle, _addr(x), _addr(y), _addr(z), _addr(m), n, pc,
-                                                      int(bool(nan_to_origin)), dptr(coef[0]), dptr(coef[1]),
+                                                      int(bool(nan_to_origin)), base, base + 8 * nc,
                                                       ws.data_ptr(), ws.numel(), stream_ptr()),
                    "xt_cyl_accumulate_sorted")
-        return coef
+        if not host:
+            return coef
+        copy_and_sync([])
+        return pinned_scratch(16 * nc).numpy()[:16 * nc].view(np.float64).reshape(2, self.mmax + 1,
+                                                                                 self.norder).copy()
 
     def eval_sorted(self, x, y, z, cos, sin, precision="f64", m1=0, m2=1000, r_out=None, res_out=None):
         """accumulated_eval_particles (no density) through the sorted pipeline
@@ -520,13 +564,23 @@ def coef_pair_to_dev(cos, sin, rows, cols):
     block until the copy has run); CUDA tensors are padded on the device."""
     if isinstance(cos, torch.Tensor) or isinstance(sin, torch.Tensor):
         return pad2(to_dev(cos), rows, cols), pad2(to_dev(sin), rows, cols)
-    h = torch.zeros((2, rows, cols), dtype=torch.float64, pin_memory=True)
-    hn = h.numpy()
+    nb = 2 * rows * cols * 8
+    st = getattr(_upload_scratch, "v", None)
+    if st is None or st[0].numel() < nb:
+        st = (torch.empty(max(nb, 1 << 16), dtype=torch.uint8, pin_memory=True), torch.cuda.Event())
+        _upload_scratch.v = st
+    buf, done = st
+    done.synchronize()                  # the previous copy out of the block has run
+    hn = buf.numpy()[:nb].view(np.float64).reshape(2, rows, cols)
+    hn[...] = 0.0
     for k, a in enumerate((cos, sin)):
         a = np.asarray(a, dtype=np.float64)
         r, c = min(rows, a.shape[0]), min(cols, a.shape[1])
         hn[k, :r, :c] = a[:r, :c]
-    d = h.to(device(), non_blocking=True)
+    d = torch.empty((2, rows, cols), dtype=torch.float64, device=device())
+    _lib.check(_lib.load().xt_copy_async(1, (ctypes.c_void_p * 1)(d.data_ptr()), (ctypes.c_void_p * 1)(buf.data_ptr()),
+                                         (ctypes.c_size_t * 1)(nb), stream_ptr()), "xt_copy_async")
+    done.record()
     return d[0], d[1]
 
 

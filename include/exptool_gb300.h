@@ -226,7 +226,9 @@ int xt_cyl_accumulate_eval(void *handle, const double *x, const double *y, const
  * and the same host-memory rules for x, y, z, m and outs.
  * xt_cyl_accumulate_sorted: eof.accumulate / eof.compute_coefficients
  * (eof.py:492-640, 1158-1260) by binning, counting sort by table cell,
- * run-accumulated deposit and contraction into cos_out/sin_out.
+ * run-accumulated deposit and contraction into cos_out/sin_out, which may be
+ * device memory or host memory the device addresses (the last kernel then
+ * writes the coefficients over the host link, with no copy behind it).
  * xt_cyl_eval_sorted: eof.accumulated_eval_particles / eof.compute_forces
  * (eof.py:989-1144, 1263-1317) without density, for m1 <= m <= m2, from the
  * coefficients cos_c/sin_c ((mmax+1) x norder, device): binning, counting
