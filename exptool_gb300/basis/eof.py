@@ -290,7 +290,7 @@ def accumulated_eval_particles(Particles, accum_cos, accum_sin, potC=0, rforceC=
     if not density and table.sorted_ok():
         # binning, counting sort by table cell, field and evaluation in cell
         # order; particle arrays in page-locked host memory are read in place
-        c, s = dev.coef_pair_to_dev(accum_cos, accum_sin, table.mmax + 1, table.norder)
+        c, s = dev.coef_pair(accum_cos, accum_sin, table.mmax + 1, table.norder)
         n = int(np.asarray(d["x"]).size) if not isinstance(d["x"], torch.Tensor) else int(d["x"].numel())
         # one page-locked block for the results: R written into it by the
         # binning kernel, p0 p fr fp fz copied in part by part (3/8, 5/8 of

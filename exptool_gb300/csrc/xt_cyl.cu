@@ -2452,6 +2452,8 @@ int xt_cyl_eval_sorted(void* handle, const double* x, const double* y, const dou
   int rc = sorted_checks(h, x, y, z, x, n, precision, outs, 6, host_out, staged);
   if (rc) return rc;
   XT_REQUIRE(cos_c && sin_c, "NULL coefficients");
+  XT_REQUIRE(pointer_access(cos_c) != XT_PTR_INACCESSIBLE && pointer_access(sin_c) != XT_PTR_INACCESSIBLE,
+             "coefficients are host memory the device cannot address");
   const FusedLayout L = fused_layout(h, n, precision);
   if (!workspace || workspace_bytes < L.total) {
     set_error("workspace of %zu bytes needed, %zu given", L.total, workspace_bytes);

@@ -115,7 +115,7 @@ def to_host_many(ts) -> list:
 
 
 _fetch_scratch = threading.local()
-_upload_scratch = threading.local()
+_coef_block = threading.local()
 
 
 def fetch_many(ts) -> list:
@@ -507,7 +507,8 @@ class CylTable:
 
     def eval_sorted(self, x, y, z, cos, sin, precision="f64", m1=0, m2=1000, r_out=None, res_out=None):
         """accumulated_eval_particles (no density) through the sorted pipeline
-        from device coefficients cos, sin ((mmax+1, norder) float64): a (6, n)
+        from coefficients cos, sin ((mmax+1, norder) float64, device tensors or
+        page-locked host arrays the kernels read in place): a (6, n)
         device tensor of p0, p, fr, fp, fz, R in particle order.  With
         ``r_out`` (a length-n float64 tensor or a raw address, device or
         page-locked host memory) R is written there by the binning kernel
@@ -527,7 +528,7 @@ class CylTable:
         if r_out is not None:
             outs[5] = _addr(r_out)
         _lib.check(self._lib.xt_cyl_eval_sorted(self.handle, _addr(x), _addr(y), _addr(z), n, pc, int(m1), int(m2),
-                                                dptr(cos), dptr(sin), outs, ws.data_ptr(), ws.numel(), stream_ptr()),
+                                                _addr(cos), _addr(sin), outs, ws.data_ptr(), ws.numel(), stream_ptr()),
                    "xt_cyl_eval_sorted")
         return res
 
@@ -557,31 +558,27 @@ class CylTable:
         return outs
 
 
-def coef_pair_to_dev(cos, sin, rows, cols):
-    """Coefficients (cos, sin) -> two (rows, cols) float64 CUDA tensors,
-    zero-padded or cropped.  Host arrays go through one page-locked block and
-    one copy enqueued on the current stream without waiting (torch holds the
-    block until the copy has run); CUDA tensors are padded on the device."""
+def coef_pair(cos, sin, rows, cols):
+    """Coefficients (cos, sin) zero-padded or cropped to (rows, cols) float64,
+    in the form the sorted evaluation reads them: CUDA tensors stay on the
+    device; host arrays are written into this thread's page-locked
+    coefficient block and read there in place by the kernels over the host
+    link (no copy).  The block is rewritten by the thread's next call, so the
+    caller waits for the kernels first."""
     if isinstance(cos, torch.Tensor) or isinstance(sin, torch.Tensor):
         return pad2(to_dev(cos), rows, cols), pad2(to_dev(sin), rows, cols)
     nb = 2 * rows * cols * 8
-    st = getattr(_upload_scratch, "v", None)
-    if st is None or st[0].numel() < nb:
-        st = (torch.empty(max(nb, 1 << 16), dtype=torch.uint8, pin_memory=True), torch.cuda.Event())
-        _upload_scratch.v = st
-    buf, done = st
-    done.synchronize()                  # the previous copy out of the block has run
+    buf = getattr(_coef_block, "v", None)
+    if buf is None or buf.numel() < nb:
+        buf = torch.empty(max(nb, 1 << 16), dtype=torch.uint8, pin_memory=True)
+        _coef_block.v = buf
     hn = buf.numpy()[:nb].view(np.float64).reshape(2, rows, cols)
     hn[...] = 0.0
     for k, a in enumerate((cos, sin)):
         a = np.asarray(a, dtype=np.float64)
         r, c = min(rows, a.shape[0]), min(cols, a.shape[1])
         hn[k, :r, :c] = a[:r, :c]
-    d = torch.empty((2, rows, cols), dtype=torch.float64, device=device())
-    _lib.check(_lib.load().xt_copy_async(1, (ctypes.c_void_p * 1)(d.data_ptr()), (ctypes.c_void_p * 1)(buf.data_ptr()),
-                                         (ctypes.c_size_t * 1)(nb), stream_ptr()), "xt_copy_async")
-    done.record()
-    return d[0], d[1]
+    return hn[0], hn[1]
 
 
 def pad2(t, rows, cols):

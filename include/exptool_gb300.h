@@ -231,7 +231,8 @@ int xt_cyl_accumulate_eval(void *handle, const double *x, const double *y, const
  * writes the coefficients over the host link, with no copy behind it).
  * xt_cyl_eval_sorted: eof.accumulated_eval_particles / eof.compute_forces
  * (eof.py:989-1144, 1263-1317) without density, for m1 <= m <= m2, from the
- * coefficients cos_c/sin_c ((mmax+1) x norder, device): binning, counting
+ * coefficients cos_c/sin_c ((mmax+1) x norder, device memory or host memory
+ * the device addresses, which the field stage then reads in place): binning, counting
  * sort, field and evaluation in cell order; outs = p0 p fr fp fz R (6 arrays
  * of n, any may be NULL), results in particle order. */
 int xt_cyl_accumulate_sorted(void *handle, const double *x, const double *y, const double *z, const double *m,
