@@ -81,3 +81,33 @@ def test_public_call_with_pinned_particles_matches_golden():
         assert np.max(np.abs(E.cos[m] - g["cos"][m])) <= 1e-10 * np.max(np.abs(g["cos"][m]))
     for k in range(6):
         assert np.max(np.abs(res[k] - g["aep"][k])) <= 1e-10 * np.max(np.abs(g["aep"][k]))
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_coefficients_in_page_locked_memory(precision):
+    """The sorted drop-in calls with their coefficients in page-locked host
+    memory: the accumulation's last kernel writes them there, and the
+    evaluation's field stage reads host coefficients in place.  The
+    accumulation agrees with the device-output call to the order of its sums;
+    the evaluation (no atomics) bit for bit with the same call on
+    device coefficients."""
+    import torch
+    from exptool_gb300 import device as dev
+    from exptool_gb300.basis import eof
+    g, path = _case()
+    table = eof.table_from_file(path)
+    xa, ya, za, ma = (np.ascontiguousarray(g[k], dtype=np.float64) for k in "xyzm")
+    d = [torch.from_numpy(a).to("cuda") for a in (xa, ya, za, ma)]
+    ref = dev.to_host(table.accumulate_sorted(*d, precision=precision))
+    got = table.accumulate_sorted(*d, precision=precision, host=True)
+    assert isinstance(got, np.ndarray) and got.shape == ref.shape
+    # FP32 path: the records' order within a cell (set by the binning's
+    # atomics) changes the FP32 run sums between calls
+    assert _close(got, ref, 1e-12 if precision == "f64" else 1e-6)
+    shape = (table.mmax + 1, table.norder)
+    hc, hs = dev.coef_pair(ref[0], ref[1], *shape)
+    res_host = dev.to_host(table.eval_sorted(*d[:3], hc, hs, precision=precision))
+    dc, ds = dev.coef_pair(torch.from_numpy(ref[0]).to("cuda"), torch.from_numpy(ref[1]).to("cuda"), *shape)
+    res_dev = dev.to_host(table.eval_sorted(*d[:3], dc, ds, precision=precision))
+    assert np.isfinite(res_dev).all()
+    assert np.array_equal(res_host, res_dev)
