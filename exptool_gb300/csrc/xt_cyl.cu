@@ -12,6 +12,7 @@
 // (cos/sin-weighted pot, rforce, zforce[, dens] per m), so each particle
 // reads 4 corners x (mmax+1) x 6 values instead of 4 x 6 x (mmax+1) x norder.
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <cmath>
 #include <mutex>
@@ -2011,9 +2012,19 @@ static int stage_copies(CylHandle* h, const FusedLayout& L, void* workspace, lon
                         double* const* outs, cudaStream_t st) {
   const double* stage = reinterpret_cast<const double*>(static_cast<char*>(workspace) + L.stage);
   const int npart = host_parts(n, qchunk);
+  // the five results as consecutive arrays of n (the stage's own layout): one
+  // 2D copy per part instead of five
+  // (pitches up to 2^31 - 1 bytes, the copy API's limit)
+  bool block = outs[0] != nullptr && (size_t)n * sizeof(double) <= (size_t)INT_MAX;
+  for (int k = 1; k < 5 && block; ++k) block = outs[k] == outs[0] + (size_t)k * n;
   for (int q = 0; q < npart; ++q) {
     XT_CUDA(cudaStreamWaitEvent(h->copy, h->qev[q], 0));
     const long long p0 = (long long)q * qchunk, np = q + 1 < npart ? qchunk : n - p0;
+    if (block) {
+      XT_CUDA(cudaMemcpy2DAsync(outs[0] + p0, (size_t)n * sizeof(double), stage + p0, (size_t)n * sizeof(double),
+                                (size_t)np * sizeof(double), 5, cudaMemcpyDefault, h->copy));
+      continue;
+    }
     for (int k = 0; k < 5; ++k)
       if (outs[k])
         XT_CUDA(cudaMemcpyAsync(outs[k] + p0, stage + (size_t)k * n + p0, (size_t)np * sizeof(double),
